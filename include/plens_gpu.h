@@ -1,0 +1,259 @@
+/*
+ * plens_gpu.h -- C ABI of the GB300 (sm_103a) implementation of PLENS's per-RK-stage
+ * right-hand side and time update.
+ *
+ * The reference has no plugin or FFI for this path: the path is the private method set of
+ * class PLENS (dgsem/plens.h:827-896), i.e. calc_rhs() (dgsem/plens.cc:3688-3779),
+ * calc_time_step() (dgsem/plens.cc:3810-3912), multiply_time_step_to_rhs()
+ * (dgsem/plens.cc:3925-3940) and update()/update_rk4() (dgsem/plens.cc:4334-4518), working on
+ * member PETSc vectors. Each entry point below names the reference routine it replaces.
+ *
+ * Conventions (the ABI is plain C: pointers, sizes, status codes; no exceptions cross it):
+ *  - P = degree+1; a cell holds P^3 GLL nodes numbered lexicographically, x fastest
+ *    (dgsem/cell_dof_info.h:60-88); the global dof index of node l of cell c is c*P^3 + l.
+ *  - Conservative state vectors are structure-of-arrays [5][ndof] in the order
+ *    (rho, rho u, rho v, rho w, rho E) (modelling/var_enums.h:25-41); auxiliary variables are
+ *    [9][ndof] in the order (txx, txy, txz, tyy, tyz, tzz, qx, qy, qz) (modelling/avars.h:14).
+ *  - Faces of a cell are numbered 0..5 = -x,+x,-y,+y,-z,+z of the reference cell; face-local
+ *    dof numbering follows dgsem/face_dof_info.h:92-150.
+ *  - Host pointers passed in are borrowed for the duration of the call and copied.
+ *  - One host thread per context; all device work runs on the context's own stream; every
+ *    call returns after its work completed unless its name ends in _async.
+ */
+#ifndef PLENS_GPU_H
+#define PLENS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define PLENS_GPU_OK 0
+#define PLENS_GPU_E_INVALID 1    /* bad argument or unsupported option (AssertThrow in the reference) */
+#define PLENS_GPU_E_CUDA 2       /* a CUDA runtime call failed */
+#define PLENS_GPU_E_POSITIVITY 3 /* rho<=0 or e<=0 at some dof (reference: std::exit, plens.cc:2531-2546) */
+#define PLENS_GPU_E_TIMEOUT 4    /* a bounded device wait gave up */
+
+/* ------------------------------------------------------------- flux scheme enums
+ * Same order as NavierStokes::inv_surf_flux_scheme / inv_vol_flux_scheme
+ * (modelling/navier_stokes.h:161-183). */
+enum plens_inv_surf_flux {
+    PLENS_ISF_HLLC = 0,
+    PLENS_ISF_RUSANOV = 1,
+    PLENS_ISF_AUSM_PLUS_UP = 2,
+    PLENS_ISF_RUSANOV_HLLC = 3,
+    PLENS_ISF_RUSANOV_AUSM_PLUS_UP = 4,
+    PLENS_ISF_MODIFIED_SW = 5,
+    PLENS_ISF_CHANDRASHEKHAR = 6,
+    PLENS_ISF_KENNEDY_GRUBER = 7,
+    PLENS_ISF_RUSANOV_KENNEDY_GRUBER = 8,
+    PLENS_ISF_ISMAIL_ROE = 9
+};
+enum plens_inv_vol_flux {
+    PLENS_IVF_CHANDRASHEKHAR = 0,
+    PLENS_IVF_KENNEDY_GRUBER = 1,
+    PLENS_IVF_ISMAIL_ROE = 2
+};
+
+/* ------------------------------------------------------------ boundary conditions
+ * One descriptor per boundary id; the types are the BCs:: classes of IBCs/. */
+enum plens_bc_type {
+    PLENS_BC_NONE = 0,
+    PLENS_BC_FREE = 1,              /* IBCs/free.cc:16-59 */
+    PLENS_BC_OUTFLOW = 2,           /* IBCs/outflow.cc:18-75 */
+    PLENS_BC_UNIFORM_INFLOW = 3,    /* IBCs/uniform_inflow.cc:23-77 */
+    PLENS_BC_UNIFORM_TEMP_WALL = 4, /* IBCs/uniform_temp_wall.cc:17-104 */
+    PLENS_BC_SYMMETRY = 5,          /* IBCs/symmetry.cc:17-98 */
+    PLENS_BC_EMPTY = 6,             /* IBCs/empty.cc:15-91 */
+    PLENS_BC_PERIODIC = 7,          /* IBCs/periodic.cc:18-165 */
+    PLENS_BC_INSULATED_WALL = 8,    /* IBCs/insulated_wall.cc:17-102 */
+    PLENS_BC_VARYING_INFLOW = 9,    /* IBCs/varying_inflow.cc:17-141 */
+    PLENS_BC_ZPG_INFLOW = 10        /* IBCs/zpg_inflow.cc:9-55 */
+};
+
+typedef struct plens_bc_desc {
+    int32_t type;       /* enum plens_bc_type */
+    int32_t expr_p;     /* varying inflow: expression index of p(x,y,z,t), else -1 */
+    int32_t expr_T;     /* varying inflow: expression index of T(x,y,z,t), else -1 */
+    int32_t expr_vel[3];/* varying inflow: expression indices of the velocity components */
+    double p;           /* prescribed p (outflow) */
+    double T;           /* prescribed T (uniform temp wall) */
+    double vel[3];      /* prescribed / wall velocity */
+    double cons[5];     /* prescribed conservative state (uniform inflow) */
+} plens_bc_desc;
+
+/* ------------------------------------------------------------------ expressions
+ * muparser-style expressions (deal.II FunctionParser in the reference) compiled on the host to
+ * a stack bytecode that the device and host evaluate identically. Variables: x,y,z,t. */
+typedef struct plens_expr_insn {
+    int32_t op;   /* opcode, see plens_gb300/csrc/common/expr.h */
+    int32_t arg;  /* variable index / arity / jump target */
+    double val;   /* literal */
+} plens_expr_insn;
+
+/* ------------------------------------------------------------------- parameters */
+enum plens_precision { PLENS_PRECISION_FP64 = 0, PLENS_PRECISION_MIXED = 1 };
+enum plens_sensor { PLENS_SENSOR_MODAL = 0, PLENS_SENSOR_LEARNED = 1 };
+
+typedef struct plens_params {
+    int32_t degree;            /* N (fe degree) */
+    /* gas model: NavierStokes (modelling/navier_stokes.h:141-507) */
+    double gamma, R, Pr, mu0, T0, S;   /* R = R0/M */
+    int32_t const_viscosity;   /* 1 reproduces the CONST_VISCOSITY build switch (mu = mu0) */
+    int32_t inv_surf_flux;     /* enum plens_inv_surf_flux */
+    int32_t inv_vol_flux;      /* enum plens_inv_vol_flux */
+    int32_t plens_2d;          /* 1 reproduces the PLENS_2D switch (rho w RHS zeroed) */
+    /* blender (dgsem/blender_calculator.cc, "blender parameters" subsection) */
+    int32_t blender_variable;  /* 0 pxrho, 1 p, 2 rho */
+    int32_t blender_function;  /* 0 Hennemann, 1 linear */
+    double threshold_factor, threshold_exp_factor, sharpness_factor, alpha_min, alpha_max;
+    int32_t expr_wall_blender_limit;   /* expression of t */
+    int32_t expr_vis_blending_region;  /* expression of x,y,z,t at cell centres */
+    int32_t expr_courant;              /* expression of t */
+    int32_t do_filtering;              /* TV filter (blender_calculator.cc:196-259) */
+    /* time integration */
+    int32_t rk_order;          /* 4: RK4(3)5[3R+]N; 3: SSP-RK3 */
+    /* precision / learned sensor (new; no counterpart in the reference) */
+    int32_t precision;         /* enum plens_precision */
+    int32_t sensor;            /* enum plens_sensor */
+    int32_t judge_every;       /* learned sensor: recompute the modal blender every k-th step */
+    double judge_alpha_tol;    /* learned sensor: per-cell alpha error that triggers fallback */
+    /* boundary conditions, indexed by boundary id (0..n_bc-1) */
+    int32_t n_bc;
+    const plens_bc_desc* bcs;
+    /* expression table */
+    int32_t n_expr;
+    const int32_t* expr_offset;  /* [n_expr] first instruction */
+    const int32_t* expr_length;  /* [n_expr] instruction count */
+    int32_t n_expr_insn;
+    const plens_expr_insn* expr_code;
+} plens_params;
+
+/* ------------------------------------------------------------ mesh description
+ * Everything the hot path needs from the reference's setup chain (read_mesh, set_dof_handler,
+ * form_neighbor_face_matchings, calc_metric_terms: dgsem/plens.cc:699-1009, 1574-1682),
+ * produced once on the host. */
+typedef struct plens_mesh_desc {
+    int32_t degree;
+    int64_t n_cells;
+    /* per-dof metric terms (dgsem/metric_terms.cc:67-142), SoA over ndof = n_cells*P^3 */
+    const double* detJ;         /* [ndof] */
+    const double* Ja;           /* [9][ndof]: Ja[(dir*3+comp)*ndof+dof] = (J a^dir)_comp */
+    const double* Jinv;         /* [9][ndof]: Jinv[(r*3+c)*ndof+dof] = d xi_r / d x_c */
+    /* per-cell data */
+    const double* h_min;        /* [n_cells] minimum vertex distance */
+    const double* cell_center;  /* [n_cells][3] vertex average */
+    const int32_t* cell_nbr;    /* [n_cells][6] interior neighbour, -1 on any boundary (periodic too) */
+    const int32_t* cell_face_bc;/* [n_cells][6] boundary id of boundary faces, -1 interior */
+    /* face tasks: each interior face once (owner = lower cell index), each boundary face
+     * (periodic included) once per side */
+    int64_t n_face_tasks;
+    const int32_t* ft_cell;      /* [n_face_tasks] */
+    const int32_t* ft_face;      /* [n_face_tasks] 0..5 */
+    const int32_t* ft_nbr_cell;  /* interior: neighbour; periodic: partner cell; else -1 */
+    const int32_t* ft_nbr_face;  /* interior/periodic: neighbour/partner face; else -1 */
+    const int32_t* ft_bc;        /* boundary id, -1 interior */
+    const int32_t* ft_nbr_fdof;  /* [n_face_tasks][P^2] matching face-local dof on the other side */
+    const double* ft_normal;     /* [n_face_tasks][P^2][3] unit outward normal of the owner side */
+    const double* ft_xyz;        /* [n_face_tasks][P^2][3] face dof location */
+} plens_mesh_desc;
+
+typedef struct plens_ctx plens_ctx;
+
+/* ------------------------------------------------------------------ lifecycle */
+
+/* Replaces the device-facing half of the setup chain (set_sol_vecs, calc_metric_terms, set_BC:
+ * dgsem/plens.cc:1025-1097, 1646-1682, 1219-1440): uploads the mesh description, the parameters
+ * and the BC descriptors, allocates all device buffers. */
+int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* params, plens_ctx** out);
+int plens_gpu_destroy(plens_ctx* ctx);
+/* Message of the last failed call on this context (never NULL). */
+const char* plens_gpu_last_error(const plens_ctx* ctx);
+/* Number of CUDA kernels this library launched on the context so far. */
+int64_t plens_gpu_kernel_launches(const plens_ctx* ctx);
+/* The cudaStream_t the context launches on (as an opaque pointer). */
+void* plens_gpu_stream(const plens_ctx* ctx);
+
+/* Kernel timing on the context stream: when enabled, CUDA events bracket every launch of the
+ * per-cell volume kernel (the dominant kernel); plens_gpu_kernel_timing returns the summed
+ * elapsed milliseconds and the launch count since the last reset. */
+int plens_gpu_set_kernel_timing(plens_ctx* ctx, int enable);
+int plens_gpu_kernel_timing(plens_ctx* ctx, double* volume_ms, int64_t* volume_launches);
+
+/* ----------------------------------------------------------------- state I/O
+ * Replaces the g_cvars / gcrk_cvars buffer copies of PLENS::update (dgsem/plens.cc:4487-4514). */
+int plens_gpu_set_state(plens_ctx* ctx, const double* U /* [5][ndof] */);
+int plens_gpu_get_state(plens_ctx* ctx, double* U /* [5][ndof] */);
+/* Simulation clock kept on the device (PLENS::cur_time, PLENS::n_time_steps). */
+int plens_gpu_set_time(plens_ctx* ctx, double t, int64_t n_steps);
+int plens_gpu_get_time(plens_ctx* ctx, double* t, int64_t* n_steps, double* last_dt);
+
+/* ----------------------------------------------------------------- hot path */
+
+/* One right-hand-side evaluation at the current state and time: PLENS::calc_rhs
+ * (dgsem/plens.cc:3688-3779) including assert_positivity, calc_aux_vars, calc_blender and
+ * calc_surf_flux. R_out ([5][ndof], may be NULL) receives the residual before the time-step
+ * multiplication. Returns PLENS_GPU_E_POSITIVITY if assert_positivity would have aborted. */
+int plens_gpu_rhs(plens_ctx* ctx, double* R_out);
+
+/* PLENS::calc_time_step (dgsem/plens.cc:3810-3912) at the current state and time, global time
+ * stepping: dt = min over dofs of Co/(N^1.5 (max_k (Jinv^T u)_k + a/h + N^2 mu/(h^2 rho))). */
+int plens_gpu_time_step(plens_ctx* ctx, double* dt_out);
+
+/* n_steps calls of PLENS::update (dgsem/plens.cc:4484-4518): each step computes dt on the device
+ * at stage 1, clips it to end_time - t (dgsem/plens.cc:4341), runs the RK stages
+ * (update_rk4 dgsem/plens.cc:4334-4403 or update_rk3 4420-4475) and advances the device clock.
+ * Steps stop early once t >= end_time. The _async form returns without synchronising; errors
+ * raised by the device (positivity, learned-sensor fallback counters) are reported by the next
+ * synchronising call. */
+int plens_gpu_advance(plens_ctx* ctx, int64_t n_steps, double end_time);
+int plens_gpu_advance_async(plens_ctx* ctx, int64_t n_steps, double end_time);
+int plens_gpu_synchronize(plens_ctx* ctx);
+
+/* Per-cell scalars of the last RHS: PLENS::gcrk_alpha, gcrk_alpha_d, loc_time_steps. */
+int plens_gpu_get_cell_scalars(plens_ctx* ctx, double* alpha, double* alpha_d, double* dt_cell);
+/* Auxiliary variables of the last viscous RHS ([9][ndof]): PLENS::gcrk_avars. */
+int plens_gpu_get_avars(plens_ctx* ctx, double* avars);
+/* First dof that failed the positivity check of the last failing call (-1 if none). */
+int plens_gpu_first_bad_dof(const plens_ctx* ctx, int64_t* dof);
+
+/* ----------------------------------------------------- learned troubled-cell sensor
+ * New component (no counterpart in the reference): an MLP (64 -> 64 -> 64 -> 1, GELU,
+ * sigmoid*alpha_max) that replaces BlenderCalculator::get_blender and the neighbour smoothing
+ * (dgsem/blender_calculator.cc:123-177, dgsem/plens.cc:2926-2947). Weights are FP32, laid out
+ * W1[64][64], b1[64], W2[64][64], b2[64], W3[64], b3[1] (row-major, out x in). */
+#define PLENS_MLP_IN 64
+#define PLENS_MLP_HIDDEN 64
+#define PLENS_MLP_N_PARAMS (64 * 64 + 64 + 64 * 64 + 64 + 64 + 1)
+int plens_gpu_set_sensor_weights(plens_ctx* ctx, const float* params /* [PLENS_MLP_N_PARAMS] */);
+/* Learned-sensor statistics: steps judged, judged steps that fell back, max per-cell alpha
+ * error seen, and the number of cells the subcell kernel ran on in the last RHS. */
+int plens_gpu_sensor_stats(plens_ctx* ctx, int64_t* judged, int64_t* fallbacks,
+                           double* max_alpha_err, int64_t* lo_cells_last);
+/* Appends (per-cell nodal rho*p interpolated to 4^3 GLL nodes -> final alpha) training pairs of
+ * the current state to host buffers: x [n_cells][64] FP32, y [n_cells] FP32. */
+int plens_gpu_sensor_pairs(plens_ctx* ctx, float* x, float* y);
+
+/* MLP training on the device with the library's own forward, backward and Adam kernels.
+ * x: [n][64] FP32 (host), y: [n] FP32 (host). params: [PLENS_MLP_N_PARAMS] in/out (host).
+ * Mini-batch SGD with Adam(lr, beta1=0.9, beta2=0.999, eps=1e-8); the sample order of each
+ * epoch is a permutation drawn from `seed`. loss_out[epochs] receives the mean-squared error
+ * of each epoch (may be NULL). Standalone: needs no context. */
+int plens_gpu_mlp_train(const float* x, const float* y, int64_t n, float* params,
+                        int32_t epochs, int32_t batch, float lr, float alpha_max,
+                        uint64_t seed, float* loss_out);
+/* One forward+backward pass over a batch, for gradient checks: loss (mean squared error) and
+ * the gradient of the loss with respect to every parameter. */
+int plens_gpu_mlp_loss_grad(const float* x, const float* y, int64_t n, const float* params,
+                            float alpha_max, float* loss, float* grad /* [PLENS_MLP_N_PARAMS] */);
+/* Inference only: alpha for n samples. */
+int plens_gpu_mlp_infer(const float* x, int64_t n, const float* params, float alpha_max,
+                        float* alpha /* [n] */);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PLENS_GPU_H */

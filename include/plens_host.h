@@ -1,0 +1,54 @@
+/*
+ * plens_host.h -- C ABI of the host-side setup chain: builds, from the reference's input.prm
+ * format, the mesh description, parameters and initial state that plens_gpu.h consumes.
+ *
+ * Replaces the reference's setup chain PLENS::PLENS / declare_parameters / read_mesh / set_NS /
+ * set_dof_handler / set_sol_vecs / set_IC / set_BC / set_blender / read_time_settings
+ * (dgsem/plens.cc:13-1499, main.cc:96-106). Host only: loads and runs without a GPU.
+ */
+#ifndef PLENS_HOST_H
+#define PLENS_HOST_H
+
+#include <stdint.h>
+
+#include "plens_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct plens_case plens_case;
+
+/* Parses prm text (input.prm contents), builds mesh, metric terms, face tables, BCs and the
+ * initial condition. base_dir resolves relative file names (mesh, IC file). Returns 0 or 1; on
+ * failure *out is NULL and plens_case_last_error() holds the message. */
+int plens_case_create(const char* prm_text, const char* base_dir, int mapping_degree,
+                      int fe_degree, plens_case** out);
+const char* plens_case_last_error(void);
+void plens_case_destroy(plens_case* c);
+
+const plens_mesh_desc* plens_case_mesh(const plens_case* c);
+const plens_params* plens_case_params(const plens_case* c);
+/* Mutable parameters (precision / sensor switches may be flipped before plens_gpu_create). */
+plens_params* plens_case_params_mut(plens_case* c);
+int64_t plens_case_n_cells(const plens_case* c);
+int64_t plens_case_n_dofs(const plens_case* c);
+/* Initial state [5][ndof] (PLENS::set_IC) and dof locations [3][ndof]. */
+int plens_case_initial_state(const plens_case* c, double* U);
+int plens_case_dof_xyz(const plens_case* c, double* xyz);
+double plens_case_start_time(const plens_case* c);
+double plens_case_end_time(const plens_case* c);
+/* Evaluates expression `idx` of the case's expression table. */
+double plens_case_eval_expr(const plens_case* c, int32_t idx, double x, double y, double z, double t);
+/* All parameters with their values (ParameterHandler::print_parameters); valid until destroy. */
+const char* plens_case_prm_echo(const plens_case* c);
+
+/* Stand-alone helpers for the known-answer tests. */
+int plens_expr_eval_string(const char* src, double x, double y, double z, double t, double* out);
+int plens_gll_1d(int n_points, double* nodes, double* weights);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PLENS_HOST_H */

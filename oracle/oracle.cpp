@@ -1,0 +1,1349 @@
+// oracle.cpp -- TEST INFRASTRUCTURE. A plain FP64 CPU restatement of PLENS's per-RK-stage
+// right-hand side and time update, written to follow the reference routine by routine (each
+// function cites the file:line it restates). It is the checker for the CUDA path and the timed
+// CPU baseline; only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm
+// load it. Nothing in the product path calls it.
+//
+// Parity pin: the reference (deal.II 9.3 + PETSc + p4est + MPI) cannot be built in this
+// environment, and its own tests ship no golden vectors, so numeric RHS parity with a deal.II run
+// is unpinned. The restatement is pinned instead to the reference's known-answer and property
+// checks (face dof maps, rotated-box metric terms, rotational invariance of the surface flux,
+// alpha = 0 for a linear field), which tests/ assert against this library.
+//
+// Threading: OpenMP over cells / face tasks; every write goes to a slot owned by exactly one
+// iteration and the only reductions are min() of dt and of the first failing dof, so results do
+// not depend on the thread count.
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "plens_gpu.h"
+#include "../plens_gb300/csrc/common/expr.h"
+
+namespace {
+
+using State = std::array<double, 5>;
+using Avars = std::array<double, 9>;
+using Vec = std::array<double, 3>;
+
+inline double dot(const Vec& a, const Vec& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline double norm(const Vec& a) { return std::sqrt(dot(a, a)); }
+
+// ============================================================================ NavierStokes
+// modelling/navier_stokes.{h,cc}
+struct NavierStokes {
+    double gma, R, Pr, mu0, T0, S;
+    bool const_visc;
+    int isf, ivf;
+    double fb = 1.0;  // flux blender value
+
+    bool is_inviscid() const { return mu0 < 1e-16; }                      // h:440
+    void set_flux_blender_value(double a) { fb = (a <= 0) ? 0 : (a <= 1 ? a : 1); }  // h:448-453
+    double get_cv() const { return R / (gma - 1); }
+    double get_mu(double T) const                                        // h:348-355
+    {
+        if (const_visc) return mu0;
+        return mu0 * std::pow(T / T0, 1.5) * (T0 + S) / (T + S);
+    }
+    double get_k(double mu) const { return mu * R * gma / ((gma - 1) * Pr); }  // h:360
+    static double get_e(const State& c)                                    // cc:349-359
+    {
+        double ske = 0;
+        for (int d = 0; d < 3; ++d) ske += c[1 + d] * c[1 + d];
+        const double ri = 1 / c[0];
+        ske *= 0.5 * ri;
+        return (c[4] - ske) * ri;
+    }
+    double get_p(const State& c) const                                     // cc:375-383
+    {
+        double ske = 0;
+        for (int d = 0; d < 3; ++d) ske += c[1 + d] * c[1 + d];
+        ske *= 0.5 / c[0];
+        return (gma - 1) * (c[4] - ske);
+    }
+    double get_a(const State& c) const { return std::sqrt(gma * get_p(c) / c[0]); }  // cc:395
+    double get_M(const State& c) const                                     // cc:405-411
+    {
+        double sp = 0;
+        const double ri = 1 / c[0];
+        for (int d = 0; d < 3; ++d) sp += (c[1 + d] * c[1 + d]) * (ri * ri);
+        return std::sqrt(sp) / get_a(c);
+    }
+    void prim_to_cons(double rho, const Vec& v, double p, State& c) const  // h:366-379
+    {
+        c[0] = rho;
+        c[4] = p / (gma - 1);
+        for (int d = 0; d < 3; ++d) {
+            c[1 + d] = rho * v[d];
+            c[4] += 0.5 * rho * v[d] * v[d];
+        }
+    }
+    void cons_to_entropy(const State& c, State& ev) const                  // h:404-430
+    {
+        const double p = get_p(c);
+        const double s = std::log(p) - gma * std::log(c[0]);
+        const double beta = 0.5 * c[0] / p;
+        const double ri = 1 / c[0];
+        Vec v;
+        for (int d = 0; d < 3; ++d) v[d] = c[1 + d] * ri;
+        ev[0] = (gma - s) / (gma - 1) - beta * dot(v, v);
+        for (int d = 0; d < 3; ++d) ev[1 + d] = 2 * beta * v[d];
+        ev[4] = -2 * beta;
+    }
+    static double log_avg(double xl, double xr)                            // h:494-501
+    {
+        const double xi = xl / xr, f = (xi - 1) / (xi + 1), u = f * f,
+                     F = (u < 1e-2 ? 1 + u / 3 + u * u / 5 + u * u * u / 7 : 0.5 * std::log(xi) / f);
+        return 0.5 * (xl + xr) / F;
+    }
+    void get_inv_flux(const State& c, const Vec& dir, State& f) const      // cc:424-442
+    {
+        Vec v;
+        const double ri = 1.0 / c[0];
+        for (int d = 0; d < 3; ++d) v[d] = c[1 + d] * ri;
+        const double p = get_p(c);
+        const double vn = dot(v, dir);
+        f[0] = c[0] * vn;
+        for (int d = 0; d < 3; ++d) f[1 + d] = vn * c[1 + d] + p * dir[d];
+        f[4] = (c[4] + p) * vn;
+    }
+
+    // ---------------------------------------------------------- x-direction surface fluxes
+    void hllc_xflux(const State& l, const State& r, State& f) const        // cc:936-1033
+    {
+        const Vec xdir{{1, 0, 0}};
+        const double pl = get_p(l), pr = get_p(r);
+        const double pmin = std::min(pl, pr), pmax = std::max(pl, pr);
+        const double ul = l[1] / l[0], ur = r[1] / r[0];
+        const double al = std::sqrt(gma * pl / l[0]), ar = std::sqrt(gma * pr / r[0]);
+        const double p_pvrs = 0.5 * (pl + pr) - 0.5 * (ur - ul) * 0.5 * (l[0] + r[0]) * 0.5 * (al + ar);
+        double ps;
+        if (pmax / pmin < 2 && pmin <= p_pvrs && p_pvrs <= pmax) {
+            ps = p_pvrs;
+        } else if (p_pvrs < pmin) {
+            const double z = (gma - 1) / (2 * gma);
+            ps = std::pow(((al + ar) - (gma - 1) / 2 * (ur - ul)) / (al / std::pow(pl, z) + ar / std::pow(pr, z)), 1 / z);
+        } else {
+            const double p0 = std::max(0.0, p_pvrs);
+            const double gl = std::sqrt(2 / ((gma + 1) * l[0]) / (p0 + (gma - 1) / (gma + 1) * pl)),
+                         gr = std::sqrt(2 / ((gma + 1) * r[0]) / (p0 + (gma - 1) / (gma + 1) * pr));
+            ps = (gl * pl + gr * pr - (ur - ul)) / (gl + gr);
+        }
+        const double ql = (ps <= pl ? 1 : std::sqrt(1 + (gma + 1) / (2 * gma) * (ps / pl - 1))),
+                     qr = (ps <= pr ? 1 : std::sqrt(1 + (gma + 1) / (2 * gma) * (ps / pr - 1)));
+        const double sl = ul - al * ql, sr = ur + ar * qr;
+        const double s = (pr - pl + l[1] * (sl - ul) - r[1] * (sr - ur)) / (l[0] * (sl - ul) - r[0] * (sr - ur));
+        if (sl > 0) {
+            get_inv_flux(l, xdir, f);
+        } else if (s > 0) {
+            const double t = (sl - ul) / (sl - s);
+            const State ss = {t * l[0], t * l[0] * s, t * l[2], t * l[3], t * (l[4] + (s - ul) * (l[0] * s + pl / (sl - ul)))};
+            State lf;
+            get_inv_flux(l, xdir, lf);
+            for (int v = 0; v < 5; ++v) f[v] = lf[v] + sl * (ss[v] - l[v]);
+        } else if (sr > 0) {
+            const double t = (sr - ur) / (sr - s);
+            const State ss = {t * r[0], t * r[0] * s, t * r[2], t * r[3], t * (r[4] + (s - ur) * (r[0] * s + pr / (sr - ur)))};
+            State rf;
+            get_inv_flux(r, xdir, rf);
+            for (int v = 0; v < 5; ++v) f[v] = rf[v] + sr * (ss[v] - r[v]);
+        } else {
+            get_inv_flux(r, xdir, f);
+        }
+    }
+    void rusanov_xflux(const State& l, const State& r, State& f) const     // cc:1044-1059
+    {
+        const Vec xdir{{1, 0, 0}};
+        State lf, rf;
+        const double al = get_a(l), ar = get_a(r);
+        const double ul = l[1] / l[0], ur = r[1] / r[0];
+        get_inv_flux(l, xdir, lf);
+        get_inv_flux(r, xdir, rf);
+        const double S = std::max(std::fabs(ul) + al, std::fabs(ur) + ar);
+        for (int v = 0; v < 5; ++v) f[v] = 0.5 * (lf[v] + rf[v]) - 0.5 * S * (r[v] - l[v]);
+    }
+    // AUSM+-up (cc:1070-1121, ausm_functions.h:11-88). `alpha = 3/16*(...)` is an integer
+    // division in the reference and therefore 0; reproduced.
+    static double msp1(double M) { return 0.5 * (M + std::fabs(M)); }
+    static double msn1(double M) { return 0.5 * (M - std::fabs(M)); }
+    static double msp2(double M) { return 0.25 * (M + 1) * (M + 1); }
+    static double msn2(double M) { return -0.25 * (M - 1) * (M - 1); }
+    static double msp4(double M) { return std::fabs(M) >= 1 ? msp1(M) : msp2(M) * (1 - 16 * 0.125 * msn2(M)); }
+    static double msn4(double M) { return std::fabs(M) >= 1 ? msn1(M) : msn2(M) * (1 + 16 * 0.125 * msp2(M)); }
+    static double psp5(double M, double a) { return std::fabs(M) >= 1 ? msp1(M) / M : msp2(M) * ((2 - M) - 16 * a * M * msn2(M)); }
+    static double psn5(double M, double a) { return std::fabs(M) >= 1 ? msn1(M) / M : msn2(M) * ((-2 - M) + 16 * a * M * msp2(M)); }
+    void ausm_plus_up_xflux(const State& l, const State& r, State& f) const
+    {
+        const double pl = get_p(l), pr = get_p(r);
+        Vec vl, vr;
+        for (int d = 0; d < 3; ++d) { vl[d] = l[1 + d] / l[0]; vr[d] = r[1 + d] / r[0]; }
+        const double Hl = (l[4] + pl) / l[0], Hr = (r[4] + pr) / r[0];
+        const double a12 = 0.5 * (get_a(l) + get_a(r));
+        const double Ml = vl[0] / a12, Mr = vr[0] / a12;
+        const double Mavgsq = 0.5 * (Ml * Ml + Mr * Mr);
+        const double Mo = std::sqrt(std::min(1.0, std::max(Mavgsq, 0.3 * 0.3)));
+        const double fa = Mo * (2 - Mo), alpha = 3 / 16 * (-4 + 5 * fa * fa);
+        const double M12 = msp4(Ml) + msn4(Mr) -
+                           0.25 / fa * std::max(1 - 1.0 * Mavgsq, 0.0) * 2 * (pr - pl) / (a12 * a12 * (l[0] + r[0]));
+        const double ppos = psp5(Ml, alpha), pneg = psn5(Mr, alpha);
+        const double p12 = ppos * pl + pneg * pr - 0.75 * fa * ppos * pneg * (l[0] + r[0]) * a12 * (vr[0] - vl[0]);
+        if (M12 > 0) {
+            const double m12 = a12 * M12 * l[0];
+            f[0] = m12; f[1] = m12 * vl[0] + p12; f[2] = m12 * vl[1]; f[3] = m12 * vl[2]; f[4] = m12 * Hl;
+        } else {
+            const double m12 = a12 * M12 * r[0];
+            f[0] = m12; f[1] = m12 * vr[0] + p12; f[2] = m12 * vr[1]; f[3] = m12 * vr[2]; f[4] = m12 * Hr;
+        }
+    }
+    // x-direction eigenvector matrices (cc:641-678, 780-825)
+    void get_xK(const Vec& v, double a, double H, double K[5][5]) const
+    {
+        K[0][0] = 1; for (int d = 0; d < 3; ++d) K[1 + d][0] = v[d]; K[1][0] -= a; K[4][0] = H - v[0] * a;
+        K[0][1] = 1; for (int d = 0; d < 3; ++d) K[1 + d][1] = v[d]; K[4][1] = 0.5 * dot(v, v);
+        K[0][2] = 0; K[1][2] = 0; K[2][2] = 1; K[3][2] = 0; K[4][2] = v[1];
+        K[0][3] = 0; K[1][3] = 0; K[2][3] = 0; K[3][3] = 1; K[4][3] = v[2];
+        K[0][4] = 1; for (int d = 0; d < 3; ++d) K[1 + d][4] = v[d]; K[1][4] += a; K[4][4] = H + v[0] * a;
+    }
+    void get_xKinv(const Vec& v, double a, double H, double Ki[5][5]) const
+    {
+        const double t = 1 / (gma - 1);
+        Ki[0][0] = H + a * (v[0] - a) * t; for (int d = 0; d < 3; ++d) Ki[0][1 + d] = -v[d]; Ki[0][1] -= a * t; Ki[0][4] = 1;
+        Ki[1][0] = 2 * (2 * a * a * t - H); for (int d = 0; d < 3; ++d) Ki[1][1 + d] = 2 * v[d]; Ki[1][4] = -2;
+        Ki[2][0] = -2 * v[1] * a * a * t; Ki[2][1] = 0; Ki[2][2] = 2 * a * a * t; Ki[2][3] = 0; Ki[2][4] = 0;
+        Ki[3][0] = -2 * v[2] * a * a * t; Ki[3][1] = 0; Ki[3][2] = 0; Ki[3][3] = 2 * a * a * t; Ki[3][4] = 0;
+        Ki[4][0] = H - a * (v[0] + a) * t; for (int d = 0; d < 3; ++d) Ki[4][1 + d] = -v[d]; Ki[4][1] += a * t; Ki[4][4] = 1;
+        const double factor = 0.5 * (gma - 1) / (a * a);
+        for (int i = 0; i < 5; ++i) for (int j = 0; j < 5; ++j) Ki[i][j] *= factor;
+    }
+    void chandrashekhar_xflux(const State& l, const State& r, State& f) const  // cc:1250-1318
+    {
+        const double pl = get_p(l), pr = get_p(r);
+        const double betal = 0.5 * l[0] / pl, betar = 0.5 * r[0] / pr, beta_ln = log_avg(betal, betar);
+        const double p_hat = 0.5 * (l[0] + r[0]) / (betal + betar);
+        const double rho_ln = log_avg(l[0], r[0]);
+        Vec va, vsq, vl, vr;
+        const double ril = 1 / l[0], rir = 1 / r[0];
+        for (int d = 0; d < 3; ++d) {
+            vl[d] = l[1 + d] * ril; vr[d] = r[1 + d] * rir;
+            va[d] = 0.5 * (vl[d] + vr[d]); vsq[d] = 0.5 * (vl[d] * vl[d] + vr[d] * vr[d]);
+        }
+        double H = 0.5 / ((gma - 1) * beta_ln) + p_hat / rho_ln;
+        for (int d = 0; d < 3; ++d) H += va[d] * va[d] - 0.5 * vsq[d];
+        f[0] = rho_ln * va[0];
+        f[1] = rho_ln * va[0] * va[0] + p_hat;
+        f[2] = rho_ln * va[0] * va[1];
+        f[3] = rho_ln * va[0] * va[2];
+        f[4] = rho_ln * va[0] * H;
+        const double sl = std::sqrt(l[0]), sr = std::sqrt(r[0]);
+        Vec vi;
+        for (int d = 0; d < 3; ++d) vi[d] = 1 / (sl + sr) * (sl * vl[d] + sr * vr[d]);
+        const double Hi = ((l[4] + pl) / sl + (r[4] + pr) / sr) / (sl + sr);
+        const double ai = std::sqrt((gma - 1) * (Hi - 0.5 * dot(vi, vi)));
+        double K[5][5], Ki[5][5], A[5][5] = {};
+        get_xK(vi, ai, Hi, K);
+        get_xKinv(vi, ai, Hi, Ki);
+        const double uabs = std::fabs(vi[0]), lrus = uabs + ai, l2 = fb * lrus + (1 - fb) * uabs;
+        const double eig[5] = {lrus, l2, l2, l2, lrus};
+        for (int i = 0; i < 5; ++i) for (int j = 0; j < 5; ++j) for (int k = 0; k < 5; ++k) A[i][j] += K[i][k] * eig[k] * Ki[k][j];
+        for (int i = 0; i < 5; ++i) for (int j = 0; j < 5; ++j) f[i] -= 0.5 * A[i][j] * (r[j] - l[j]);
+    }
+    void inv_surf_xflux(const State& l, const State& r, State& f) const
+    {
+        switch (isf) {
+        case PLENS_ISF_HLLC: hllc_xflux(l, r, f); return;
+        case PLENS_ISF_RUSANOV: rusanov_xflux(l, r, f); return;
+        case PLENS_ISF_AUSM_PLUS_UP: ausm_plus_up_xflux(l, r, f); return;
+        case PLENS_ISF_RUSANOV_HLLC: {                                     // cc:1132-1140
+            State a, b;
+            rusanov_xflux(l, r, a);
+            hllc_xflux(l, r, b);
+            for (int v = 0; v < 5; ++v) f[v] = fb * a[v] + (1 - fb) * b[v];
+            return;
+        }
+        case PLENS_ISF_RUSANOV_AUSM_PLUS_UP: {                             // cc:1150-1158
+            State a, b;
+            rusanov_xflux(l, r, a);
+            ausm_plus_up_xflux(l, r, b);
+            for (int v = 0; v < 5; ++v) f[v] = fb * a[v] + (1 - fb) * b[v];
+            return;
+        }
+        case PLENS_ISF_CHANDRASHEKHAR: chandrashekhar_xflux(l, r, f); return;
+        default: for (int v = 0; v < 5; ++v) f[v] = NAN; return;
+        }
+    }
+    // rotation to the normal frame (cc:482-569)
+    void get_inv_surf_flux(const State& o, const State& n, const Vec& normal, State& f) const
+    {
+        const Vec m0{{0.0 * normal[2] - 0.0 * normal[1], 0.0 * normal[0] - 1.0 * normal[2], 1.0 * normal[1] - 0.0 * normal[0]}};
+        Vec m = m0;
+        const double M = norm(m);
+        double R[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        if (M > 1e-3) {
+            for (int d = 0; d < 3; ++d) m[d] /= M;
+            const double c = 1 * normal[0] + 0 * normal[1] + 0 * normal[2], t = 1 - c, s = std::sqrt(1 - c * c);
+            R[0][0] = t * m[0] * m[0] + c;        R[0][1] = t * m[0] * m[1] - s * m[2]; R[0][2] = t * m[0] * m[2] + s * m[1];
+            R[1][0] = t * m[0] * m[1] + s * m[2]; R[1][1] = t * m[1] * m[1] + c;        R[1][2] = t * m[1] * m[2] - s * m[0];
+            R[2][0] = t * m[0] * m[2] - s * m[1]; R[2][1] = t * m[1] * m[2] + s * m[0]; R[2][2] = t * m[2] * m[2] + c;
+        } else {
+            const double dgl = (normal[0] < 0) ? -1 : 1;
+            for (int d = 0; d < 3; ++d) R[d][d] = dgl;
+        }
+        Vec om{{o[1], o[2], o[3]}}, nm{{n[1], n[2], n[3]}}, omr{{0, 0, 0}}, nmr{{0, 0, 0}};
+        for (int row = 0; row < 3; ++row)
+            for (int col = 0; col < 3; ++col) {
+                omr[row] += R[col][row] * om[col];
+                nmr[row] += R[col][row] * nm[col];
+            }
+        const State orr = {o[0], omr[0], omr[1], omr[2], o[4]}, nr = {n[0], nmr[0], nmr[1], nmr[2], n[4]};
+        State fr;
+        inv_surf_xflux(orr, nr, fr);
+        Vec mf{{0, 0, 0}};
+        for (int row = 0; row < 3; ++row)
+            for (int col = 0; col < 3; ++col) mf[row] += R[row][col] * fr[1 + col];
+        f[0] = fr[0];
+        for (int d = 0; d < 3; ++d) f[1 + d] = mf[d];
+        f[4] = fr[4];
+    }
+    // volume fluxes
+    void chandrashekhar_vol_flux(const State& c1, const State& c2, const Vec& dir, State& f) const  // cc:1510-1542
+    {
+        const double p1 = get_p(c1), p2 = get_p(c2);
+        const double b1 = 0.5 * c1[0] / p1, b2 = 0.5 * c2[0] / p2, bln = log_avg(b1, b2);
+        const double p_hat = 0.5 * (c1[0] + c2[0]) / (b1 + b2);
+        const double rho_ln = log_avg(c1[0], c2[0]);
+        Vec va, vsq;
+        const double r1 = 1 / c1[0], r2 = 1 / c2[0];
+        for (int d = 0; d < 3; ++d) {
+            const double v1 = c1[1 + d] * r1, v2 = c2[1 + d] * r2;
+            va[d] = 0.5 * (v1 + v2);
+            vsq[d] = 0.5 * (v1 * v1 + v2 * v2);
+        }
+        double H = 0.5 / ((gma - 1) * bln) + p_hat / rho_ln;
+        for (int d = 0; d < 3; ++d) H += va[d] * va[d] - 0.5 * vsq[d];
+        const double vn = dot(va, dir);
+        f[0] = vn * rho_ln;
+        for (int d = 0; d < 3; ++d) f[1 + d] = rho_ln * vn * va[d] + p_hat * dir[d];
+        f[4] = rho_ln * vn * H;
+    }
+    void kennedy_gruber_vol_flux(const State& c1, const State& c2, const Vec& dir, State& f) const  // cc:1549-1574
+    {
+        Vec va, v1, v2;
+        const double r1 = 1 / c1[0], r2 = 1 / c2[0];
+        for (int d = 0; d < 3; ++d) { v1[d] = c1[1 + d] * r1; v2[d] = c2[1 + d] * r2; va[d] = 0.5 * (v1[d] + v2[d]); }
+        const double ra = 0.5 * (c1[0] + c2[0]);
+        const double e1 = get_e(c1), e2 = get_e(c2);
+        const double Ea = 0.5 * (e1 + e2 + 0.5 * (dot(v1, v1) + dot(v2, v2)));
+        const double pa = (gma - 1) * 0.5 * (c1[0] * e1 + c2[0] * e2);
+        const double vn = dot(va, dir);
+        f[0] = vn * ra;
+        for (int d = 0; d < 3; ++d) f[1 + d] = ra * vn * va[d] + pa * dir[d];
+        f[4] = vn * (ra * Ea + pa);
+    }
+    void ismail_roe_vol_flux(const State& c1, const State& c2, const Vec& dir, State& f) const  // cc:1590-1617
+    {
+        const double gs = std::sqrt(gma);
+        const double a1 = get_a(c1), a2 = get_a(c2);
+        const double z11 = gs / a1, z12 = gs / a2, z51 = c1[0] * a1 / gs, z52 = c2[0] * a2 / gs;
+        const double z5ln = log_avg(z51, z52);
+        const double rh = 0.5 * (z11 + z12) * z5ln;
+        const double p1h = (z51 + z52) / (z11 + z12), p2h = 0.5 * ((gma + 1) * z5ln / log_avg(z11, z12) + (gma - 1) * p1h) / (gma);
+        double hh = gma * p2h / ((gma - 1) * rh);
+        Vec vh;
+        for (int d = 0; d < 3; ++d) {
+            const double v1 = c1[1 + d] / c1[0], v2 = c2[1 + d] / c2[0];
+            vh[d] = (z11 * v1 + z12 * v2) / (z11 + z12);
+            hh += 0.5 * (vh[d] * vh[d]);
+        }
+        const double vn = dot(vh, dir);
+        f[0] = rh * vn;
+        for (int d = 0; d < 3; ++d) f[1 + d] = rh * vh[d] * vn + p1h * dir[d];
+        f[4] = rh * vn * hh;
+    }
+    void get_inv_vol_flux(const State& c1, const State& c2, const Vec& dir, State& f) const
+    {
+        if (ivf == PLENS_IVF_CHANDRASHEKHAR) chandrashekhar_vol_flux(c1, c2, dir, f);
+        else if (ivf == PLENS_IVF_KENNEDY_GRUBER) kennedy_gruber_vol_flux(c1, c2, dir, f);
+        else ismail_roe_vol_flux(c1, c2, dir, f);
+    }
+    static void get_dif_flux(const State& c, const Avars& av, const Vec& dir, State& f)  // cc:599-624
+    {
+        double st[3][3];
+        int i = 0;
+        for (int row = 0; row < 3; ++row)
+            for (int col = row; col < 3; ++col) {
+                st[row][col] = av[i];
+                if (col != row) st[col][row] = av[i];
+                ++i;
+            }
+        Vec mf{{0, 0, 0}};
+        for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) mf[a] += st[a][b] * dir[b];
+        f[0] = 0;
+        f[4] = 0;
+        const double ri = 1.0 / c[0];
+        for (int d = 0; d < 3; ++d) {
+            const double v = c[1 + d] * ri;
+            f[1 + d] = mf[d];
+            f[4] += -av[6 + d] * dir[d] + v * mf[d];
+        }
+    }
+};
+
+// ============================================================================== solver
+
+struct Oracle {
+    plens_mesh_desc M{};
+    plens_params Pm{};
+    // owned copies of the borrowed arrays
+    std::vector<double> detJ, Ja, Jinv, h_min, center, ft_normal, ft_xyz;
+    std::vector<int32_t> cell_nbr, cell_face_bc, ft_cell, ft_face, ft_nbr_cell, ft_nbr_face, ft_bc, ft_nbr_fdof;
+    std::vector<plens_bc_desc> bcs;
+    std::vector<int32_t> expr_off, expr_len;
+    std::vector<plens_expr_insn> expr_code;
+
+    NavierStokes ns{};
+    int N = 1, P = 2, P2 = 4, P3 = 8;
+    int64_t nc = 0, nd = 0;
+    std::vector<double> w, D, Q;         // 1D GLL weights, D_ij = l_j'(xi_i), Q = diag(w) D
+    std::vector<double> cbm;             // P3 x P3 change of basis
+    std::vector<int> mode_Nm1, mode_Nm2, mode_lin;
+    std::vector<double> leg_tv;
+    std::vector<int> fmap;               // [6][P2] face dof -> cell dof
+
+    std::vector<double> U, U0, R, R1, R0, avars, mu, kk, alpha, alpha_d, bvar;
+    std::vector<double> sf;              // [5][nc*6*P2] surface flux of the current stage
+    double time = 0, dt = 0;
+    int64_t n_steps = 0;
+    int64_t bad_dof = -1;
+
+    const double* metric(const std::vector<double>& a, int comp, int64_t dof) const { return &a[comp * nd + dof]; }
+    Vec JaV(int64_t dof, int dir) const { return {Ja[(dir * 3 + 0) * nd + dof], Ja[(dir * 3 + 1) * nd + dof], Ja[(dir * 3 + 2) * nd + dof]}; }
+    State state(const std::vector<double>& X, int64_t dof) const { return {X[dof], X[nd + dof], X[2 * nd + dof], X[3 * nd + dof], X[4 * nd + dof]}; }
+    Avars avar(int64_t dof) const { Avars a; for (int v = 0; v < 9; ++v) a[v] = avars[v * nd + dof]; return a; }
+    double& sfv(int v, int64_t c, int f, int q) { return sf[v * (nc * 6 * P2) + (c * 6 + f) * P2 + q]; }
+    double ev(int32_t idx, double x, double y, double z, double t) const
+    {
+        return plens::expr_eval(expr_code.data() + expr_off[idx], expr_len[idx], x, y, z, t);
+    }
+
+    // ------------------------------------------------------------ 1D operators (own copies)
+    static void gll(int n, std::vector<double>& x01, std::vector<double>& w01)
+    {
+        const int Nn = n - 1;
+        std::vector<long double> x(n);
+        for (int i = 0; i < n; ++i) x[i] = std::cos(M_PI * (long double)i / Nn);
+        std::vector<long double> PN(n);
+        for (int it = 0; it < 200; ++it) {
+            long double diff = 0;
+            for (int i = 0; i < n; ++i) {
+                long double a = 1, b = x[i];
+                for (int k = 2; k <= Nn; ++k) { long double c = ((2 * k - 1) * x[i] * b - (k - 1) * a) / k; a = b; b = c; }
+                if (Nn == 1) a = 1;
+                const long double xn = x[i] - (x[i] * b - a) / (n * b);
+                diff = std::max(diff, std::fabs(xn - x[i]));
+                x[i] = xn;
+                PN[i] = b;
+            }
+            if (diff < 1e-19L) break;
+        }
+        x01.resize(n); w01.resize(n);
+        for (int i = 0; i < n; ++i) {
+            long double a = 1, b = x[i];
+            for (int k = 2; k <= Nn; ++k) { long double c = ((2 * k - 1) * x[i] * b - (k - 1) * a) / k; a = b; b = c; }
+            x01[n - 1 - i] = (double)((x[i] + 1) / 2);
+            w01[n - 1 - i] = (double)(1.0L / (Nn * n * b * b));
+        }
+        x01[0] = 0; x01[n - 1] = 1;
+    }
+    static double legendre01(int k, double x)  // orthonormal on [0,1] (deal.II Polynomials::Legendre)
+    {
+        const double t = 2 * x - 1;
+        double a = 1, b = t;
+        if (k == 0) return 1.0;
+        for (int j = 2; j <= k; ++j) { const double c = ((2 * j - 1) * t * b - (j - 1) * a) / j; a = b; b = c; }
+        return std::sqrt(2.0 * k + 1) * b;
+    }
+    static double lag(const std::vector<double>& nd_, int j, double x)
+    {
+        double v = 1;
+        for (size_t m = 0; m < nd_.size(); ++m) if ((int)m != j) v *= (x - nd_[m]) / (nd_[j] - nd_[m]);
+        return v;
+    }
+
+    void setup_operators()
+    {
+        std::vector<double> xi;
+        gll(P, xi, w);
+        D.assign(P * P, 0);
+        Q.assign(P * P, 0);
+        for (int i = 0; i < P; ++i)
+            for (int j = 0; j < P; ++j) {
+                // l_j'(xi_i) by the product rule (FE_DGQ<1>::shape_grad)
+                double s = 0;
+                for (int k = 0; k < P; ++k) {
+                    if (k == j) continue;
+                    double t = 1.0 / (xi[j] - xi[k]);
+                    for (int m = 0; m < P; ++m) if (m != j && m != k) t *= (xi[i] - xi[m]) / (xi[j] - xi[m]);
+                    s += t;
+                }
+                D[i * P + j] = s;
+                Q[i * P + j] = w[i] * s;
+            }
+        // change of basis (dgsem/change_of_basis_matrix.h:74-98): C_jk = int psi_j phi_k over
+        // [0,1]^3 with the (N+1)-point Gauss rule
+        std::vector<double> gx(P), gw(P);
+        for (int i = 0; i < P; ++i) {
+            long double x = std::cos(M_PI * (i + 0.75L) / (P + 0.5L)), dp = 0;
+            for (int it = 0; it < 100; ++it) {
+                long double a = 1, b = x;
+                for (int k = 2; k <= P; ++k) { long double c = ((2 * k - 1) * x * b - (k - 1) * a) / k; a = b; b = c; }
+                if (P == 1) { b = x; a = 1; }
+                dp = P * (x * b - a) / (x * x - 1);
+                const long double dx = b / dp;
+                x -= dx;
+                if (std::fabs(dx) < 1e-20L) break;
+            }
+            gx[P - 1 - i] = (double)((x + 1) / 2);
+            gw[P - 1 - i] = (double)(1.0L / ((1 - x * x) * dp * dp));
+        }
+        std::vector<double> psi(P * P), phi(P * P);  // [basis][gauss point]
+        for (int a = 0; a < P; ++a)
+            for (int g = 0; g < P; ++g) { psi[a * P + g] = legendre01(a, gx[g]); phi[a * P + g] = lag(xi, a, gx[g]); }
+        cbm.assign((size_t)P3 * P3, 0);
+        for (int i = 0; i < P3; ++i)
+            for (int j = 0; j < P3; ++j) {
+                double s = 0;
+                for (int gk = 0; gk < P; ++gk)
+                    for (int gj = 0; gj < P; ++gj)
+                        for (int gi = 0; gi < P; ++gi) {
+                            const double wq = gw[gi] * gw[gj] * gw[gk];
+                            const double ps = psi[(i % P) * P + gi] * psi[((i / P) % P) * P + gj] * psi[(i / P2) * P + gk];
+                            const double ph = phi[(j % P) * P + gi] * phi[((j / P) % P) * P + gj] * phi[(j / P2) * P + gk];
+                            s += wq * ps * ph;
+                        }
+                cbm[(size_t)i * P3 + j] = s;
+            }
+        // mode index sets (dgsem/blender_calculator.cc:24-87)
+        const int d = N;
+        for (int k = 0; k < d; ++k) for (int j = 0; j < d; ++j) for (int i = 0; i < d; ++i) mode_Nm1.push_back(i + j * P + k * P2);
+        if (d > 1) for (int k = 0; k < d - 1; ++k) for (int j = 0; j < d - 1; ++j) for (int i = 0; i < d - 1; ++i) mode_Nm2.push_back(i + j * P + k * P2);
+        for (int k = 0; k <= 1; ++k) for (int j = 0; j <= 1; ++j) for (int i = 0; i <= 1; ++i) mode_lin.push_back(i + j * P + k * P2);
+        leg_tv.push_back(0.0);
+        leg_tv.push_back(std::fabs(legendre01(1, 1) - legendre01(1, 0)));
+        for (int ip = 2; ip <= d; ++ip) {
+            std::vector<double> qx, qw;
+            gll(ip + 1, qx, qw);
+            double tv = 0;
+            for (int k = 0; k < ip; ++k) tv += std::fabs(legendre01(ip, qx[k + 1]) - legendre01(ip, qx[k]));
+            leg_tv.push_back(tv);
+        }
+        // face dof maps (dgsem/face_dof_info.h:92-150)
+        fmap.assign(6 * P2, 0);
+        for (int q = 0; q < P2; ++q) {
+            fmap[0 * P2 + q] = P * q;
+            fmap[1 * P2 + q] = N + P * q;
+            fmap[2 * P2 + q] = (q % P) + P2 * (q / P);
+            fmap[3 * P2 + q] = P * N + (q % P) + P2 * (q / P);
+            fmap[4 * P2 + q] = q;
+            fmap[5 * P2 + q] = N * P2 + q;
+        }
+    }
+
+    int tl(int i, int j, int k) const { return i + j * P + k * P2; }
+
+    // ------------------------------------------------------------------- BC ghost states
+    // IBCs/*.cc get_ghost_stage{1,2,3}; `stage` is 1, 2 or 3.
+    void ghost(int stage, int ti, const State& c, const Avars& av, State& cg, Avars& ag, double t) const
+    {
+        const int64_t cell = ft_cell[ti];
+        const int bid = ft_bc[ti];
+        (void)cell;
+        const plens_bc_desc& b = bcs[bid];
+        ag = av;
+        switch (b.type) {
+        case PLENS_BC_FREE: cg = c; return;
+        case PLENS_BC_OUTFLOW:
+            cg = c;
+            if (stage == 2) {
+                const double Mn = ns.get_M(c);
+                if (!(ns.is_inviscid() || Mn >= 1)) cg[4] += 2 * (b.p - ns.get_p(c)) / (ns.gma - 1);
+            }
+            return;
+        case PLENS_BC_UNIFORM_INFLOW:
+            if (stage == 2) { for (int v = 0; v < 5; ++v) cg[v] = b.cons[v]; return; }
+            for (int v = 0; v < 5; ++v) cg[v] = 2 * b.cons[v] - c[v];
+            return;
+        case PLENS_BC_UNIFORM_TEMP_WALL:
+        case PLENS_BC_INSULATED_WALL: {
+            const Vec vw{{b.vel[0], b.vel[1], b.vel[2]}};
+            if (stage == 2) {
+                cg[0] = c[0];
+                cg[4] = c[4];
+                // the normal is passed separately; see ghost_n
+                return;
+            }
+            State cp;
+            const double pin = ns.get_p(c);
+            const double rho_pr = (b.type == PLENS_BC_UNIFORM_TEMP_WALL) ? pin / (ns.R * b.T) : c[0];
+            ns.prim_to_cons(rho_pr, vw, pin, cp);
+            for (int v = 0; v < 5; ++v) cg[v] = 2 * cp[v] - c[v];
+            return;
+        }
+        case PLENS_BC_ZPG_INFLOW: {
+            const Vec vw{{b.vel[0], b.vel[1], b.vel[2]}};
+            State cp;
+            ns.prim_to_cons(c[0], vw, ns.get_p(c), cp);
+            if (stage == 2) { cg = cp; return; }
+            for (int v = 0; v < 5; ++v) cg[v] = 2 * cp[v] - c[v];
+            return;
+        }
+        default: cg = c; return;
+        }
+    }
+    // full ghost evaluation incl. the normal-dependent and location-dependent types
+    void get_ghost(int stage, int ti, int q, const State& c, const Avars& av, const Vec& n, State& cg, Avars& ag, double t) const
+    {
+        const plens_bc_desc& b = bcs[ft_bc[ti]];
+        ag = av;
+        switch (b.type) {
+        case PLENS_BC_PERIODIC: {
+            // IBCs/periodic.cc:69-165: partner cell/face, same face dof
+            const int64_t pc = ft_nbr_cell[ti];
+            const int pf = ft_nbr_face[ti];
+            const int64_t gd = pc * P3 + fmap[pf * P2 + ft_nbr_fdof[(int64_t)ti * P2 + q]];
+            cg = state(U, gd);
+            if (stage == 3) ag = avar(gd);
+            return;
+        }
+        case PLENS_BC_SYMMETRY:
+        case PLENS_BC_EMPTY: {
+            // symmetry.cc:17-98, empty.cc:15-91
+            if (stage == 2 && b.type == PLENS_BC_SYMMETRY) {
+                cg[0] = c[0]; cg[4] = c[4];
+                const Vec sm{{c[1], c[2], c[3]}};
+                const double nsm = dot(sm, n);
+                for (int d = 0; d < 3; ++d) cg[1 + d] = sm[d] - 2 * nsm * n[d];
+                return;
+            }
+            Vec vin, vpr;
+            for (int d = 0; d < 3; ++d) vin[d] = c[1 + d] / c[0];
+            const double nv = dot(vin, n);
+            for (int d = 0; d < 3; ++d) vpr[d] = vin[d] - nv * n[d];
+            const double pin = ns.get_p(c);
+            State cp;
+            ns.prim_to_cons(c[0], vpr, pin, cp);
+            if (stage == 2) { cg = cp; return; }  // empty, stage 2
+            for (int v = 0; v < 5; ++v) cg[v] = 2 * cp[v] - c[v];
+            return;
+        }
+        case PLENS_BC_UNIFORM_TEMP_WALL:
+        case PLENS_BC_INSULATED_WALL:
+            ghost(stage, ti, c, av, cg, ag, t);
+            if (stage == 2) {
+                // uniform_temp_wall.cc:55-69
+                if (ns.is_inviscid()) {
+                    Vec sm, smr;
+                    for (int d = 0; d < 3; ++d) { sm[d] = c[1 + d]; smr[d] = c[1 + d] - c[0] * b.vel[d]; }
+                    const double nsm = dot(smr, n);
+                    for (int d = 0; d < 3; ++d) cg[1 + d] = sm[d] - 2 * nsm * n[d];
+                } else {
+                    for (int d = 0; d < 3; ++d) cg[1 + d] = 2 * c[0] * b.vel[d] - c[1 + d];
+                }
+            }
+            if (stage == 3 && b.type == PLENS_BC_INSULATED_WALL) {
+                // insulated_wall.cc:92-101, with the heat flux mirrored as its documentation
+                // states (the reference writes it out of bounds)
+                const Vec hf{{av[6], av[7], av[8]}};
+                const double nh = dot(hf, n);
+                for (int d = 0; d < 3; ++d) ag[6 + d] = hf[d] - 2 * nh * n[d];
+            }
+            return;
+        case PLENS_BC_VARYING_INFLOW: {
+            // varying_inflow.cc:17-35 at the dof location and the step's start time
+            const double* x = &ft_xyz[((int64_t)ti * P2 + q) * 3];
+            const double p = ev(b.expr_p, x[0], x[1], x[2], t), T = ev(b.expr_T, x[0], x[1], x[2], t);
+            Vec vel;
+            for (int d = 0; d < 3; ++d) vel[d] = ev(b.expr_vel[d], x[0], x[1], x[2], t);
+            State cp;
+            ns.prim_to_cons(p / (ns.R * T), vel, p, cp);
+            if (stage == 2) { cg = cp; return; }
+            for (int v = 0; v < 5; ++v) cg[v] = 2 * cp[v] - c[v];
+            return;
+        }
+        default:
+            ghost(stage, ti, c, av, cg, ag, t);
+            return;
+        }
+    }
+
+    // ------------------------------------------------------ calc_surf_flux (plens.cc:1717-1913)
+    void surf_flux_stage(int stage, const State& c1, const Avars& a1, const State& c2, const Avars& a2, const Vec& n, State& f, NavierStokes& nsl) const
+    {
+        if (stage == 1) { for (int v = 0; v < 5; ++v) f[v] = 0.5 * (c1[v] + c2[v]); return; }
+        if (stage == 2) { nsl.get_inv_surf_flux(c1, c2, n, f); return; }
+        State f1, f2;
+        NavierStokes::get_dif_flux(c1, a1, n, f1);
+        NavierStokes::get_dif_flux(c2, a2, n, f2);
+        for (int v = 0; v < 5; ++v) f[v] = 0.5 * (f1[v] + f2[v]);
+    }
+    void calc_surf_flux(int stage)
+    {
+        const double rsign = (stage == 1) ? 1.0 : -1.0;
+        const int64_t nt = M.n_face_tasks;
+#pragma omp parallel for schedule(static)
+        for (int64_t ti = 0; ti < nt; ++ti) {
+            NavierStokes nsl = ns;
+            const int64_t c = ft_cell[ti];
+            const int f = ft_face[ti];
+            const bool boundary = ft_bc[ti] >= 0;
+            if (boundary) nsl.set_flux_blender_value(alpha[c]);
+            else nsl.set_flux_blender_value(0.5 * (alpha[c] + alpha[ft_nbr_cell[ti]]));
+            for (int q = 0; q < P2; ++q) {
+                const int64_t gd = c * P3 + fmap[f * P2 + q];
+                const State cs = state(U, gd);
+                const Avars av = (stage == 3) ? avar(gd) : Avars{};
+                const Vec n{{ft_normal[(ti * P2 + q) * 3], ft_normal[(ti * P2 + q) * 3 + 1], ft_normal[(ti * P2 + q) * 3 + 2]}};
+                State flux;
+                if (boundary) {
+                    State cg;
+                    Avars ag;
+                    get_ghost(stage, (int)ti, q, cs, av, n, cg, ag, time);
+                    surf_flux_stage(stage, cs, av, cg, ag, n, flux, nsl);
+                    for (int v = 0; v < 5; ++v) sfv(v, c, f, q) = flux[v];
+                } else {
+                    const int64_t nb = ft_nbr_cell[ti];
+                    const int fn = ft_nbr_face[ti];
+                    const int qn = ft_nbr_fdof[ti * P2 + q];
+                    const int64_t gdn = nb * P3 + fmap[fn * P2 + qn];
+                    const State cn = state(U, gdn);
+                    const Avars an = (stage == 3) ? avar(gdn) : Avars{};
+                    surf_flux_stage(stage, cs, av, cn, an, n, flux, nsl);
+                    for (int v = 0; v < 5; ++v) {
+                        sfv(v, c, f, q) = flux[v];
+                        sfv(v, nb, fn, qn) = rsign * flux[v];
+                    }
+                }
+            }
+        }
+    }
+
+    // --------------------------------------------------- assert_positivity (plens.cc:2531-2546)
+    bool assert_positivity()
+    {
+        int64_t bad = INT64_MAX;
+#pragma omp parallel for reduction(min : bad)
+        for (int64_t i = 0; i < nd; ++i) {
+            const State c = state(U, i);
+            if (!(c[0] > 0) || !(NavierStokes::get_e(c) > 0)) bad = std::min(bad, i);
+        }
+        bad_dof = (bad == INT64_MAX) ? -1 : bad;
+        return bad_dof < 0;
+    }
+
+    // ------------------------------------------------------------- calc_aux_vars (2593-2748)
+    void calc_aux_vars()
+    {
+        const double cv = ns.get_cv();
+#pragma omp parallel for
+        for (int64_t i = 0; i < nd; ++i) {
+            const double e = NavierStokes::get_e(state(U, i));
+            mu[i] = ns.get_mu(e / cv);
+            kk[i] = ns.get_k(mu[i]);
+        }
+        calc_surf_flux(1);
+        // face entropy variables of the BR1 face values
+        const int64_t nsf = nc * 6 * P2;
+        std::vector<double> es(5 * nsf);
+#pragma omp parallel for
+        for (int64_t s = 0; s < nsf; ++s) {
+            State c, e;
+            for (int v = 0; v < 5; ++v) c[v] = sf[v * nsf + s];
+            ns.cons_to_entropy(c, e);
+            for (int v = 0; v < 5; ++v) es[v * nsf + s] = e[v];
+        }
+#pragma omp parallel for schedule(static)
+        for (int64_t c = 0; c < nc; ++c) {
+            std::vector<State> evars(P3);
+            std::vector<std::array<State, 3>> g(P3);
+            for (int l = 0; l < P3; ++l) ns.cons_to_entropy(state(U, c * P3 + l), evars[l]);
+            // calc_cell_evar_grad (plens.cc:2294-2405)
+            for (int l = 0; l < P3; ++l) for (int d = 0; d < 3; ++d) g[l][d].fill(0.0);
+            const double ssign[2] = {1, -1};
+            for (int gd = 0; gd < 3; ++gd) {
+                for (int l = 0; l < P3; ++l) {
+                    const int ti[3] = {l % P, (l / P) % P, l / P2};
+                    for (int m = 0; m <= N; ++m)
+                        for (int md = 0; md < 3; ++md) {
+                            int to[3] = {ti[0], ti[1], ti[2]};
+                            to[md] = m;
+                            const int lo = tl(to[0], to[1], to[2]);
+                            const double jc = Ja[(md * 3 + gd) * nd + c * P3 + lo];
+                            const double dv = D[ti[md] * P + m];
+                            for (int v = 0; v < 5; ++v) g[l][gd][v] += dv * evars[lo][v] * jc;
+                        }
+                }
+                for (int sd = 0; sd < 3; ++sd)
+                    for (int lr = 0; lr <= 1; ++lr) {
+                        const int f = 2 * sd + lr;
+                        for (int q = 0; q < P2; ++q) {
+                            const int l = fmap[f * P2 + q];
+                            const double jc = Ja[(sd * 3 + gd) * nd + c * P3 + l];
+                            for (int v = 0; v < 5; ++v) {
+                                const double fin = evars[l][v] * jc;
+                                const double fsu = es[v * nsf + (c * 6 + f) * P2 + q] * jc;
+                                g[l][gd][v] -= ssign[lr] * (fsu - fin) / w[lr * N];
+                            }
+                        }
+                    }
+                for (int l = 0; l < P3; ++l) {
+                    const double ji = 1.0 / detJ[c * P3 + l];
+                    for (int v = 0; v < 5; ++v) g[l][gd][v] *= ji;
+                }
+            }
+            for (int l = 0; l < P3; ++l) {
+                const int64_t dof = c * P3 + l;
+                State et;
+                ns.cons_to_entropy(state(U, dof), et);
+                double vg[3][3];
+                for (int vd = 0; vd < 3; ++vd)
+                    for (int gd = 0; gd < 3; ++gd)
+                        vg[vd][gd] = (et[1 + vd] * g[l][gd][4] / et[4] - g[l][gd][1 + vd]) / et[4];
+                int sid = 0;
+                double tr = 0;
+                for (int d = 0; d < 3; ++d) tr += vg[d][d];
+                for (int row = 0; row < 3; ++row)
+                    for (int col = row; col < 3; ++col) {
+                        avars[sid * nd + dof] = (col == row) ? vg[row][col] + vg[col][row] - 2.0 / 3 * tr : vg[row][col] + vg[col][row];
+                        ++sid;
+                    }
+                for (int gd = 0; gd < 3; ++gd) avars[(6 + gd) * nd + dof] = -(g[l][gd][4] / (et[4] * et[4] * ns.R));
+                for (int v = 0; v < 6; ++v) avars[v * nd + dof] *= mu[dof];
+                for (int v = 6; v < 9; ++v) avars[v * nd + dof] *= kk[dof];
+            }
+        }
+    }
+
+    // ------------------------------------------------------- blender (plens.cc:2858-2962)
+    double get_blender(int64_t c) const  // blender_calculator.cc:123-177, 277-303
+    {
+        std::vector<double> modes(P3);
+        for (int row = 0; row < P3; ++row) {
+            modes[row] = 0;
+            for (int col = 0; col < P3; ++col) modes[row] += cbm[(size_t)row * P3 + col] * bvar[c * P3 + col];
+        }
+        double et = 0, e1 = 0, e2 = 0;
+        for (double m : modes) et += m * m;
+        for (int i : mode_Nm1) e1 += modes[i] * modes[i];
+        for (int i : mode_Nm2) e2 += modes[i] * modes[i];
+        const double trouble = (N > 2) ? std::max(1 - e1 / et, 1 - e2 / e1) : 1 - e1 / et;
+        const double thr = Pm.threshold_factor * std::pow(10, -Pm.threshold_exp_factor * (std::pow(N + 1, 0.25)));
+        if (Pm.blender_function == 0) {
+            const double at = 1 / (1 + std::exp(-Pm.sharpness_factor * (trouble / thr - 1)));
+            if (at < Pm.alpha_min) return 0;
+            if (at < Pm.alpha_max) return at;
+            return Pm.alpha_max;
+        }
+        const double at = trouble / thr;
+        return at > 1 ? 1 : at;
+    }
+    double post_filter(double a, int64_t c) const  // blender_calculator.cc:196-259
+    {
+        if (a > Pm.alpha_min) return a;
+        std::vector<double> am(P3);
+        double ub = 0, asum = 0;
+        for (int row = 0; row < P3; ++row) {
+            double s = 0;
+            for (int col = 0; col < P3; ++col) s += cbm[(size_t)row * P3 + col] * bvar[c * P3 + col];
+            const int k = row / P2, j = (row - k * P2) / P, i = row - k * P2 - j * P;
+            const double t = std::fabs(s);
+            asum += t;
+            am[row] = t * (leg_tv[i] + leg_tv[j] + leg_tv[k]);
+            ub += am[row];
+        }
+        if (ub < 1e-2 * asum) return a;
+        double tl_ = 0;
+        for (int r : mode_lin) tl_ += am[r];
+        return a + (Pm.alpha_max - a) * (1 - tl_ / ub);
+    }
+    void calc_blender()
+    {
+#pragma omp parallel for
+        for (int64_t i = 0; i < nd; ++i) {
+            const State c = state(U, i);
+            bvar[i] = (Pm.blender_variable == 2) ? c[0] : (Pm.blender_variable == 1) ? ns.get_p(c) : ns.get_p(c) * c[0];
+        }
+        const double wall_limit = ev(Pm.expr_wall_blender_limit, 0, 0, 0, time);
+#pragma omp parallel for
+        for (int64_t c = 0; c < nc; ++c) {
+            const double bv = get_blender(c);
+            alpha[c] = bv;
+            for (int f = 0; f < 6; ++f) {
+                const int b = cell_face_bc[6 * c + f];
+                if (b >= 0 && (bcs[b].type == PLENS_BC_INSULATED_WALL || bcs[b].type == PLENS_BC_UNIFORM_TEMP_WALL))
+                    alpha[c] = std::max(wall_limit, bv);
+            }
+        }
+        const std::vector<double> snap = alpha;
+#pragma omp parallel for
+        for (int64_t c = 0; c < nc; ++c) {
+            for (int f = 0; f < 6; ++f) {
+                const int32_t nb = cell_nbr[6 * c + f];
+                if (nb < 0) continue;
+                alpha[c] = std::max(alpha[c], 0.5 * snap[nb]);
+            }
+            if (Pm.do_filtering) alpha[c] = post_filter(alpha[c], c);
+        }
+#pragma omp parallel for
+        for (int64_t c = 0; c < nc; ++c) {
+            const double* x = &center[3 * c];
+            if (ev(Pm.expr_vis_blending_region, x[0], x[1], x[2], time) > 0) alpha_d[c] = std::min(1.0, alpha[c] / Pm.alpha_max);
+            else alpha_d[c] = 0;
+        }
+    }
+
+    // ------------------------------------------- calc_cell_ho_inv_residual (plens.cc:3153-3275)
+    void ho_inv(int64_t c, std::vector<State>& res) const
+    {
+        const double ssign[2] = {1, -1};
+        for (auto& r : res) r.fill(0.0);
+        for (int l = 0; l < P3; ++l) {
+            const State ct = state(U, c * P3 + l);
+            const int ti[3] = {l % P, (l / P) % P, l / P2};
+            for (int m = 0; m <= N; ++m)
+                for (int md = 0; md < 3; ++md) {
+                    int to[3] = {ti[0], ti[1], ti[2]};
+                    to[md] = m;
+                    const int lo = tl(to[0], to[1], to[2]);
+                    const State co = state(U, c * P3 + lo);
+                    const Vec a = JaV(c * P3 + l, md), b = JaV(c * P3 + lo, md);
+                    Vec dir{{0.5 * (a[0] + b[0]), 0.5 * (a[1] + b[1]), 0.5 * (a[2] + b[2])}};
+                    const double nr = norm(dir);
+                    for (int d = 0; d < 3; ++d) dir[d] /= nr;
+                    State flux;
+                    ns.get_inv_vol_flux(ct, co, dir, flux);
+                    const double dv = 2 * D[ti[md] * P + m] * nr;
+                    for (int v = 0; v < 5; ++v) res[l][v] += dv * flux[v];
+                }
+        }
+        for (int sd = 0; sd < 3; ++sd)
+            for (int lr = 0; lr <= 1; ++lr) {
+                const int f = 2 * sd + lr;
+                for (int q = 0; q < P2; ++q) {
+                    const int l = fmap[f * P2 + q];
+                    Vec dir = JaV(c * P3 + l, sd);
+                    const double nr = norm(dir);
+                    for (int d = 0; d < 3; ++d) dir[d] /= nr;
+                    State fs, fin;
+                    for (int v = 0; v < 5; ++v) fs[v] = -ssign[lr] * sf[v * (nc * 6 * P2) + (c * 6 + f) * P2 + q];
+                    ns.get_inv_flux(state(U, c * P3 + l), dir, fin);
+                    for (int v = 0; v < 5; ++v) res[l][v] += -ssign[lr] * (fs[v] - fin[v]) * nr / w[lr * N];
+                }
+            }
+        for (int l = 0; l < P3; ++l) {
+            const double js = 1 / (-1 * detJ[c * P3 + l]);
+            for (int v = 0; v < 5; ++v) res[l][v] *= js;
+        }
+    }
+
+    // ------------------------------------------- calc_cell_ho_dif_residual (plens.cc:3283-3413)
+    void ho_dif(int64_t c, const std::vector<double>& sf3, std::vector<State>& res) const
+    {
+        const double ssign[2] = {1, -1};
+        for (auto& r : res) r.fill(0.0);
+        for (int l = 0; l < P3; ++l) {
+            const int ti[3] = {l % P, (l / P) % P, l / P2};
+            for (int m = 0; m <= N; ++m)
+                for (int md = 0; md < 3; ++md) {
+                    int to[3] = {ti[0], ti[1], ti[2]};
+                    to[md] = m;
+                    const int lo = tl(to[0], to[1], to[2]);
+                    Vec dir = JaV(c * P3 + lo, md);
+                    const double nr = norm(dir);
+                    for (int d = 0; d < 3; ++d) dir[d] /= nr;
+                    State flux;
+                    NavierStokes::get_dif_flux(state(U, c * P3 + lo), avar(c * P3 + lo), dir, flux);
+                    const double dv = D[ti[md] * P + m] * nr;
+                    for (int v = 0; v < 5; ++v) res[l][v] += dv * flux[v];
+                }
+        }
+        for (int sd = 0; sd < 3; ++sd)
+            for (int lr = 0; lr <= 1; ++lr) {
+                const int f = 2 * sd + lr;
+                for (int q = 0; q < P2; ++q) {
+                    const int l = fmap[f * P2 + q];
+                    Vec dir = JaV(c * P3 + l, sd);
+                    const double nr = norm(dir);
+                    for (int d = 0; d < 3; ++d) dir[d] /= nr;
+                    State fs, fin;
+                    for (int v = 0; v < 5; ++v) fs[v] = -ssign[lr] * sf3[v * (nc * 6 * P2) + (c * 6 + f) * P2 + q];
+                    NavierStokes::get_dif_flux(state(U, c * P3 + l), avar(c * P3 + l), dir, fin);
+                    for (int v = 0; v < 5; ++v) res[l][v] += -ssign[lr] * (fs[v] - fin[v]) * nr / w[lr * N];
+                }
+            }
+        for (int l = 0; l < P3; ++l) {
+            const double js = 1 / (1 * detJ[c * P3 + l]);
+            for (int v = 0; v < 5; ++v) res[l][v] *= js;
+        }
+    }
+
+    // ------------------------------------------- calc_cell_lo_inv_residual (plens.cc:3469-3583)
+    Vec subcell_normal(int64_t c, int dir, const int ti[3]) const  // metric_terms.cc:106-141
+    {
+        int t0[3] = {ti[0], ti[1], ti[2]};
+        t0[dir] = 0;
+        Vec n = JaV(c * P3 + tl(t0[0], t0[1], t0[2]), dir);
+        for (int l = 0; l <= ti[dir] - 1; ++l)
+            for (int m = 0; m <= N; ++m) {
+                int tm[3] = {ti[0], ti[1], ti[2]};
+                tm[dir] = m;
+                const Vec a = JaV(c * P3 + tl(tm[0], tm[1], tm[2]), dir);
+                for (int d = 0; d < 3; ++d) n[d] += Q[l * P + m] * a[d];
+            }
+        return n;
+    }
+    void lo_inv(int64_t c, std::vector<State>& res) const
+    {
+        for (auto& r : res) r.fill(0.0);
+        NavierStokes nsl = ns;
+        nsl.set_flux_blender_value(alpha[c]);
+        for (int dir = 0; dir < 3; ++dir) {
+            const int d1 = (dir + 1) % 3, d2 = (dir + 2) % 3;
+            for (int id1 = 0; id1 <= N; ++id1)
+                for (int id2 = 0; id2 <= N; ++id2)
+                    for (int id = 1; id <= N; ++id) {
+                        int tlf[3], trt[3];
+                        tlf[dir] = id - 1; tlf[d1] = id1; tlf[d2] = id2;
+                        trt[dir] = id; trt[d1] = id1; trt[d2] = id2;
+                        const int ll = tl(tlf[0], tlf[1], tlf[2]), lr_ = tl(trt[0], trt[1], trt[2]);
+                        const State cl = state(U, c * P3 + ll), cr = state(U, c * P3 + lr_);
+                        Vec nd_ = subcell_normal(c, dir, trt);
+                        const double nn = norm(nd_);
+                        for (int d = 0; d < 3; ++d) nd_[d] /= nn;
+                        State flux;
+                        nsl.get_inv_surf_flux(cl, cr, nd_, flux);
+                        for (int v = 0; v < 5; ++v) {
+                            res[ll][v] += flux[v] * nn / w[id - 1];
+                            res[lr_][v] -= flux[v] * nn / w[id];
+                        }
+                    }
+        }
+        for (int dir = 0; dir < 3; ++dir)
+            for (int lr = 0; lr <= 1; ++lr) {
+                const int f = 2 * dir + lr;
+                const float cs = -std::pow(-1, lr), fsg = -std::pow(-1, lr);
+                for (int q = 0; q < P2; ++q) {
+                    const int l = fmap[f * P2 + q];
+                    const double nn = norm(JaV(c * P3 + l, dir));
+                    for (int v = 0; v < 5; ++v) {
+                        const double fl = fsg * sf[v * (nc * 6 * P2) + (c * 6 + f) * P2 + q];
+                        res[l][v] += cs * fl * nn / w[lr * N];
+                    }
+                }
+            }
+        for (int l = 0; l < P3; ++l)
+            for (int v = 0; v < 5; ++v) res[l][v] /= -detJ[c * P3 + l];
+    }
+
+    // ------------------------------------------------------------ calc_rhs (plens.cc:3688-3779)
+    int calc_rhs()
+    {
+        if (!assert_positivity()) return PLENS_GPU_E_POSITIVITY;
+        const bool visc = !ns.is_inviscid();
+        if (visc) calc_aux_vars();
+        calc_blender();
+        std::vector<double> sf3;
+        if (visc) {
+            calc_surf_flux(3);
+            sf3 = sf;
+        }
+        calc_surf_flux(2);
+#pragma omp parallel for schedule(static)
+        for (int64_t c = 0; c < nc; ++c) {
+            std::vector<State> hi(P3), hd(P3), lo(P3);
+            ho_inv(c, hi);
+            if (visc) ho_dif(c, sf3, hd);
+            lo_inv(c, lo);
+            const double a = alpha[c], ad = alpha_d[c];
+            for (int l = 0; l < P3; ++l) {
+                const int64_t dof = c * P3 + l;
+                for (int v = 0; v < 5; ++v) {
+                    if (visc) R[v * nd + dof] = (1 - ad) * hd[l][v] + a * lo[l][v] + (1 - a) * hi[l][v];
+                    else R[v * nd + dof] = a * lo[l][v] + (1 - a) * hi[l][v];
+                }
+                if (Pm.plens_2d) R[3 * nd + dof] = 0;
+            }
+        }
+        return PLENS_GPU_OK;
+    }
+
+    // -------------------------------------------------------- calc_time_step (plens.cc:3810-3912)
+    double calc_time_step()
+    {
+        double Co = ev(Pm.expr_courant, 0, 0, 0, time);
+        if (Co >= 1) Co = 0.9;
+        double proc = 1e6;
+#pragma omp parallel for reduction(min : proc)
+        for (int64_t c = 0; c < nc; ++c) {
+            double cell_step = 1e6;
+            const double h = h_min[c];
+            for (int l = 0; l < P3; ++l) {
+                const int64_t dof = c * P3 + l;
+                const State cs = state(U, dof);
+                const double a = ns.get_a(cs);
+                const Vec vel{{cs[1] / cs[0], cs[2] / cs[0], cs[3] / cs[0]}};
+                Vec adv{{0, 0, 0}};
+                for (int row = 0; row < 3; ++row)
+                    for (int col = 0; col < 3; ++col) adv[row] += Jinv[(col * 3 + row) * nd + dof] * vel[col];
+                const double madv = std::max({adv[0], adv[1], adv[2]});
+                const double cur = Co / (std::pow(N, 1.5) * (madv + a / h + N * N * mu[dof] / (h * h * cs[0])));
+                if (cur < cell_step) cell_step = cur;
+            }
+            if (cell_step < proc) proc = cell_step;
+        }
+        return proc;
+    }
+
+    // ------------------------------------------------------ update_rk4 / update (4334-4518)
+    static constexpr double b_[5] = {314199625218.0 / 7198350928319, 6410344372641.0 / 17000082738695,
+                                     292278564125.0 / 5593752632744, 5010207514426.0 / 21876007855139,
+                                     5597675544274.0 / 18784428342765};
+    int update(double end_time)
+    {
+        U0 = U;  // g_cvars
+        const double ao[5] = {4745337637855.0 / 22386579876409, 6808157035527.0 / 13197844641179,
+                              4367509502613.0 / 10454198590847, 1236962429870.0 / 3429868089329, b_[4]};
+        const double ai[4] = {546509042554.0 / 9152262712923, 625707605167.0 / 5316659119056,
+                              582400652113.0 / 7078426004906, b_[3]};
+        int st = calc_rhs();
+        if (st) return st;
+        // loc_time_steps holds the unclipped global step and multiplies the RHS; only the clock
+        // uses the step clipped to end_time (dgsem/plens.cc:3903-3911, 4339-4341, 3925-3940)
+        dt = calc_time_step();
+        const double dt_update = dt;
+        if (dt > (end_time - time)) dt = end_time - time;
+        auto mult = [&]() {
+#pragma omp parallel for
+            for (int64_t i = 0; i < 5 * nd; ++i) R[i] = R[i] * dt_update;
+        };
+        mult();
+        if (Pm.rk_order == 4) {
+#pragma omp parallel for
+            for (int64_t i = 0; i < 5 * nd; ++i) { U[i] = U[i] + ao[0] * R[i]; R1[i] = R[i]; }
+            if ((st = calc_rhs())) return st;
+            mult();
+#pragma omp parallel for
+            for (int64_t i = 0; i < 5 * nd; ++i) {
+                U[i] = U[i] + ((ai[0] - ao[0]) * R1[i] + ao[1] * R[i]);
+                R0[i] = R1[i];
+                R1[i] = R[i];
+            }
+            for (int s = 3; s <= 5; ++s) {
+                if ((st = calc_rhs())) return st;
+                mult();
+#pragma omp parallel for
+                for (int64_t i = 0; i < 5 * nd; ++i) {
+                    U[i] = U[i] + ((b_[s - 3] - ai[s - 3]) * R0[i] + (ai[s - 2] - ao[s - 2]) * R1[i] + ao[s - 1] * R[i]);
+                    R0[i] = R1[i];
+                    R1[i] = R[i];
+                }
+            }
+        } else {
+            // update_rk3 (plens.cc:4420-4475)
+#pragma omp parallel for
+            for (int64_t i = 0; i < 5 * nd; ++i) U[i] = U[i] + R[i];
+            if ((st = calc_rhs())) return st;
+            mult();
+#pragma omp parallel for
+            for (int64_t i = 0; i < 5 * nd; ++i) U[i] = 0.75 * U0[i] + 0.25 * U[i] + 0.25 * R[i];
+            if ((st = calc_rhs())) return st;
+            mult();
+#pragma omp parallel for
+            for (int64_t i = 0; i < 5 * nd; ++i) U[i] = 1.0 / 3 * U0[i] + 2.0 / 3 * U[i] + 2.0 / 3 * R[i];
+        }
+        time += dt;
+        ++n_steps;
+        return PLENS_GPU_OK;
+    }
+};
+
+template <class T>
+std::vector<T> cp(const T* p, int64_t n) { return p ? std::vector<T>(p, p + n) : std::vector<T>(); }
+
+}  // namespace
+
+extern "C" {
+
+void* oracle_create(const plens_mesh_desc* m, const plens_params* p)
+{
+    if (!m || !p || m->degree < 1 || m->degree > 5 || m->degree != p->degree) return nullptr;
+    auto* o = new Oracle();
+    o->N = m->degree;
+    o->P = o->N + 1;
+    o->P2 = o->P * o->P;
+    o->P3 = o->P2 * o->P;
+    o->nc = m->n_cells;
+    o->nd = o->nc * o->P3;
+    const int64_t nd = o->nd, nc = o->nc, nt = m->n_face_tasks, P2 = o->P2;
+    o->detJ = cp(m->detJ, nd);
+    o->Ja = cp(m->Ja, 9 * nd);
+    o->Jinv = cp(m->Jinv, 9 * nd);
+    o->h_min = cp(m->h_min, nc);
+    o->center = cp(m->cell_center, 3 * nc);
+    o->cell_nbr = cp(m->cell_nbr, 6 * nc);
+    o->cell_face_bc = cp(m->cell_face_bc, 6 * nc);
+    o->ft_cell = cp(m->ft_cell, nt);
+    o->ft_face = cp(m->ft_face, nt);
+    o->ft_nbr_cell = cp(m->ft_nbr_cell, nt);
+    o->ft_nbr_face = cp(m->ft_nbr_face, nt);
+    o->ft_bc = cp(m->ft_bc, nt);
+    o->ft_nbr_fdof = cp(m->ft_nbr_fdof, nt * P2);
+    o->ft_normal = cp(m->ft_normal, nt * P2 * 3);
+    o->ft_xyz = cp(m->ft_xyz, nt * P2 * 3);
+    o->bcs = cp(p->bcs, p->n_bc);
+    o->expr_off = cp(p->expr_offset, p->n_expr);
+    o->expr_len = cp(p->expr_length, p->n_expr);
+    o->expr_code = cp(p->expr_code, p->n_expr_insn);
+    o->M = *m;
+    o->Pm = *p;
+    o->ns.gma = p->gamma; o->ns.R = p->R; o->ns.Pr = p->Pr; o->ns.mu0 = p->mu0; o->ns.T0 = p->T0; o->ns.S = p->S;
+    o->ns.const_visc = p->const_viscosity != 0;
+    o->ns.isf = p->inv_surf_flux;
+    o->ns.ivf = p->inv_vol_flux;
+    o->setup_operators();
+    o->U.assign(5 * nd, 0); o->R.assign(5 * nd, 0); o->R1.assign(5 * nd, 0); o->R0.assign(5 * nd, 0);
+    o->avars.assign(9 * nd, 0); o->mu.assign(nd, 0); o->kk.assign(nd, 0); o->bvar.assign(nd, 0);
+    o->alpha.assign(nc, 0); o->alpha_d.assign(nc, 0);
+    o->sf.assign(5 * nc * 6 * P2, 0);
+    return o;
+}
+
+void oracle_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+void oracle_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+int oracle_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+int oracle_set_state(void* h, const double* U, double t, int64_t n_steps)
+{
+    auto* o = static_cast<Oracle*>(h);
+    std::memcpy(o->U.data(), U, sizeof(double) * 5 * o->nd);
+    o->time = t;
+    o->n_steps = n_steps;
+    std::fill(o->mu.begin(), o->mu.end(), 0.0);
+    return 0;
+}
+
+int oracle_get_state(void* h, double* U, double* t, int64_t* n_steps, double* dt)
+{
+    auto* o = static_cast<Oracle*>(h);
+    if (U) std::memcpy(U, o->U.data(), sizeof(double) * 5 * o->nd);
+    if (t) *t = o->time;
+    if (n_steps) *n_steps = o->n_steps;
+    if (dt) *dt = o->dt;
+    return 0;
+}
+
+int oracle_rhs(void* h, double* R, double* alpha, double* alpha_d, double* avars)
+{
+    auto* o = static_cast<Oracle*>(h);
+    const int st = o->calc_rhs();
+    if (st) return st;
+    if (R) std::memcpy(R, o->R.data(), sizeof(double) * 5 * o->nd);
+    if (alpha) std::memcpy(alpha, o->alpha.data(), sizeof(double) * o->nc);
+    if (alpha_d) std::memcpy(alpha_d, o->alpha_d.data(), sizeof(double) * o->nc);
+    if (avars) std::memcpy(avars, o->avars.data(), sizeof(double) * 9 * o->nd);
+    return 0;
+}
+
+int oracle_time_step(void* h, double* dt)
+{
+    auto* o = static_cast<Oracle*>(h);
+    // mu of the current state (calc_aux_vars sets it at stage 1 before the time step)
+    const double cv = o->ns.get_cv();
+    for (int64_t i = 0; i < o->nd; ++i) {
+        const double e = NavierStokes::get_e(o->state(o->U, i));
+        o->mu[i] = o->ns.is_inviscid() ? 0.0 : o->ns.get_mu(e / cv);
+    }
+    *dt = o->calc_time_step();
+    return 0;
+}
+
+int oracle_advance(void* h, int64_t n_steps, double end_time)
+{
+    auto* o = static_cast<Oracle*>(h);
+    for (int64_t s = 0; s < n_steps && o->time < end_time; ++s) {
+        const int st = o->update(end_time);
+        if (st) return st;
+    }
+    return 0;
+}
+
+int64_t oracle_first_bad_dof(void* h) { return static_cast<Oracle*>(h)->bad_dof; }
+
+// 1D operators and the change-of-basis matrix, for the known-answer tests
+int oracle_operators(void* h, double* w, double* D, double* cbm)
+{
+    auto* o = static_cast<Oracle*>(h);
+    if (w) std::memcpy(w, o->w.data(), sizeof(double) * o->P);
+    if (D) std::memcpy(D, o->D.data(), sizeof(double) * o->P * o->P);
+    if (cbm) std::memcpy(cbm, o->cbm.data(), sizeof(double) * o->P3 * o->P3);
+    return 0;
+}
+
+// Flux functions in isolation (NavierStokes known-answer / invariance tests):
+// which = 0 get_inv_surf_flux, 1 get_inv_vol_flux, 2 hllc_xflux, 3 rusanov_xflux, 4 ausm x flux
+int oracle_flux(const plens_params* p, int which, const double* l, const double* r, const double* n, double blender, double* f)
+{
+    NavierStokes ns{};
+    ns.gma = p->gamma; ns.R = p->R; ns.Pr = p->Pr; ns.mu0 = p->mu0; ns.T0 = p->T0; ns.S = p->S;
+    ns.isf = p->inv_surf_flux; ns.ivf = p->inv_vol_flux;
+    ns.set_flux_blender_value(blender);
+    const State L{{l[0], l[1], l[2], l[3], l[4]}}, Rr{{r[0], r[1], r[2], r[3], r[4]}};
+    const Vec N{{n[0], n[1], n[2]}};
+    State F;
+    switch (which) {
+    case 0: ns.get_inv_surf_flux(L, Rr, N, F); break;
+    case 1: ns.get_inv_vol_flux(L, Rr, N, F); break;
+    case 2: ns.hllc_xflux(L, Rr, F); break;
+    case 3: ns.rusanov_xflux(L, Rr, F); break;
+    case 4: ns.ausm_plus_up_xflux(L, Rr, F); break;
+    default: return 1;
+    }
+    for (int v = 0; v < 5; ++v) f[v] = F[v];
+    return 0;
+}
+
+// Blender of one cell from its nodal blender-variable values (BlenderCalculator::get_blender).
+double oracle_cell_blender(void* h, const double* var)
+{
+    auto* o = static_cast<Oracle*>(h);
+    std::vector<double> save(o->bvar.begin(), o->bvar.begin() + o->P3);
+    std::copy(var, var + o->P3, o->bvar.begin());
+    const double a = o->get_blender(0);
+    std::copy(save.begin(), save.end(), o->bvar.begin());
+    return a;
+}
+
+}  // extern "C"

@@ -1,0 +1,383 @@
+"""Python host mirror of the reference's solver interface, over the two C ABIs.
+
+``Case`` is the setup chain (PLENS::PLENS ... read_time_settings, dgsem/plens.cc:13-1499): it
+parses input.prm text and owns the mesh description, parameters and initial state.
+``GpuSolver`` is the hot path on the GPU (PLENS::calc_rhs / calc_time_step / update,
+dgsem/plens.cc:3688-4518) through include/plens_gpu.h. Errors raise ``PlensError`` with the
+library's message; a positivity failure raises ``PositivityError`` carrying the first bad dof
+(the reference prints the dof location and calls std::exit, dgsem/plens.cc:2531-2546).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_DIR = _PKG / "lib"
+
+PLENS_GPU_OK = 0
+PLENS_GPU_E_INVALID = 1
+PLENS_GPU_E_CUDA = 2
+PLENS_GPU_E_POSITIVITY = 3
+PLENS_GPU_E_TIMEOUT = 4
+
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+SENSOR_MODAL = 0
+SENSOR_LEARNED = 1
+MLP_N_PARAMS = 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1
+
+
+class PlensError(RuntimeError):
+    pass
+
+
+class PositivityError(PlensError):
+    def __init__(self, msg: str, dof: int):
+        super().__init__(msg)
+        self.dof = dof
+
+
+class BCDesc(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32), ("expr_p", C.c_int32), ("expr_T", C.c_int32),
+        ("expr_vel", C.c_int32 * 3), ("p", C.c_double), ("T", C.c_double),
+        ("vel", C.c_double * 3), ("cons", C.c_double * 5),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("degree", C.c_int32),
+        ("gamma", C.c_double), ("R", C.c_double), ("Pr", C.c_double), ("mu0", C.c_double),
+        ("T0", C.c_double), ("S", C.c_double),
+        ("const_viscosity", C.c_int32), ("inv_surf_flux", C.c_int32), ("inv_vol_flux", C.c_int32),
+        ("plens_2d", C.c_int32), ("blender_variable", C.c_int32), ("blender_function", C.c_int32),
+        ("threshold_factor", C.c_double), ("threshold_exp_factor", C.c_double),
+        ("sharpness_factor", C.c_double), ("alpha_min", C.c_double), ("alpha_max", C.c_double),
+        ("expr_wall_blender_limit", C.c_int32), ("expr_vis_blending_region", C.c_int32),
+        ("expr_courant", C.c_int32), ("do_filtering", C.c_int32), ("rk_order", C.c_int32),
+        ("precision", C.c_int32), ("sensor", C.c_int32), ("judge_every", C.c_int32),
+        ("judge_alpha_tol", C.c_double),
+        ("n_bc", C.c_int32), ("bcs", C.POINTER(BCDesc)),
+        ("n_expr", C.c_int32), ("expr_offset", C.POINTER(C.c_int32)),
+        ("expr_length", C.POINTER(C.c_int32)),
+        ("n_expr_insn", C.c_int32), ("expr_code", C.c_void_p),
+    ]
+
+
+_host = None
+_gpu = None
+
+
+def _load(name: str) -> C.CDLL:
+    path = LIB_DIR / name
+    if not path.exists():
+        raise PlensError(f"{path} is missing: build it with __graft_entry__.build() or "
+                         "python -m plens_gb300.build")
+    return C.CDLL(str(path))
+
+
+def host_lib() -> C.CDLL:
+    global _host
+    if _host is None:
+        L = _load("libplens_host.so")
+        vp, i64, dbl, i32 = C.c_void_p, C.c_int64, C.c_double, C.c_int32
+        L.plens_case_create.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.POINTER(vp)]
+        L.plens_case_last_error.restype = C.c_char_p
+        L.plens_case_destroy.argtypes = [vp]
+        L.plens_case_mesh.argtypes = [vp]
+        L.plens_case_mesh.restype = vp
+        L.plens_case_params.argtypes = [vp]
+        L.plens_case_params.restype = vp
+        L.plens_case_params_mut.argtypes = [vp]
+        L.plens_case_params_mut.restype = C.POINTER(Params)
+        L.plens_case_n_cells.argtypes = [vp]
+        L.plens_case_n_cells.restype = i64
+        L.plens_case_n_dofs.argtypes = [vp]
+        L.plens_case_n_dofs.restype = i64
+        L.plens_case_initial_state.argtypes = [vp, vp]
+        L.plens_case_dof_xyz.argtypes = [vp, vp]
+        L.plens_case_start_time.argtypes = [vp]
+        L.plens_case_start_time.restype = dbl
+        L.plens_case_end_time.argtypes = [vp]
+        L.plens_case_end_time.restype = dbl
+        L.plens_case_eval_expr.argtypes = [vp, i32, dbl, dbl, dbl, dbl]
+        L.plens_case_eval_expr.restype = dbl
+        L.plens_case_prm_echo.argtypes = [vp]
+        L.plens_case_prm_echo.restype = C.c_char_p
+        L.plens_expr_eval_string.argtypes = [C.c_char_p, dbl, dbl, dbl, dbl, C.POINTER(dbl)]
+        L.plens_gll_1d.argtypes = [C.c_int, vp, vp]
+        _host = L
+    return _host
+
+
+def gpu_lib() -> C.CDLL:
+    """The CUDA library. Raises if it was not built: there is no CPU fallback for the hot path."""
+    global _gpu
+    if _gpu is None:
+        L = _load("libplens_gpu.so")
+        vp, i64, dbl, i32 = C.c_void_p, C.c_int64, C.c_double, C.c_int32
+        L.plens_gpu_create.argtypes = [vp, vp, C.POINTER(vp)]
+        L.plens_gpu_destroy.argtypes = [vp]
+        L.plens_gpu_last_error.argtypes = [vp]
+        L.plens_gpu_last_error.restype = C.c_char_p
+        L.plens_gpu_kernel_launches.argtypes = [vp]
+        L.plens_gpu_kernel_launches.restype = i64
+        L.plens_gpu_stream.argtypes = [vp]
+        L.plens_gpu_stream.restype = vp
+        L.plens_gpu_set_state.argtypes = [vp, vp]
+        L.plens_gpu_get_state.argtypes = [vp, vp]
+        L.plens_gpu_set_time.argtypes = [vp, dbl, i64]
+        L.plens_gpu_get_time.argtypes = [vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(dbl)]
+        L.plens_gpu_rhs.argtypes = [vp, vp]
+        L.plens_gpu_time_step.argtypes = [vp, C.POINTER(dbl)]
+        L.plens_gpu_advance.argtypes = [vp, i64, dbl]
+        L.plens_gpu_advance_async.argtypes = [vp, i64, dbl]
+        L.plens_gpu_synchronize.argtypes = [vp]
+        L.plens_gpu_get_cell_scalars.argtypes = [vp, vp, vp, vp]
+        L.plens_gpu_get_avars.argtypes = [vp, vp]
+        L.plens_gpu_first_bad_dof.argtypes = [vp, C.POINTER(i64)]
+        L.plens_gpu_set_sensor_weights.argtypes = [vp, vp]
+        L.plens_gpu_sensor_stats.argtypes = [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(dbl), C.POINTER(i64)]
+        L.plens_gpu_sensor_pairs.argtypes = [vp, vp, vp]
+        L.plens_gpu_mlp_train.argtypes = [vp, vp, i64, vp, i32, i32, C.c_float, C.c_float, C.c_uint64, vp]
+        L.plens_gpu_mlp_loss_grad.argtypes = [vp, vp, i64, vp, C.c_float, C.POINTER(C.c_float), vp]
+        L.plens_gpu_mlp_infer.argtypes = [vp, i64, vp, C.c_float, vp]
+        L.plens_gpu_set_kernel_timing.argtypes = [vp, C.c_int]
+        L.plens_gpu_kernel_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(i64)]
+        _gpu = L
+    return _gpu
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Case:
+    """input.prm text -> mesh description, parameters and initial state (host only)."""
+
+    def __init__(self, prm_text: str, fe_degree: int, mapping_degree: int = 2, base_dir: str = "."):
+        L = host_lib()
+        h = C.c_void_p()
+        rc = L.plens_case_create(prm_text.encode(), str(base_dir).encode(), mapping_degree,
+                                 fe_degree, C.byref(h))
+        if rc != 0:
+            raise PlensError(L.plens_case_last_error().decode())
+        self._h = h
+        self._L = L
+        self.degree = fe_degree
+        self.n_cells = L.plens_case_n_cells(h)
+        self.n_dofs = L.plens_case_n_dofs(h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._L.plens_case_destroy(h)
+            self._h = None
+
+    @property
+    def mesh_ptr(self) -> int:
+        return self._L.plens_case_mesh(self._h)
+
+    @property
+    def params_ptr(self) -> int:
+        return self._L.plens_case_params(self._h)
+
+    @property
+    def params(self) -> Params:
+        return self._L.plens_case_params_mut(self._h).contents
+
+    def initial_state(self) -> np.ndarray:
+        U = np.empty((5, self.n_dofs), dtype=np.float64)
+        self._L.plens_case_initial_state(self._h, _ptr(U))
+        return U
+
+    def dof_xyz(self) -> np.ndarray:
+        X = np.empty((3, self.n_dofs), dtype=np.float64)
+        self._L.plens_case_dof_xyz(self._h, _ptr(X))
+        return X
+
+    @property
+    def start_time(self) -> float:
+        return self._L.plens_case_start_time(self._h)
+
+    @property
+    def end_time(self) -> float:
+        return self._L.plens_case_end_time(self._h)
+
+    def eval_expr(self, idx: int, x=0.0, y=0.0, z=0.0, t=0.0) -> float:
+        return self._L.plens_case_eval_expr(self._h, idx, x, y, z, t)
+
+    def prm_echo(self) -> str:
+        return self._L.plens_case_prm_echo(self._h).decode()
+
+
+def eval_expression(src: str, x=0.0, y=0.0, z=0.0, t=0.0) -> float:
+    L = host_lib()
+    out = C.c_double()
+    if L.plens_expr_eval_string(src.encode(), x, y, z, t, C.byref(out)) != 0:
+        raise PlensError(L.plens_case_last_error().decode())
+    return out.value
+
+
+def gll_1d(n: int):
+    x = np.empty(n)
+    w = np.empty(n)
+    if host_lib().plens_gll_1d(n, _ptr(x), _ptr(w)) != 0:
+        raise PlensError(host_lib().plens_case_last_error().decode())
+    return x, w
+
+
+class GpuSolver:
+    """The GPU hot path for one Case (plens_gpu_create ... plens_gpu_destroy)."""
+
+    def __init__(self, case: Case):
+        self.L = gpu_lib()
+        self.case = case
+        h = C.c_void_p()
+        rc = self.L.plens_gpu_create(case.mesh_ptr, case.params_ptr, C.byref(h))
+        if rc != 0:
+            msg = self.L.plens_gpu_last_error(h).decode() if h else "plens_gpu_create failed"
+            raise PlensError(f"plens_gpu_create: {msg} (status {rc})")
+        self.h = h
+        self.n_dofs = case.n_dofs
+        self.n_cells = case.n_cells
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.plens_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc: int, what: str):
+        if rc == PLENS_GPU_OK:
+            return
+        msg = self.L.plens_gpu_last_error(self.h).decode()
+        if rc == PLENS_GPU_E_POSITIVITY:
+            d = C.c_int64(-1)
+            self.L.plens_gpu_first_bad_dof(self.h, C.byref(d))
+            raise PositivityError(f"{what}: {msg}", d.value)
+        raise PlensError(f"{what}: {msg} (status {rc})")
+
+    @property
+    def kernel_launches(self) -> int:
+        return self.L.plens_gpu_kernel_launches(self.h)
+
+    @property
+    def stream(self) -> int:
+        return self.L.plens_gpu_stream(self.h) or 0
+
+    def set_state(self, U: np.ndarray, t: float | None = None, n_steps: int = 0):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        assert U.shape == (5, self.n_dofs)
+        self._check(self.L.plens_gpu_set_state(self.h, _ptr(U)), "set_state")
+        if t is not None:
+            self._check(self.L.plens_gpu_set_time(self.h, t, n_steps), "set_time")
+
+    def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        U = out if out is not None else np.empty((5, self.n_dofs))
+        self._check(self.L.plens_gpu_get_state(self.h, _ptr(U)), "get_state")
+        return U
+
+    def get_time(self):
+        t, n, dt = C.c_double(), C.c_int64(), C.c_double()
+        self._check(self.L.plens_gpu_get_time(self.h, C.byref(t), C.byref(n), C.byref(dt)), "get_time")
+        return t.value, n.value, dt.value
+
+    def rhs(self) -> np.ndarray:
+        R = np.empty((5, self.n_dofs))
+        self._check(self.L.plens_gpu_rhs(self.h, _ptr(R)), "rhs")
+        return R
+
+    def time_step(self) -> float:
+        dt = C.c_double()
+        self._check(self.L.plens_gpu_time_step(self.h, C.byref(dt)), "time_step")
+        return dt.value
+
+    def advance(self, n_steps: int, end_time: float = 1e300):
+        self._check(self.L.plens_gpu_advance(self.h, n_steps, end_time), "advance")
+
+    def advance_async(self, n_steps: int, end_time: float = 1e300):
+        self._check(self.L.plens_gpu_advance_async(self.h, n_steps, end_time), "advance_async")
+
+    def synchronize(self):
+        self._check(self.L.plens_gpu_synchronize(self.h), "synchronize")
+
+    def cell_scalars(self):
+        a = np.empty(self.n_cells)
+        ad = np.empty(self.n_cells)
+        dt = np.empty(self.n_cells)
+        self._check(self.L.plens_gpu_get_cell_scalars(self.h, _ptr(a), _ptr(ad), _ptr(dt)), "cell_scalars")
+        return a, ad, dt
+
+    def avars(self) -> np.ndarray:
+        A = np.empty((9, self.n_dofs))
+        self._check(self.L.plens_gpu_get_avars(self.h, _ptr(A)), "avars")
+        return A
+
+    def set_kernel_timing(self, enable: bool):
+        self._check(self.L.plens_gpu_set_kernel_timing(self.h, 1 if enable else 0), "set_kernel_timing")
+
+    def kernel_timing(self):
+        ms, n = C.c_double(), C.c_int64()
+        self._check(self.L.plens_gpu_kernel_timing(self.h, C.byref(ms), C.byref(n)), "kernel_timing")
+        return ms.value, n.value
+
+    def set_sensor_weights(self, params: np.ndarray):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        assert p.size == MLP_N_PARAMS
+        self._check(self.L.plens_gpu_set_sensor_weights(self.h, _ptr(p)), "set_sensor_weights")
+
+    def sensor_stats(self):
+        j, f, lo = C.c_int64(), C.c_int64(), C.c_int64()
+        e = C.c_double()
+        self._check(self.L.plens_gpu_sensor_stats(self.h, C.byref(j), C.byref(f), C.byref(e), C.byref(lo)), "sensor_stats")
+        return {"judged": j.value, "fallbacks": f.value, "max_alpha_err": e.value, "lo_cells_last": lo.value}
+
+    def sensor_pairs(self):
+        x = np.empty((self.n_cells, 64), dtype=np.float32)
+        y = np.empty(self.n_cells, dtype=np.float32)
+        self._check(self.L.plens_gpu_sensor_pairs(self.h, _ptr(x), _ptr(y)), "sensor_pairs")
+        return x, y
+
+
+def mlp_train(x: np.ndarray, y: np.ndarray, params: np.ndarray, epochs=20, batch=4096, lr=1e-3,
+              alpha_max=0.5, seed=0):
+    L = gpu_lib()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32).copy()
+    loss = np.zeros(epochs, dtype=np.float32)
+    rc = L.plens_gpu_mlp_train(_ptr(x), _ptr(y), len(y), _ptr(p), epochs, batch, lr, alpha_max, seed, _ptr(loss))
+    if rc != 0:
+        raise PlensError(f"plens_gpu_mlp_train failed with status {rc}")
+    return p, loss
+
+
+def mlp_loss_grad(x: np.ndarray, y: np.ndarray, params: np.ndarray, alpha_max=0.5):
+    L = gpu_lib()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    g = np.zeros(MLP_N_PARAMS, dtype=np.float32)
+    loss = C.c_float()
+    rc = L.plens_gpu_mlp_loss_grad(_ptr(x), _ptr(y), len(y), _ptr(p), alpha_max, C.byref(loss), _ptr(g))
+    if rc != 0:
+        raise PlensError(f"plens_gpu_mlp_loss_grad failed with status {rc}")
+    return loss.value, g
+
+
+def mlp_infer(x: np.ndarray, params: np.ndarray, alpha_max=0.5) -> np.ndarray:
+    L = gpu_lib()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    out = np.empty(x.shape[0], dtype=np.float32)
+    rc = L.plens_gpu_mlp_infer(_ptr(x), x.shape[0], _ptr(p), alpha_max, _ptr(out))
+    if rc != 0:
+        raise PlensError(f"plens_gpu_mlp_infer failed with status {rc}")
+    return out

@@ -1,0 +1,989 @@
+// kernels.cuh -- the hot-path kernels, templated on P = N+1 and on the arithmetic type T
+// (double: plain path; float: mixed path, with state, metrics, registers and the RK update kept
+// in double). One block handles CellBlock<P>::CPB cells with one thread per GLL node.
+#pragma once
+
+#include "device.cuh"
+#include "flux.cuh"
+
+namespace plens_gpu {
+
+struct StageArgs {
+    int mode;        // 0: write the unscaled residual to Rout; 1: RK4 stage; 2: RK3 stage
+    int stage;       // 1..5 (RK4) or 1..3 (RK3)
+    double* Rout;
+    double* Rw;      // register receiving dt*R (RK4)
+    const double* R0;
+    const double* R1;
+    double c0, c1, c2;
+    int lo_from_list;  // 1: the subcell residual runs only on cells of the compacted list
+};
+
+// ------------------------------------------------------------------------ step bookkeeping
+
+static __global__ void k_step_begin(Dev dv, double end_time)
+{
+    Scalars* s = dv.sc;
+    s->end_time = end_time;
+    s->active = (s->err == 0 && s->time < end_time) ? 1 : 0;
+    s->dtmin = ord_double(1e6);
+}
+
+// dt after the global min-reduction; the clip to end_time affects the clock only, the RHS is
+// multiplied by the unclipped value (loc_time_steps is set before the clip in update_rk4,
+// dgsem/plens.cc:3903-3911 and 4339-4341)
+static __global__ void k_dt_finalize(Dev dv)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const double dt = unord_double(s->dtmin);
+    s->dt_update = dt;
+    s->dt = (dt > (s->end_time - s->time)) ? s->end_time - s->time : dt;
+}
+
+static __global__ void k_clock(Dev dv)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    s->time += s->dt;
+    s->n_steps += 1;
+}
+
+// --------------------------------------------------------------------------- time step
+// PLENS::calc_time_step (dgsem/plens.cc:3810-3912): per-dof stable step, min over dofs.
+template <int P>
+__global__ void __launch_bounds__(256) k_time_step(Dev dv, GasP g, double N15, int N)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    constexpr int P3 = P * P * P;
+    __shared__ double s_red[8];
+    double local = 1e6;
+    const int64_t dof = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (dof < dv.nd) {
+        const int64_t c = dof / P3;
+        double cs[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) cs[v] = dv.U[v * dv.nd + dof];
+        const double a = sqrt(g.gamma * get_p(cs, g.gamma) / cs[0]);
+        const double vel[3] = {cs[1] / cs[0], cs[2] / cs[0], cs[3] / cs[0]};
+        double adv[3];
+#pragma unroll
+        for (int row = 0; row < 3; ++row) {
+            double acc = 0.0;
+#pragma unroll
+            for (int col = 0; col < 3; ++col) acc += dv.Jinv[(col * 3 + row) * dv.nd + dof] * vel[col];
+            adv[row] = acc;
+        }
+        double madv = adv[0];
+        if (adv[1] > madv) madv = adv[1];
+        if (adv[2] > madv) madv = adv[2];
+        double mu = 0.0;
+        if (!g.inviscid) {
+            const double T = get_e(cs) / (g.R / (g.gamma - 1));
+            mu = g.const_visc ? g.mu0 : g.mu0 * pow(T / g.T0, 1.5) * (g.T0 + g.S) / (T + g.S);
+        }
+        const double h = dv.h_min[c];
+        const double Co = s->courant;
+        const double cur = Co / (N15 * (madv + a / h + (double)(N * N) * mu / (h * h * cs[0])));
+        if (cur < local) local = cur;
+    }
+    // warp-shuffle min, then block min, then one atomic per block
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double o = __shfl_xor_sync(0xffffffffu, local, off);
+        if (o < local) local = o;
+    }
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = s_red[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            if (s_red[w] < m) m = s_red[w];
+        atomicMin(&s->dtmin, ord_double(m));
+    }
+}
+
+// Courant number of the step from its expression of t (capped to 0.9 when >= 1,
+// dgsem/plens.cc:3815-3823).
+static __global__ void k_courant(Dev dv, int expr_courant)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    double Co = eval_expr(dv, expr_courant, 0, 0, 0, s->time);
+    if (Co >= 1) Co = 0.9;
+    s->courant = Co;
+}
+
+// ------------------------------------------------------------------------------- blender
+// calc_blender's first half + BlenderCalculator::get_blender / get_trouble
+// (dgsem/plens.cc:2858-2924, dgsem/blender_calculator.cc:123-177, 277-303), with
+// assert_positivity (dgsem/plens.cc:2531-2546) fused in.
+template <int P>
+__global__ void __launch_bounds__(CellBlock<P>::THREADS) k_blender(Dev dv, Ops ops, GasP g, BlendP bp)
+{
+    using CB = CellBlock<P>;
+    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1;
+    __shared__ double sA[CPB][P3];
+    __shared__ double sB[CPB][P3];
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    if (bp.gate && !s->sensor_fallback) return;
+    const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
+    const int64_t cell = (int64_t)blockIdx.x * CPB + cl;
+    const bool valid = (cl < CPB) && (cell < dv.nc);
+    const int i = node % P, j = (node / P) % P, k = node / P2;
+    if (valid) {
+        const int64_t dof = cell * P3 + node;
+        double c[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) c[v] = dv.U[v * dv.nd + dof];
+        if (!(c[0] > 0) || !(get_e(c) > 0)) {
+            atomicMin(&s->bad_dof, (long long)dof);
+            s->err = PLENS_GPU_E_POSITIVITY;
+        }
+        const double p = get_p(c, g.gamma);
+        sA[cl][node] = (bp.var == 2) ? c[0] : (bp.var == 1) ? p : p * c[0];
+    }
+    __syncthreads();
+    // separable nodal -> modal transform: x, then y, then z
+    if (valid) {
+        double acc = 0;
+#pragma unroll
+        for (int m = 0; m < P; ++m) acc += ops.C1[i * P + m] * sA[cl][m + P * j + P2 * k];
+        sB[cl][node] = acc;
+    }
+    __syncthreads();
+    if (valid) {
+        double acc = 0;
+#pragma unroll
+        for (int m = 0; m < P; ++m) acc += ops.C1[j * P + m] * sB[cl][i + P * m + P2 * k];
+        sA[cl][node] = acc;
+    }
+    __syncthreads();
+    if (valid) {
+        double acc = 0;
+#pragma unroll
+        for (int m = 0; m < P; ++m) acc += ops.C1[k * P + m] * sA[cl][i + P * j + P2 * m];
+        sB[cl][node] = acc;
+    }
+    __syncthreads();
+    if (valid && node == 0) {
+        double et = 0, e1 = 0, e2 = 0, asum = 0, ub = 0, tl = 0;
+        for (int m = 0; m < P3; ++m) {
+            const double md = sB[cl][m];
+            const int mi = m % P, mj = (m / P) % P, mk = m / P2;
+            et += md * md;
+            if (mi < N && mj < N && mk < N) e1 += md * md;
+            if (mi < N - 1 && mj < N - 1 && mk < N - 1) e2 += md * md;
+            if (bp.do_filter) {
+                const double t = fabs(md);
+                asum += t;
+                const double x = t * (ops.tv[mi] + ops.tv[mj] + ops.tv[mk]);
+                ub += x;
+                if (mi <= 1 && mj <= 1 && mk <= 1) tl += x;
+            }
+        }
+        double trouble = 1 - e1 / et;
+        if (N > 2) {
+            const double t2 = 1 - e2 / e1;
+            if (t2 > trouble) trouble = t2;
+        }
+        double alpha;
+        if (bp.func == 0) {
+            const double at = 1 / (1 + exp(-bp.sharp * (trouble / bp.thr - 1)));
+            alpha = (at < bp.amin) ? 0.0 : (at < bp.amax ? at : bp.amax);
+        } else {
+            const double at = trouble / bp.thr;
+            alpha = (at > 1) ? 1.0 : at;
+        }
+        if (dv.cell_wall[cell]) {
+            const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
+            alpha = (wl > alpha) ? wl : alpha;
+        }
+        dv.alpha_raw[cell] = alpha;
+        if (bp.do_filter) {
+            dv.tvstat[cell] = asum;
+            dv.tvstat[dv.nc + cell] = ub;
+            dv.tvstat[2 * dv.nc + cell] = tl;
+        }
+    }
+}
+
+// neighbour smoothing over interior faces against the pre-smoothing values, optional TV filter
+// and alpha_d (dgsem/plens.cc:2926-2961, blender_calculator.cc:196-259)
+static __global__ void k_alpha_smooth(Dev dv, BlendP bp)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    if (bp.gate && !s->sensor_fallback) return;
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= dv.nc) return;
+    double a = dv.alpha_raw[c];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        const int32_t nb = dv.cell_nbr[6 * c + f];
+        if (nb < 0) continue;
+        const double h = 0.5 * dv.alpha_raw[nb];
+        a = (h > a) ? h : a;
+    }
+    if (bp.do_filter && !(a > bp.amin)) {
+        const double asum = dv.tvstat[c], ub = dv.tvstat[dv.nc + c], tl = dv.tvstat[2 * dv.nc + c];
+        if (!(ub < 1e-2 * asum)) a = a + (bp.amax - a) * (1 - tl / ub);
+    }
+    dv.alpha[c] = a;
+    const double* x = dv.center + 3 * c;
+    dv.alpha_d[c] = (eval_expr(dv, bp.expr_vis, x[0], x[1], x[2], s->time) > 0) ? ((1.0 < a / bp.amax) ? 1.0 : a / bp.amax) : 0.0;
+    if (dv.lo_list && a > 0) {  // compacted troubled-cell list (learned-sensor contexts)
+        const int k = atomicAdd(dv.lo_count, 1);
+        dv.lo_list[k] = (int32_t)c;
+    }
+}
+
+// --------------------------------------------------------------------------- BC ghosts
+// get_ghost_stage{1,2,3} of the BCs:: classes (IBCs/*.cc). Prescribed states are formed in double.
+template <class T>
+__device__ __forceinline__ void prim_to_cons_d(double rho, const double v[3], double p, double gma, T out[5])
+{
+    double c4 = p / (gma - 1);
+    double c[5];
+    c[0] = rho;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        c[1 + d] = rho * v[d];
+        c4 += 0.5 * rho * v[d] * v[d];
+    }
+    c[4] = c4;
+#pragma unroll
+    for (int v2 = 0; v2 < 5; ++v2) out[v2] = (T)c[v2];
+}
+
+template <class T>
+__device__ __forceinline__ void prim_to_cons_t(T rho, const T v[3], T p, T gma, T c[5])
+{
+    c[0] = rho;
+    T c4 = p / (gma - 1);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        c[1 + d] = rho * v[d];
+        c4 += T(0.5) * rho * v[d] * v[d];
+    }
+    c[4] = c4;
+}
+
+template <class T>
+__device__ void bc_ghost(int stage, const Dev& dv, const GasP& g, const plens_bc_desc& b,
+                         const T c[5], const T av[9], const T n[3], const double* xyz, double t,
+                         int64_t partner_dof, T cg[5], T ag[9])
+{
+    const T gm = (T)g.gamma;
+#pragma unroll
+    for (int v = 0; v < 9; ++v) ag[v] = av[v];
+    switch (b.type) {
+    case PLENS_BC_PERIODIC:
+#pragma unroll
+        for (int v = 0; v < 5; ++v) cg[v] = (T)dv.U[v * dv.nd + partner_dof];
+        if (stage == 3)
+#pragma unroll
+            for (int v = 0; v < 9; ++v) ag[v] = (T)dv.avars[v * dv.nd + partner_dof];
+        return;
+    case PLENS_BC_OUTFLOW: {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) cg[v] = c[v];
+        if (stage == 2 && !g.inviscid) {
+            const T ri = T(1) / c[0];
+            T sp = (c[1] * c[1]) * (ri * ri);
+            sp += (c[2] * c[2]) * (ri * ri);
+            sp += (c[3] * c[3]) * (ri * ri);
+            const T pin = get_p(c, gm);
+            const T M = dsqrt(sp) / dsqrt(gm * pin / c[0]);
+            if (!(M >= T(1))) cg[4] += T(2) * ((T)b.p - pin) / (gm - 1);
+        }
+        return;
+    }
+    case PLENS_BC_UNIFORM_INFLOW:
+        if (stage == 2) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) cg[v] = (T)b.cons[v];
+        } else {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) cg[v] = T(2) * (T)b.cons[v] - c[v];
+        }
+        return;
+    case PLENS_BC_VARYING_INFLOW: {
+        const double p = eval_expr(dv, b.expr_p, xyz[0], xyz[1], xyz[2], t);
+        const double Tt = eval_expr(dv, b.expr_T, xyz[0], xyz[1], xyz[2], t);
+        double vel[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) vel[d] = eval_expr(dv, b.expr_vel[d], xyz[0], xyz[1], xyz[2], t);
+        T cp[5];
+        prim_to_cons_d(p / (g.R * Tt), vel, p, g.gamma, cp);
+        if (stage == 2) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) cg[v] = cp[v];
+        } else {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) cg[v] = T(2) * cp[v] - c[v];
+        }
+        return;
+    }
+    case PLENS_BC_UNIFORM_TEMP_WALL:
+    case PLENS_BC_INSULATED_WALL: {
+        const T vw[3] = {(T)b.vel[0], (T)b.vel[1], (T)b.vel[2]};
+        if (stage == 2) {
+            cg[0] = c[0];
+            cg[4] = c[4];
+            if (g.inviscid) {
+                T sr[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) sr[d] = c[1 + d] - c[0] * vw[d];
+                T nsm = sr[0] * n[0];
+                nsm += sr[1] * n[1];
+                nsm += sr[2] * n[2];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) cg[1 + d] = c[1 + d] - T(2) * nsm * n[d];
+            } else {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) cg[1 + d] = T(2) * c[0] * vw[d] - c[1 + d];
+            }
+            return;
+        }
+        const T pin = get_p(c, gm);
+        const T rho_pr = (b.type == PLENS_BC_UNIFORM_TEMP_WALL) ? pin / ((T)g.R * (T)b.T) : c[0];
+        T cp[5];
+        prim_to_cons_t(rho_pr, vw, pin, gm, cp);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) cg[v] = T(2) * cp[v] - c[v];
+        if (stage == 3 && b.type == PLENS_BC_INSULATED_WALL) {
+            T nh = av[6] * n[0];
+            nh += av[7] * n[1];
+            nh += av[8] * n[2];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) ag[6 + d] = av[6 + d] - T(2) * nh * n[d];
+        }
+        return;
+    }
+    case PLENS_BC_SYMMETRY:
+    case PLENS_BC_EMPTY: {
+        if (stage == 2 && b.type == PLENS_BC_SYMMETRY) {
+            cg[0] = c[0];
+            cg[4] = c[4];
+            T nsm = c[1] * n[0];
+            nsm += c[2] * n[1];
+            nsm += c[3] * n[2];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) cg[1 + d] = c[1 + d] - T(2) * nsm * n[d];
+            return;
+        }
+        T vin[3], vpr[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) vin[d] = c[1 + d] / c[0];
+        T nv = vin[0] * n[0];
+        nv += vin[1] * n[1];
+        nv += vin[2] * n[2];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) vpr[d] = vin[d] - nv * n[d];
+        T cp[5];
+        prim_to_cons_t(c[0], vpr, get_p(c, gm), gm, cp);
+        if (stage == 2) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) cg[v] = cp[v];
+        } else {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) cg[v] = T(2) * cp[v] - c[v];
+        }
+        return;
+    }
+    case PLENS_BC_ZPG_INFLOW: {
+        const T vw[3] = {(T)b.vel[0], (T)b.vel[1], (T)b.vel[2]};
+        T cp[5];
+        prim_to_cons_t(c[0], vw, get_p(c, gm), gm, cp);
+        if (stage == 2) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) cg[v] = cp[v];
+        } else {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) cg[v] = T(2) * cp[v] - c[v];
+        }
+        return;
+    }
+    default:  // free
+#pragma unroll
+        for (int v = 0; v < 5; ++v) cg[v] = c[v];
+        return;
+    }
+}
+
+// -------------------------------------------------------------------------- surface flux
+// PLENS::calc_surf_flux (dgsem/plens.cc:1717-1913) for one stage: one thread per face dof of a
+// face task. Interior faces are computed once and written to both sides (neighbour sign +1 in
+// stage 1, -1 in stages 2 and 3); boundary faces (periodic included) once per side.
+template <int P, class T, int STAGE>
+__global__ void __launch_bounds__(128) k_surface(Dev dv, GasP g, double* out)
+{
+    constexpr int P2 = P * P, P3 = P2 * P;
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= dv.ntask * P2) return;
+    const int64_t ti = idx / P2;
+    const int q = (int)(idx - ti * P2);
+    const int64_t c = dv.ft_cell[ti];
+    const int f = dv.ft_face[ti];
+    const int bc = dv.ft_bc[ti];
+    const int64_t gd = c * P3 + face_node<P>(f, q);
+    const T gm = (T)g.gamma;
+    T cs[5], av[9] = {}, n[3];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) cs[v] = (T)dv.U[v * dv.nd + gd];
+    if (STAGE == 3) {
+#pragma unroll
+        for (int v = 0; v < 9; ++v) av[v] = (T)dv.avars[v * dv.nd + gd];
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) n[d] = (T)dv.ft_normal[(ti * P2 + q) * 3 + d];
+    T fb = T(0);
+    if (STAGE == 2) {
+        double a = (bc >= 0) ? dv.alpha[c] : 0.5 * (dv.alpha[c] + dv.alpha[dv.ft_nbr_cell[ti]]);
+        fb = (T)((a <= 0) ? 0.0 : (a <= 1 ? a : 1.0));
+    }
+    T c2[5], a2[9] = {};
+    int64_t slot_nb = -1;
+    if (bc >= 0) {
+        int64_t pd = -1;
+        const plens_bc_desc b = dv.bcs[bc];
+        if (b.type == PLENS_BC_PERIODIC)
+            pd = (int64_t)dv.ft_nbr_cell[ti] * P3 + face_node<P>(dv.ft_nbr_face[ti], dv.ft_nbr_fdof[ti * P2 + q]);
+        bc_ghost<T>(STAGE, dv, g, b, cs, av, n, dv.ft_xyz + (ti * P2 + q) * 3, s->time, pd, c2, a2);
+    } else {
+        const int64_t nb = dv.ft_nbr_cell[ti];
+        const int fn = dv.ft_nbr_face[ti];
+        const int qn = dv.ft_nbr_fdof[ti * P2 + q];
+        const int64_t gdn = nb * P3 + face_node<P>(fn, qn);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) c2[v] = (T)dv.U[v * dv.nd + gdn];
+        if (STAGE == 3) {
+#pragma unroll
+            for (int v = 0; v < 9; ++v) a2[v] = (T)dv.avars[v * dv.nd + gdn];
+        }
+        slot_nb = (nb * 6 + fn) * P2 + qn;
+    }
+    T fl[5];
+    if (STAGE == 1) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) fl[v] = T(0.5) * (cs[v] + c2[v]);
+    } else if (STAGE == 2) {
+        inv_surf_flux(cs, c2, n, gm, g.isf, fb, fl);
+    } else {
+        T f1[5], f2[5];
+        dif_flux(cs, av, n, f1);
+        dif_flux(c2, a2, n, f2);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) fl[v] = T(0.5) * (f1[v] + f2[v]);
+    }
+    const int64_t slot = (c * 6 + f) * P2 + q;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[v * dv.nslot + slot] = (double)fl[v];
+    if (slot_nb >= 0) {
+        const T sg = (STAGE == 1) ? T(1) : T(-1);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) out[v * dv.nslot + slot_nb] = (double)(sg * fl[v]);
+    }
+}
+
+// ----------------------------------------------------------------------- auxiliary variables
+// PLENS::calc_aux_vars + calc_cell_evar_grad (dgsem/plens.cc:2593-2748, 2294-2405): BR1 lifting
+// of the entropy variables, then the stress tensor and heat flux scaled by mu and k.
+template <int P, class T>
+__global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, GasP g)
+{
+    using CB = CellBlock<P>;
+    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sE = reinterpret_cast<T*>(smem_raw);        // [CPB][5][P3]
+    T* sJa = sE + CPB * 5 * P3;                     // [CPB][9][P3]
+    T* sEf = sJa + CPB * 9 * P3;                    // [CPB][6][5][P2]
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
+    const int64_t cell = (int64_t)blockIdx.x * CPB + cl;
+    const bool valid = (cl < CPB) && (cell < dv.nc);
+    const T gm = (T)g.gamma;
+    double cd[5] = {1, 0, 0, 0, 1};
+    if (valid) {
+        const int64_t dof = cell * P3 + node;
+        T c[5], e[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            cd[v] = dv.U[v * dv.nd + dof];
+            c[v] = (T)cd[v];
+        }
+        cons_to_entropy(c, gm, e);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) sE[(cl * 5 + v) * P3 + node] = e[v];
+#pragma unroll
+        for (int m = 0; m < 9; ++m) sJa[(cl * 9 + m) * P3 + node] = (T)dv.Ja[m * dv.nd + dof];
+        for (int sl = node; sl < 6 * P2; sl += P3) {
+            T fc[5], fe[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) fc[v] = (T)dv.sf[v * dv.nslot + cell * 6 * P2 + sl];
+            cons_to_entropy(fc, gm, fe);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) sEf[((cl * 6 + sl / P2) * 5 + v) * P2 + (sl % P2)] = fe[v];
+        }
+    }
+    __syncthreads();
+    if (!valid) return;
+    const int ti[3] = {node % P, (node / P) % P, node / P2};
+    const T* E = sE + cl * 5 * P3;
+    const T* J = sJa + cl * 9 * P3;
+    T grad[3][5];
+#pragma unroll
+    for (int gd = 0; gd < 3; ++gd) {
+        T acc[5] = {0, 0, 0, 0, 0};
+        for (int m = 0; m < P; ++m) {
+#pragma unroll
+            for (int md = 0; md < 3; ++md) {
+                const int lo = (md == 0) ? m + P * ti[1] + P2 * ti[2] : (md == 1) ? ti[0] + P * m + P2 * ti[2] : ti[0] + P * ti[1] + P2 * m;
+                const T jc = J[(md * 3 + gd) * P3 + lo];
+                const T dvl = (T)ops.D[ti[md] * P + m];
+#pragma unroll
+                for (int v = 0; v < 5; ++v) acc[v] += dvl * E[v * P3 + lo] * jc;
+            }
+        }
+#pragma unroll
+        for (int sd = 0; sd < 3; ++sd) {
+#pragma unroll
+            for (int lr = 0; lr < 2; ++lr) {
+                if (ti[sd] != (lr ? N : 0)) continue;
+                const int f = 2 * sd + lr;
+                const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
+                const T jc = J[(sd * 3 + gd) * P3 + node];
+                const T sgn = lr ? T(-1) : T(1);
+                const T wend = (T)ops.w[lr * N];
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    const T fin = E[v * P3 + node] * jc;
+                    const T fsu = sEf[((cl * 6 + f) * 5 + v) * P2 + q] * jc;
+                    acc[v] -= sgn * (fsu - fin) / wend;
+                }
+            }
+        }
+        const T jinv = T(1.0) / (T)dv.detJ[cell * P3 + node];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) grad[gd][v] = acc[v] * jinv;
+    }
+    const int64_t dof = cell * P3 + node;
+    T et[5];
+    {
+        T c[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) c[v] = (T)cd[v];
+        cons_to_entropy(c, gm, et);
+    }
+    T vg[3][3];
+#pragma unroll
+    for (int vd = 0; vd < 3; ++vd)
+#pragma unroll
+        for (int gd = 0; gd < 3; ++gd) vg[vd][gd] = (et[1 + vd] * grad[gd][4] / et[4] - grad[gd][1 + vd]) / et[4];
+    const T tr = vg[0][0] + vg[1][1] + vg[2][2];
+    // mu and k in double from the double state (NavierStokes::get_mu / get_k, h:348-360)
+    const double e = get_e(cd);
+    const double Tk = e / (g.R / (g.gamma - 1));
+    const double mu = g.const_visc ? g.mu0 : g.mu0 * pow(Tk / g.T0, 1.5) * (g.T0 + g.S) / (Tk + g.S);
+    const double kk = mu * g.R * g.gamma / ((g.gamma - 1) * g.Pr);
+    T tau[6];
+    int sid = 0;
+#pragma unroll
+    for (int row = 0; row < 3; ++row)
+#pragma unroll
+        for (int col = row; col < 3; ++col) {
+            tau[sid] = (col == row) ? vg[row][col] + vg[col][row] - T(2.0) / T(3) * tr : vg[row][col] + vg[col][row];
+            ++sid;
+        }
+#pragma unroll
+    for (int v = 0; v < 6; ++v) dv.avars[v * dv.nd + dof] = (double)tau[v] * mu;
+#pragma unroll
+    for (int gd = 0; gd < 3; ++gd) {
+        const T tg = grad[gd][4] / (et[4] * et[4] * (T)g.R);
+        dv.avars[(6 + gd) * dv.nd + dof] = (double)(-tg) * kk;
+    }
+}
+
+// ------------------------------------------------------------------------------ volume
+// One RHS of a cell: calc_cell_ho_inv_residual (dgsem/plens.cc:3153-3275), calc_cell_ho_dif_residual
+// (3283-3413), calc_cell_lo_inv_residual (3469-3583), the blend of calc_rhs (3753-3775), and --
+// when stepping -- multiply_time_step_to_rhs (3925-3940) and the register update of update_rk4 /
+// update_rk3 (4353-4400, 4433-4472). The two-point volume fluxes are evaluated once per node pair
+// of a line (F_im = F_mi) by one thread per line; per-direction partial sums live in shared memory
+// owned by exactly one thread, so the accumulation is deterministic.
+template <int P, class T>
+struct VolSmem {
+    static constexpr int P3 = P * P * P;
+    static constexpr int CPB = CellBlock<P>::CPB;
+    static constexpr int NQ = 7;  // rho, 1/rho, v0, v1, v2, p, beta
+    static constexpr size_t bytes(bool visc)
+    {
+        return sizeof(T) * (size_t)CPB * P3 * (NQ + 5 + 9 + 15 + (visc ? 9 : 0) + 1);
+    }
+};
+
+template <int P, class T, bool VISC>
+__global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops ops, GasP g, StageArgs sa)
+{
+    using CB = CellBlock<P>;
+    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1, NQ = 7;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sQ = reinterpret_cast<T*>(smem_raw);   // [CPB][NQ][P3]
+    T* sC = sQ + CPB * NQ * P3;               // [CPB][5][P3]
+    T* sJ = sC + CPB * 5 * P3;                // [CPB][9][P3]
+    T* sAcc = sJ + CPB * 9 * P3;              // [CPB][3][5][P3]
+    T* sAv = sAcc + CPB * 15 * P3;            // [CPB][9][P3] (viscous)
+    T* sNorm = sAv + (VISC ? CPB * 9 * P3 : 0);  // [CPB][P3] scratch
+    (void)sNorm;
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
+    const int64_t cell = (int64_t)blockIdx.x * CPB + cl;
+    const bool valid = (cl < CPB) && (cell < dv.nc);
+    const T gm = (T)g.gamma;
+    T* Q = sQ + cl * NQ * P3;
+    T* Cc = sC + cl * 5 * P3;
+    T* J = sJ + cl * 9 * P3;
+    T* Acc = sAcc + cl * 15 * P3;
+    T* Av = sAv + cl * 9 * P3;
+    const int64_t dof = cell * P3 + node;
+    double ud[5] = {0, 0, 0, 0, 0};
+    if (valid) {
+        T c[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            ud[v] = dv.U[v * dv.nd + dof];
+            c[v] = (T)ud[v];
+            Cc[v * P3 + node] = c[v];
+        }
+        // per-node quantities with the reference's own expressions
+        const T p = get_p(c, gm);
+        const T ri = T(1) / c[0];
+        Q[0 * P3 + node] = c[0];
+        Q[1 * P3 + node] = ri;
+        Q[2 * P3 + node] = c[1] * ri;
+        Q[3 * P3 + node] = c[2] * ri;
+        Q[4 * P3 + node] = c[3] * ri;
+        Q[5 * P3 + node] = p;
+        Q[6 * P3 + node] = T(0.5) * c[0] / p;
+#pragma unroll
+        for (int m = 0; m < 9; ++m) J[m * P3 + node] = (T)dv.Ja[m * dv.nd + dof];
+        if (VISC) {
+#pragma unroll
+            for (int m = 0; m < 9; ++m) Av[m * P3 + node] = (T)dv.avars[m * dv.nd + dof];
+        }
+    }
+    __syncthreads();
+    const double alpha = valid ? dv.alpha[cell] : 0.0;
+
+    // ---- phase A: two-point volume fluxes per line
+    if (valid) {
+        for (int task = node; task < 3 * P2; task += P3) {
+            const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
+            T acc[P][5];
+#pragma unroll
+            for (int i = 0; i < P; ++i)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) acc[i][v] = T(0);
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int ni = line_node<P>(dir, la, lb, i);
+                T qi[7];
+#pragma unroll
+                for (int k = 0; k < 7; ++k) qi[k] = Q[k * P3 + ni];
+                const T ci[5] = {Cc[ni], Cc[P3 + ni], Cc[2 * P3 + ni], Cc[3 * P3 + ni], Cc[4 * P3 + ni]};
+                // diagonal term m = i (the pair flux of a state with itself)
+                {
+                    T nv[3] = {J[(dir * 3) * P3 + ni], J[(dir * 3 + 1) * P3 + ni], J[(dir * 3 + 2) * P3 + ni]};
+                    nv[0] = T(0.5) * (nv[0] + nv[0]);
+                    nv[1] = T(0.5) * (nv[1] + nv[1]);
+                    nv[2] = T(0.5) * (nv[2] + nv[2]);
+                    T nn = nv[0] * nv[0];
+                    nn += nv[1] * nv[1];
+                    nn += nv[2] * nv[2];
+                    nn = dsqrt(nn);
+                    const T dn[3] = {nv[0] / nn, nv[1] / nn, nv[2] / nn};
+                    T F[5];
+                    if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) chandrashekhar_vol(qi, qi, dn, gm, F);
+                    else if (g.ivf == PLENS_IVF_KENNEDY_GRUBER) kennedy_gruber_vol(qi, qi, get_e(ci), get_e(ci), dn, gm, F);
+                    else ismail_roe_vol(ci, ci, dn, gm, F);
+                    const T dvn = T(2) * (T)ops.D[i * P + i] * nn;
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) acc[i][v] += dvn * F[v];
+                }
+#pragma unroll
+                for (int m = i + 1; m < P; ++m) {
+                    const int nm = line_node<P>(dir, la, lb, m);
+                    T qm[7];
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) qm[k] = Q[k * P3 + nm];
+                    T nv[3];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) nv[d] = T(0.5) * (J[(dir * 3 + d) * P3 + ni] + J[(dir * 3 + d) * P3 + nm]);
+                    T nn = nv[0] * nv[0];
+                    nn += nv[1] * nv[1];
+                    nn += nv[2] * nv[2];
+                    nn = dsqrt(nn);
+                    const T dn[3] = {nv[0] / nn, nv[1] / nn, nv[2] / nn};
+                    T F[5];
+                    if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) {
+                        chandrashekhar_vol(qi, qm, dn, gm, F);
+                    } else if (g.ivf == PLENS_IVF_KENNEDY_GRUBER) {
+                        const T cm[5] = {Cc[nm], Cc[P3 + nm], Cc[2 * P3 + nm], Cc[3 * P3 + nm], Cc[4 * P3 + nm]};
+                        kennedy_gruber_vol(qi, qm, get_e(ci), get_e(cm), dn, gm, F);
+                    } else {
+                        const T cm[5] = {Cc[nm], Cc[P3 + nm], Cc[2 * P3 + nm], Cc[3 * P3 + nm], Cc[4 * P3 + nm]};
+                        ismail_roe_vol(ci, cm, dn, gm, F);
+                    }
+                    const T di = T(2) * (T)ops.D[i * P + m] * nn, dm = T(2) * (T)ops.D[m * P + i] * nn;
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        acc[i][v] += di * F[v];
+                        acc[m][v] += dm * F[v];
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int ni = line_node<P>(dir, la, lb, i);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) Acc[(dir * 5 + v) * P3 + ni] = acc[i][v];
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- phase B: HO inviscid = volume + surface, scaled by 1/(-detJ)
+    const int ti[3] = {node % P, (node / P) % P, node / P2};
+    const double detJ = valid ? dv.detJ[dof] : 1.0;
+    T ho[5] = {0, 0, 0, 0, 0};
+    if (valid) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) ho[v] = Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node];
+        const T ci[5] = {Cc[node], Cc[P3 + node], Cc[2 * P3 + node], Cc[3 * P3 + node], Cc[4 * P3 + node]};
+#pragma unroll
+        for (int sd = 0; sd < 3; ++sd) {
+#pragma unroll
+            for (int lr = 0; lr < 2; ++lr) {
+                if (ti[sd] != (lr ? N : 0)) continue;
+                const int f = 2 * sd + lr;
+                const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
+                T dn[3] = {J[(sd * 3) * P3 + node], J[(sd * 3 + 1) * P3 + node], J[(sd * 3 + 2) * P3 + node]};
+                T nn = dn[0] * dn[0];
+                nn += dn[1] * dn[1];
+                nn += dn[2] * dn[2];
+                nn = dsqrt(nn);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) dn[d] /= nn;
+                T fin[5];
+                inv_flux(ci, dn, gm, fin);
+                const T ss = lr ? T(-1) : T(1);
+                const T wend = (T)ops.w[lr * N];
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    const T fs = -ss * (T)dv.sf[v * dv.nslot + (cell * 6 + f) * P2 + q];
+                    ho[v] += -ss * (fs - fin[v]) * nn / wend;
+                }
+            }
+        }
+        const T js = T(1) / (T(-1) * (T)detJ);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) ho[v] *= js;
+    }
+
+    // ---- viscous HO residual: nodal viscous fluxes along each contravariant direction
+    T hd[5] = {0, 0, 0, 0, 0};
+    if (VISC) {
+        __syncthreads();  // Acc is reused
+        if (valid) {
+            const T ci[5] = {Cc[node], Cc[P3 + node], Cc[2 * P3 + node], Cc[3 * P3 + node], Cc[4 * P3 + node]};
+            T av[9];
+#pragma unroll
+            for (int m = 0; m < 9; ++m) av[m] = Av[m * P3 + node];
+#pragma unroll
+            for (int md = 0; md < 3; ++md) {
+                T dn[3] = {J[(md * 3) * P3 + node], J[(md * 3 + 1) * P3 + node], J[(md * 3 + 2) * P3 + node]};
+                T nn = dn[0] * dn[0];
+                nn += dn[1] * dn[1];
+                nn += dn[2] * dn[2];
+                nn = dsqrt(nn);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) dn[d] /= nn;
+                T F[5];
+                dif_flux(ci, av, dn, F);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) Acc[(md * 5 + v) * P3 + node] = F[v] * nn;
+            }
+        }
+        __syncthreads();
+        if (valid) {
+            for (int m = 0; m < P; ++m) {
+#pragma unroll
+                for (int md = 0; md < 3; ++md) {
+                    const int lo = (md == 0) ? m + P * ti[1] + P2 * ti[2] : (md == 1) ? ti[0] + P * m + P2 * ti[2] : ti[0] + P * ti[1] + P2 * m;
+                    const T dvl = (T)ops.D[ti[md] * P + m];
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) hd[v] += dvl * Acc[(md * 5 + v) * P3 + lo];
+                }
+            }
+            const T ci[5] = {Cc[node], Cc[P3 + node], Cc[2 * P3 + node], Cc[3 * P3 + node], Cc[4 * P3 + node]};
+            T av[9];
+#pragma unroll
+            for (int m = 0; m < 9; ++m) av[m] = Av[m * P3 + node];
+#pragma unroll
+            for (int sd = 0; sd < 3; ++sd) {
+#pragma unroll
+                for (int lr = 0; lr < 2; ++lr) {
+                    if (ti[sd] != (lr ? N : 0)) continue;
+                    const int f = 2 * sd + lr;
+                    const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
+                    T dn[3] = {J[(sd * 3) * P3 + node], J[(sd * 3 + 1) * P3 + node], J[(sd * 3 + 2) * P3 + node]};
+                    T nn = dn[0] * dn[0];
+                    nn += dn[1] * dn[1];
+                    nn += dn[2] * dn[2];
+                    nn = dsqrt(nn);
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) dn[d] /= nn;
+                    T fin[5];
+                    dif_flux(ci, av, dn, fin);
+                    const T ss = lr ? T(-1) : T(1);
+                    const T wend = (T)ops.w[lr * N];
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        const T fs = -ss * (T)dv.sf3[v * dv.nslot + (cell * 6 + f) * P2 + q];
+                        hd[v] += -ss * (fs - fin[v]) * nn / wend;
+                    }
+                }
+            }
+            const T js = T(1) / (T(1) * (T)detJ);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) hd[v] *= js;
+        }
+    }
+
+    // ---- phase C: first-order subcell residual, only where alpha > 0
+    T lo[5] = {0, 0, 0, 0, 0};
+    bool any_lo = false;
+#pragma unroll
+    for (int k = 0; k < CPB; ++k) {
+        const int64_t ck = (int64_t)blockIdx.x * CPB + k;
+        if (ck < dv.nc && dv.alpha[ck] > 0) any_lo = true;
+    }
+    if (any_lo) {
+        __syncthreads();
+        const bool do_lo = valid && alpha > 0;
+        if (do_lo) {
+            const T fb = (T)((alpha <= 0) ? 0.0 : (alpha <= 1 ? alpha : 1.0));
+            for (int task = node; task < 3 * P2; task += P3) {
+                const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
+                T acc[P][5];
+#pragma unroll
+                for (int i = 0; i < P; ++i)
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) acc[i][v] = T(0);
+                // running subcell normal n_(i-1,i) = Ja_0 + sum_{l<i} sum_m Q_lm Ja_m
+                // (metric_terms.cc:106-141)
+                const int n0 = line_node<P>(dir, la, lb, 0);
+                T sn[3] = {J[(dir * 3) * P3 + n0], J[(dir * 3 + 1) * P3 + n0], J[(dir * 3 + 2) * P3 + n0]};
+#pragma unroll
+                for (int id = 1; id < P; ++id) {
+#pragma unroll
+                    for (int m = 0; m < P; ++m) {
+                        const int nm = line_node<P>(dir, la, lb, m);
+                        const T qlm = (T)ops.Q[(id - 1) * P + m];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) sn[d] += qlm * J[(dir * 3 + d) * P3 + nm];
+                    }
+                    const int nl = line_node<P>(dir, la, lb, id - 1), nr = line_node<P>(dir, la, lb, id);
+                    T nn = sn[0] * sn[0];
+                    nn += sn[1] * sn[1];
+                    nn += sn[2] * sn[2];
+                    nn = dsqrt(nn);
+                    const T dn[3] = {sn[0] / nn, sn[1] / nn, sn[2] / nn};
+                    const T cL[5] = {Cc[nl], Cc[P3 + nl], Cc[2 * P3 + nl], Cc[3 * P3 + nl], Cc[4 * P3 + nl]};
+                    const T cR[5] = {Cc[nr], Cc[P3 + nr], Cc[2 * P3 + nr], Cc[3 * P3 + nr], Cc[4 * P3 + nr]};
+                    T F[5];
+                    inv_surf_flux(cL, cR, dn, gm, g.isf, fb, F);
+                    const T wl = (T)ops.w[id - 1], wr = (T)ops.w[id];
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        acc[id - 1][v] += F[v] * nn / wl;
+                        acc[id][v] -= F[v] * nn / wr;
+                    }
+                }
+                // cell-face terms at both ends of the line
+#pragma unroll
+                for (int lr = 0; lr < 2; ++lr) {
+                    const int i = lr ? N : 0;
+                    const int ni = line_node<P>(dir, la, lb, i);
+                    const int f = 2 * dir + lr;
+                    const int q = (dir == 0) ? la + P * lb : (dir == 1) ? la + P * lb : la + P * lb;
+                    T nn = J[(dir * 3) * P3 + ni] * J[(dir * 3) * P3 + ni];
+                    nn += J[(dir * 3 + 1) * P3 + ni] * J[(dir * 3 + 1) * P3 + ni];
+                    nn += J[(dir * 3 + 2) * P3 + ni] * J[(dir * 3 + 2) * P3 + ni];
+                    nn = dsqrt(nn);
+                    const T sg = lr ? T(1) : T(-1);  // contrib_sign and flux_sign
+                    const T wend = (T)ops.w[lr * N];
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        const T fl = sg * (T)dv.sf[v * dv.nslot + (cell * 6 + f) * P2 + q];
+                        acc[i][v] += sg * fl * nn / wend;
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < P; ++i) {
+                    const int ni = line_node<P>(dir, la, lb, i);
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) Acc[(dir * 5 + v) * P3 + ni] = acc[i][v];
+                }
+            }
+        }
+        __syncthreads();
+        if (do_lo) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) lo[v] = (Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node]) / (T)(-detJ);
+        }
+    }
+    if (!valid) return;
+
+    // ---- phase D: blend, then either store the residual or advance the RK registers
+    double R[5];
+    const double ad = VISC ? dv.alpha_d[cell] : 0.0;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        if (VISC) R[v] = (1 - ad) * (double)hd[v] + alpha * (double)lo[v] + (1 - alpha) * (double)ho[v];
+        else R[v] = alpha * (double)lo[v] + (1 - alpha) * (double)ho[v];
+    }
+    if (g.plens_2d) R[3] = 0;
+    if (sa.mode == 0) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) sa.Rout[v * dv.nd + dof] = R[v];
+        return;
+    }
+    const double dtu = s->dt_update;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        const double Rs = R[v] * dtu;
+        const int64_t k = v * dv.nd + dof;
+        double un;
+        if (sa.mode == 1) {
+            if (sa.stage == 1) un = ud[v] + sa.c2 * Rs;
+            else if (sa.stage == 2) un = ud[v] + (sa.c1 * sa.R1[k] + sa.c2 * Rs);
+            else un = ud[v] + (sa.c0 * sa.R0[k] + sa.c1 * sa.R1[k] + sa.c2 * Rs);
+            sa.Rw[k] = Rs;
+        } else {
+            if (sa.stage == 1) un = ud[v] + Rs;
+            else if (sa.stage == 2) un = 0.75 * dv.U0[k] + 0.25 * ud[v] + 0.25 * Rs;
+            else un = 1.0 / 3 * dv.U0[k] + 2.0 / 3 * ud[v] + 2.0 / 3 * Rs;
+        }
+        dv.U[k] = un;
+    }
+}
+
+}  // namespace plens_gpu

@@ -1,0 +1,91 @@
+// launch.cuh -- host-side launchers of the templated kernels, gathered into a table per
+// (P, arithmetic type) so the context can dispatch on the run-time degree and precision.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace plens_gpu {
+
+struct LaunchTable {
+    int P = 0;
+    // each returns the number of kernels it launched
+    int (*blender)(const Dev&, const Ops&, const GasP&, const BlendP&, cudaStream_t) = nullptr;
+    int (*surface)(int stage, const Dev&, const GasP&, double* out, cudaStream_t) = nullptr;
+    int (*aux)(const Dev&, const Ops&, const GasP&, cudaStream_t) = nullptr;
+    int (*volume)(bool visc, const Dev&, const Ops&, const GasP&, const StageArgs&, cudaStream_t) = nullptr;
+    int (*time_step)(const Dev&, const GasP&, double N15, int N, cudaStream_t) = nullptr;
+};
+
+LaunchTable table_fp64(int P);
+LaunchTable table_mixed(int P);
+
+template <int P, class T>
+struct Launch {
+    using CB = CellBlock<P>;
+    static int grid_cells(int64_t nc) { return (int)((nc + CB::CPB - 1) / CB::CPB); }
+
+    static int blender(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
+    {
+        k_blender<P><<<grid_cells(dv.nc), CB::THREADS, 0, st>>>(dv, ops, g, bp);
+        return 1;
+    }
+    static int surface(int stage, const Dev& dv, const GasP& g, double* out, cudaStream_t st)
+    {
+        const int64_t n = dv.ntask * P * P;
+        const int grid = (int)((n + 127) / 128);
+        if (stage == 1) k_surface<P, T, 1><<<grid, 128, 0, st>>>(dv, g, out);
+        else if (stage == 2) k_surface<P, T, 2><<<grid, 128, 0, st>>>(dv, g, out);
+        else k_surface<P, T, 3><<<grid, 128, 0, st>>>(dv, g, out);
+        return 1;
+    }
+    static int aux(const Dev& dv, const Ops& ops, const GasP& g, cudaStream_t st)
+    {
+        const size_t bytes = sizeof(T) * (size_t)CB::CPB * (5 * CB::P3 + 9 * CB::P3 + 30 * CB::P2);
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_aux<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            attr = true;
+        }
+        k_aux<P, T><<<grid_cells(dv.nc), CB::THREADS, bytes, st>>>(dv, ops, g);
+        return 1;
+    }
+    static int volume(bool visc, const Dev& dv, const Ops& ops, const GasP& g, const StageArgs& sa, cudaStream_t st)
+    {
+        const size_t bytes = VolSmem<P, T>::bytes(visc);
+        if (visc) {
+            static bool attr = false;
+            if (!attr) {
+                cudaFuncSetAttribute(k_volume<P, T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+                attr = true;
+            }
+            k_volume<P, T, true><<<grid_cells(dv.nc), CB::THREADS, bytes, st>>>(dv, ops, g, sa);
+        } else {
+            static bool attr = false;
+            if (!attr) {
+                cudaFuncSetAttribute(k_volume<P, T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+                attr = true;
+            }
+            k_volume<P, T, false><<<grid_cells(dv.nc), CB::THREADS, bytes, st>>>(dv, ops, g, sa);
+        }
+        return 1;
+    }
+    static int time_step(const Dev& dv, const GasP& g, double N15, int N, cudaStream_t st)
+    {
+        const int grid = (int)((dv.nd + 255) / 256);
+        k_time_step<P><<<grid, 256, 0, st>>>(dv, g, N15, N);
+        return 1;
+    }
+    static LaunchTable table()
+    {
+        LaunchTable t;
+        t.P = P;
+        t.blender = &blender;
+        t.surface = &surface;
+        t.aux = &aux;
+        t.volume = &volume;
+        t.time_step = &time_step;
+        return t;
+    }
+};
+
+}  // namespace plens_gpu

@@ -1,0 +1,660 @@
+// mlp.cu -- learned troubled-cell sensor: fused inference + troubled-cell compaction inside the
+// RHS, the judge/fallback logic, training-pair extraction, and the training kernels (forward,
+// backward, Adam) behind plens_gpu_mlp_train / _loss_grad / _infer. FP32 throughout.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <vector>
+
+#include "kernels.cuh"
+#include "mlp.cuh"
+
+namespace plens_gpu {
+
+namespace {
+
+// 1D Lagrange interpolation from the P GLL nodes to the 4 GLL nodes of [0,1] (exact for
+// polynomials of degree <= 3, so N = 2 data is represented without loss).
+struct Interp {
+    float I[4 * kMaxP];
+    int P;
+};
+
+void host_gll(int n, std::vector<double>& x)
+{
+    const int N = n - 1;
+    std::vector<long double> t(n);
+    for (int i = 0; i < n; ++i) t[i] = std::cos(M_PI * (long double)i / N);
+    for (int it = 0; it < 200; ++it) {
+        for (int i = 0; i < n; ++i) {
+            long double a = 1, b = t[i];
+            for (int k = 2; k <= N; ++k) { const long double c = ((2 * k - 1) * t[i] * b - (k - 1) * a) / k; a = b; b = c; }
+            if (N == 1) a = 1;
+            t[i] = t[i] - (t[i] * b - a) / (n * b);
+        }
+    }
+    x.assign(n, 0);
+    for (int i = 0; i < n; ++i) x[n - 1 - i] = (double)((t[i] + 1) / 2);
+    x[0] = 0;
+    x[n - 1] = 1;
+}
+
+Interp make_interp(int P)
+{
+    Interp r;
+    std::memset(&r, 0, sizeof(r));
+    r.P = P;
+    std::vector<double> xs, x4;
+    host_gll(P, xs);
+    host_gll(4, x4);
+    for (int a = 0; a < 4; ++a)
+        for (int i = 0; i < P; ++i) {
+            double l = 1;
+            for (int m = 0; m < P; ++m)
+                if (m != i) l *= (x4[a] - xs[m]) / (xs[i] - xs[m]);
+            r.I[a * kMaxP + i] = (float)l;
+        }
+    return r;
+}
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_d(float x)
+{
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+// Features of one cell into xs[64] (shared): rho*p at the nodes, interpolated to 4^3 GLL nodes,
+// normalised by its mean. Executed by one warp.
+template <int P>
+__device__ void cell_features(const Dev& dv, double gamma, const Interp& ip, int64_t cell, float* vs, float* ts, float* xs)
+{
+    constexpr int P2 = P * P, P3 = P2 * P;
+    const int lane = threadIdx.x & 31;
+    for (int n = lane; n < P3; n += 32) {
+        const int64_t dof = cell * P3 + n;
+        double c[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) c[v] = dv.U[v * dv.nd + dof];
+        vs[n] = (float)(get_p(c, gamma) * c[0]);
+    }
+    __syncwarp();
+    if (P == 4) {
+        for (int n = lane; n < 64; n += 32) xs[n] = vs[n];
+    } else {
+        // x: [a][j][k] (a < 4), then y, then z
+        for (int n = lane; n < 4 * P2; n += 32) {
+            const int a = n % 4, j = (n / 4) % P, k = n / (4 * P);
+            float s = 0;
+            for (int i = 0; i < P; ++i) s += ip.I[a * kMaxP + i] * vs[i + P * j + P2 * k];
+            ts[n] = s;  // layout a + 4 j + 4P k
+        }
+        __syncwarp();
+        for (int n = lane; n < 16 * P; n += 32) {
+            const int a = n % 4, b = (n / 4) % 4, k = n / 16;
+            float s = 0;
+            for (int j = 0; j < P; ++j) s += ip.I[b * kMaxP + j] * ts[a + 4 * j + 4 * P * k];
+            vs[n] = s;  // layout a + 4 b + 16 k
+        }
+        __syncwarp();
+        for (int n = lane; n < 64; n += 32) {
+            const int a = n % 4, b = (n / 4) % 4, cc = n / 16;
+            float s = 0;
+            for (int k = 0; k < P; ++k) s += ip.I[cc * kMaxP + k] * vs[a + 4 * b + 16 * k];
+            xs[n] = s;
+        }
+    }
+    __syncwarp();
+    float m = xs[lane] + xs[lane + 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m += __shfl_xor_sync(0xffffffffu, m, off);
+    m *= (1.0f / 64.0f);
+    const float inv = 1.0f / m;
+    xs[lane] = xs[lane] * inv - 1.0f;
+    xs[lane + 32] = xs[lane + 32] * inv - 1.0f;
+    __syncwarp();
+}
+
+// MLP forward of one sample held in xs (shared) by one warp; returns alpha_max*sigmoid(z).
+__device__ float mlp_forward_warp(const float* W, const float* xs, float* hs, float amax)
+{
+    const int lane = threadIdx.x & 31;
+    const float* W1 = W;
+    const float* b1 = W1 + kMlpHid * kMlpIn;
+    const float* W2 = b1 + kMlpHid;
+    const float* b2 = W2 + kMlpHid * kMlpHid;
+    const float* w3 = b2 + kMlpHid;
+    const float b3 = w3[kMlpHid];
+    float h[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int o = lane + 32 * r;
+        float s = b1[o];
+        for (int k = 0; k < kMlpIn; ++k) s += W1[o * kMlpIn + k] * xs[k];
+        h[r] = gelu(s);
+    }
+    __syncwarp();
+    hs[lane] = h[0];
+    hs[lane + 32] = h[1];
+    __syncwarp();
+    float z = 0;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int o = lane + 32 * r;
+        float s = b2[o];
+        for (int k = 0; k < kMlpHid; ++k) s += W2[o * kMlpHid + k] * hs[k];
+        z += w3[o] * gelu(s);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) z += __shfl_xor_sync(0xffffffffu, z, off);
+    z += b3;
+    __syncwarp();
+    return amax / (1.0f + expf(-z));
+}
+
+constexpr int kWarpsPerBlock = 8;
+
+// Fused inference: features, MLP, alpha_min cut, wall override, alpha_d, compacted list.
+template <int P>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_sensor_infer(Dev dv, const float* __restrict__ Wg, GasP g,
+                                                                       BlendP bp, Interp ip, double* out, int final_write, int gated)
+{
+    __shared__ float sW[kMlpParams];
+    __shared__ float sv[kWarpsPerBlock][kMaxP * kMaxP * kMaxP];
+    __shared__ float st[kWarpsPerBlock][4 * kMaxP * kMaxP];
+    __shared__ float sx[kWarpsPerBlock][64];
+    __shared__ float sh[kWarpsPerBlock][64];
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    if (gated && s->sensor_fallback) return;
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sW[i] = Wg[i];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t cell = (int64_t)blockIdx.x * kWarpsPerBlock + warp; cell < dv.nc; cell += (int64_t)gridDim.x * kWarpsPerBlock) {
+        cell_features<P>(dv, g.gamma, ip, cell, sv[warp], st[warp], sx[warp]);
+        const float at = mlp_forward_warp(sW, sx[warp], sh[warp], (float)bp.amax);
+        if (lane == 0) {
+            double a = (at < (float)bp.amin) ? 0.0 : (double)at;
+            if (dv.cell_wall[cell]) {
+                const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
+                a = (wl > a) ? wl : a;
+            }
+            out[cell] = a;
+            if (final_write) {
+                const double* x = dv.center + 3 * cell;
+                dv.alpha_d[cell] = (eval_expr(dv, bp.expr_vis, x[0], x[1], x[2], s->time) > 0) ? ((1.0 < a / bp.amax) ? 1.0 : a / bp.amax) : 0.0;
+                if (a > 0) {
+                    const int k = atomicAdd(dv.lo_count, 1);
+                    dv.lo_list[k] = (int32_t)cell;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// judge: per-cell |alpha_mlp - alpha_plain|, max over cells
+__global__ void k_judge_compare(Dev dv, const double* alpha_mlp, unsigned long long* maxerr)
+{
+    if (!dv.sc->active) return;
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double e = 0;
+    if (c < dv.nc) e = fabs(alpha_mlp[c] - dv.alpha[c]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double o = __shfl_xor_sync(0xffffffffu, e, off);
+        e = (o > e) ? o : e;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(maxerr, ord_double(e));
+}
+
+__global__ void k_judge_decide(Dev dv, unsigned long long* maxerr, double tol)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const double e = unord_double(*maxerr);
+    s->judged += 1;
+    if (e > s->max_alpha_err) s->max_alpha_err = e;
+    s->sensor_fallback = (e > tol) ? 1 : 0;
+    if (s->sensor_fallback) s->fallbacks += 1;
+    *maxerr = ord_double(0.0);
+}
+
+// keep the MLP alpha unless the judge fell back
+__global__ void k_judge_select(Dev dv, const double* alpha_mlp, BlendP bp)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= dv.nc) return;
+    double a = dv.alpha[c];
+    if (!s->sensor_fallback) {
+        a = alpha_mlp[c];
+        dv.alpha[c] = a;
+        const double* x = dv.center + 3 * c;
+        dv.alpha_d[c] = (eval_expr(dv, bp.expr_vis, x[0], x[1], x[2], s->time) > 0) ? ((1.0 < a / bp.amax) ? 1.0 : a / bp.amax) : 0.0;
+    }
+    if (a > 0) {
+        const int k = atomicAdd(dv.lo_count, 1);
+        dv.lo_list[k] = (int32_t)c;
+    }
+}
+
+__global__ void k_lo_stat(Dev dv)
+{
+    if (!dv.sc->active) return;
+    dv.sc->lo_cells = *dv.lo_count;
+}
+
+template <int P>
+__global__ void k_features(Dev dv, GasP g, Interp ip, float* x)
+{
+    __shared__ float sv[kWarpsPerBlock][kMaxP * kMaxP * kMaxP];
+    __shared__ float st[kWarpsPerBlock][4 * kMaxP * kMaxP];
+    __shared__ float sx[kWarpsPerBlock][64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t cell = (int64_t)blockIdx.x * kWarpsPerBlock + warp; cell < dv.nc; cell += (int64_t)gridDim.x * kWarpsPerBlock) {
+        cell_features<P>(dv, g.gamma, ip, cell, sv[warp], st[warp], sx[warp]);
+        x[cell * 64 + lane] = sx[warp][lane];
+        x[cell * 64 + lane + 32] = sx[warp][lane + 32];
+        __syncwarp();
+    }
+}
+
+struct MlpScratch {
+    unsigned long long* maxerr = nullptr;
+    double* alpha_mlp = nullptr;
+};
+
+template <int P>
+int launch_infer(const Dev& dv, const float* W, const GasP& g, const BlendP& bp, double* out, int final_write, int gated, cudaStream_t st)
+{
+    const Interp ip = make_interp(P);
+    const int64_t blocks = std::min<int64_t>((dv.nc + kWarpsPerBlock - 1) / kWarpsPerBlock, 152 * 8);
+    k_sensor_infer<P><<<(unsigned)blocks, 32 * kWarpsPerBlock, 0, st>>>(dv, W, g, bp, ip, out, final_write, gated);
+    return 1;
+}
+
+template <int P>
+int launch_plain(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
+{
+    using CB = CellBlock<P>;
+    k_blender<P><<<(unsigned)((dv.nc + CB::CPB - 1) / CB::CPB), CB::THREADS, 0, st>>>(dv, ops, g, bp);
+    k_alpha_smooth<<<(unsigned)((dv.nc + 127) / 128), 128, 0, st>>>(dv, bp);
+    return 2;
+}
+
+template <int P>
+int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
+{
+    int n = 0;
+    cudaMemsetAsync(dv.lo_count, 0, sizeof(int32_t), st);
+    if (m.judge_this_step) {
+        // MLP into the scratch buffer, plain blender into alpha (no compaction), compare, select
+        n += launch_infer<P>(dv, m.params, g, bp, m.alpha_plain, 0, 0, st);
+        Dev d2 = dv;
+        d2.lo_list = nullptr;
+        BlendP b0 = bp;
+        b0.gate = 0;
+        n += launch_plain<P>(d2, ops, g, b0, st);
+        const unsigned grid = (unsigned)((dv.nc + 127) / 128);
+        k_judge_compare<<<grid, 128, 0, st>>>(dv, m.alpha_plain, m.maxerr);
+        k_judge_decide<<<1, 1, 0, st>>>(dv, m.maxerr, m.tol);
+        k_judge_select<<<grid, 128, 0, st>>>(dv, m.alpha_plain, bp);
+        n += 3;
+        m.judge_this_step = false;  // the remaining stages of this step follow the decision
+    } else {
+        n += launch_infer<P>(dv, m.params, g, bp, dv.alpha, 1, 1, st);
+        BlendP b1 = bp;
+        b1.gate = 1;
+        n += launch_plain<P>(dv, ops, g, b1, st);
+    }
+    k_lo_stat<<<1, 1, 0, st>>>(dv);
+    return n + 1;
+}
+
+}  // namespace
+
+int mlp_create(MlpDevice& m, int64_t nc, std::vector<void*>& allocs)
+{
+    m.nc = nc;
+    if (cudaMalloc(&m.params, sizeof(float) * kMlpParams) != cudaSuccess) return 1;
+    allocs.push_back(m.params);
+    if (cudaMalloc(&m.alpha_plain, sizeof(double) * (nc + 1)) != cudaSuccess) return 1;
+    allocs.push_back(m.alpha_plain);
+    if (cudaMalloc(&m.maxerr, sizeof(unsigned long long)) != cudaSuccess) return 1;
+    allocs.push_back(m.maxerr);
+    const unsigned long long z = ord_double_host(0.0);
+    if (cudaMemcpy(m.maxerr, &z, sizeof(z), cudaMemcpyHostToDevice) != cudaSuccess) return 1;
+    return 0;
+}
+
+int mlp_set_weights(MlpDevice& m, const float* host_params, cudaStream_t st)
+{
+    if (cudaMemcpyAsync(m.params, host_params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, st) != cudaSuccess) return 1;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return 1;
+    m.weights_set = true;
+    return 0;
+}
+
+int mlp_sensor_launch(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, int P, cudaStream_t st)
+{
+    switch (P) {
+    case 2: return sensor_stage<2>(m, dv, ops, g, bp, st);
+    case 3: return sensor_stage<3>(m, dv, ops, g, bp, st);
+    case 4: return sensor_stage<4>(m, dv, ops, g, bp, st);
+    case 5: return sensor_stage<5>(m, dv, ops, g, bp, st);
+    default: return sensor_stage<6>(m, dv, ops, g, bp, st);
+    }
+}
+
+int mlp_step_begin(MlpDevice& m, const Dev& dv, int judge_every, cudaStream_t st)
+{
+    (void)dv;
+    (void)st;
+    m.judge_this_step = (judge_every <= 1) || (m.step_counter % judge_every == 0);
+    ++m.step_counter;
+    return 0;
+}
+
+int mlp_step_end(MlpDevice& m, const Dev& dv, cudaStream_t st)
+{
+    (void)m;
+    (void)dv;
+    (void)st;
+    return 0;
+}
+
+int mlp_pairs(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, int P, float* x, float* y,
+              cudaStream_t st, int64_t& launches)
+{
+    float* dx = nullptr;
+    if (cudaMalloc(&dx, sizeof(float) * 64 * dv.nc) != cudaSuccess) return PLENS_GPU_E_CUDA;
+    k_step_begin<<<1, 1, 0, st>>>(dv, 1e300);
+    Dev d2 = dv;
+    d2.lo_list = nullptr;
+    BlendP b0 = bp;
+    b0.gate = 0;
+    const int64_t blocks = std::min<int64_t>((dv.nc + kWarpsPerBlock - 1) / kWarpsPerBlock, 152 * 8);
+    switch (P) {
+    case 2: launch_plain<2>(d2, ops, g, b0, st); k_features<2><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(2), dx); break;
+    case 3: launch_plain<3>(d2, ops, g, b0, st); k_features<3><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(3), dx); break;
+    case 4: launch_plain<4>(d2, ops, g, b0, st); k_features<4><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(4), dx); break;
+    case 5: launch_plain<5>(d2, ops, g, b0, st); k_features<5><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(5), dx); break;
+    default: launch_plain<6>(d2, ops, g, b0, st); k_features<6><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(6), dx); break;
+    }
+    launches += 4;
+    std::vector<double> a(dv.nc);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaMemcpy(x, dx, sizeof(float) * 64 * dv.nc, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(a.data(), dv.alpha, sizeof(double) * dv.nc, cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    if (e != cudaSuccess) return PLENS_GPU_E_CUDA;
+    for (int64_t i = 0; i < dv.nc; ++i) y[i] = (float)a[i];
+    return 0;
+}
+
+// ===================================================================== training kernels
+
+namespace {
+
+// a = act(x W^T + b) for a batch: one thread per (sample, output)
+__global__ void k_dense_fwd(const float* __restrict__ X, int in, const float* __restrict__ W, const float* __restrict__ b,
+                            int out, int64_t B, float* __restrict__ Apre, float* __restrict__ H)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= B * out) return;
+    const int64_t s = i / out;
+    const int o = (int)(i - s * out);
+    float acc = b[o];
+    for (int k = 0; k < in; ++k) acc += W[o * in + k] * X[s * in + k];
+    Apre[i] = acc;
+    H[i] = gelu(acc);
+}
+
+// output layer, loss and its gradient with respect to z
+__global__ void k_head(const float* __restrict__ H2, const float* __restrict__ w3, float b3, const float* __restrict__ y,
+                       int64_t B, float amax, float* __restrict__ alpha, float* __restrict__ dz, float* __restrict__ loss_terms)
+{
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= B) return;
+    float z = b3;
+    for (int k = 0; k < kMlpHid; ++k) z += w3[k] * H2[s * kMlpHid + k];
+    const float sg = 1.0f / (1.0f + expf(-z));
+    const float a = amax * sg;
+    alpha[s] = a;
+    if (y) {
+        const float d = a - y[s];
+        loss_terms[s] = d * d;
+        dz[s] = (2.0f / (float)B) * d * amax * sg * (1.0f - sg);
+    }
+}
+
+// dH_in[s][k] = sum_o dA[s][o] W[o][k], then times act'(Apre_in)
+__global__ void k_dense_bwd_input(const float* __restrict__ dA, const float* __restrict__ W, int in, int out, int64_t B,
+                                  const float* __restrict__ Apre_in, float* __restrict__ dA_in)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= B * in) return;
+    const int64_t s = i / in;
+    const int k = (int)(i - s * in);
+    float acc = 0;
+    for (int o = 0; o < out; ++o) acc += dA[s * out + o] * W[o * in + k];
+    dA_in[i] = acc * gelu_d(Apre_in[i]);
+}
+
+// dW[o][k] = sum_s dA[s][o] X[s][k], db[o] = sum_s dA[s][o] (fixed summation order)
+__global__ void k_dense_bwd_weight(const float* __restrict__ dA, const float* __restrict__ X, int in, int out, int64_t B,
+                                   float* __restrict__ dW, float* __restrict__ db)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= out * (in + 1)) return;
+    const int o = i / (in + 1), k = i - o * (in + 1);
+    float acc = 0;
+    if (k < in) {
+        for (int64_t s = 0; s < B; ++s) acc += dA[s * out + o] * X[s * in + k];
+        dW[o * in + k] = acc;
+    } else {
+        for (int64_t s = 0; s < B; ++s) acc += dA[s * out + o];
+        db[o] = acc;
+    }
+}
+
+// head gradients: dw3[k] = sum_s dz[s] H2[s][k], db3 = sum dz, dA2[s][k] = dz[s] w3[k] act'(A2)
+__global__ void k_head_bwd(const float* __restrict__ dz, const float* __restrict__ H2, const float* __restrict__ A2,
+                           const float* __restrict__ w3, int64_t B, float* __restrict__ dw3, float* __restrict__ db3,
+                           float* __restrict__ dA2)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < B * kMlpHid) {
+        const int64_t s = i / kMlpHid;
+        const int k = (int)(i - s * kMlpHid);
+        dA2[i] = dz[s] * w3[k] * gelu_d(A2[i]);
+    }
+    if (i < kMlpHid + 1) {
+        float acc = 0;
+        if (i < kMlpHid) {
+            for (int64_t s = 0; s < B; ++s) acc += dz[s] * H2[s * kMlpHid + i];
+            dw3[i] = acc;
+        } else {
+            for (int64_t s = 0; s < B; ++s) acc += dz[s];
+            db3[0] = acc;
+        }
+    }
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       int n, float lr, float b1, float b2, float eps, float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1 - b1) * gi;
+    const float vi = b2 * v[i] + (1 - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+__global__ void k_gather(const float* __restrict__ X, const float* __restrict__ Y, const int64_t* __restrict__ idx,
+                         int64_t B, float* __restrict__ Xb, float* __restrict__ Yb)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= B * kMlpIn) return;
+    const int64_t s = i / kMlpIn;
+    const int k = (int)(i - s * kMlpIn);
+    const int64_t src = idx[s];
+    Xb[i] = X[src * kMlpIn + k];
+    if (k == 0) Yb[s] = Y[src];
+}
+
+struct Trainer {
+    int64_t cap = 0;
+    float *x = nullptr, *y = nullptr, *a1 = nullptr, *h1 = nullptr, *a2 = nullptr, *h2 = nullptr;
+    float *alpha = nullptr, *dz = nullptr, *lt = nullptr, *da2 = nullptr, *da1 = nullptr;
+    float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+    cudaStream_t st = nullptr;
+    std::vector<void*> allocs;
+    bool ok = true;
+    template <class T>
+    void alloc(T** ptr, size_t n)
+    {
+        if (cudaMalloc(ptr, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) ok = false;
+        else allocs.push_back(*ptr);
+    }
+    explicit Trainer(int64_t B) : cap(B)
+    {
+        cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        alloc(&x, B * kMlpIn); alloc(&y, B); alloc(&a1, B * kMlpHid); alloc(&h1, B * kMlpHid);
+        alloc(&a2, B * kMlpHid); alloc(&h2, B * kMlpHid); alloc(&alpha, B); alloc(&dz, B); alloc(&lt, B);
+        alloc(&da2, B * kMlpHid); alloc(&da1, B * kMlpHid);
+        alloc(&p, kMlpParams); alloc(&g, kMlpParams); alloc(&m, kMlpParams); alloc(&v, kMlpParams);
+    }
+    ~Trainer()
+    {
+        if (st) cudaStreamSynchronize(st);
+        for (void* q : allocs) cudaFree(q);
+        if (st) cudaStreamDestroy(st);
+    }
+    // forward (+ backward when y given) of B samples already in x / y
+    void run(int64_t B, float amax, bool backward)
+    {
+        const float* W1 = p;
+        const float* b1 = W1 + kMlpHid * kMlpIn;
+        const float* W2 = b1 + kMlpHid;
+        const float* b2 = W2 + kMlpHid * kMlpHid;
+        const float* w3 = b2 + kMlpHid;
+        const unsigned gh = (unsigned)((B * kMlpHid + 255) / 256), gb = (unsigned)((B + 255) / 256);
+        k_dense_fwd<<<gh, 256, 0, st>>>(x, kMlpIn, W1, b1, kMlpHid, B, a1, h1);
+        k_dense_fwd<<<gh, 256, 0, st>>>(h1, kMlpHid, W2, b2, kMlpHid, B, a2, h2);
+        float b3h;
+        cudaMemcpyAsync(&b3h, w3 + kMlpHid, sizeof(float), cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        k_head<<<gb, 256, 0, st>>>(h2, w3, b3h, backward ? y : nullptr, B, amax, alpha, dz, lt);
+        if (!backward) return;
+        float* gW1 = g;
+        float* gb1 = gW1 + kMlpHid * kMlpIn;
+        float* gW2 = gb1 + kMlpHid;
+        float* gb2 = gW2 + kMlpHid * kMlpHid;
+        float* gw3 = gb2 + kMlpHid;
+        k_head_bwd<<<gh, 256, 0, st>>>(dz, h2, a2, w3, B, gw3, gw3 + kMlpHid, da2);
+        k_dense_bwd_weight<<<(kMlpHid * (kMlpHid + 1) + 127) / 128, 128, 0, st>>>(da2, h1, kMlpHid, kMlpHid, B, gW2, gb2);
+        k_dense_bwd_input<<<gh, 256, 0, st>>>(da2, W2, kMlpHid, kMlpHid, B, a1, da1);
+        k_dense_bwd_weight<<<(kMlpHid * (kMlpIn + 1) + 127) / 128, 128, 0, st>>>(da1, x, kMlpIn, kMlpHid, B, gW1, gb1);
+    }
+    double loss(int64_t B)
+    {
+        std::vector<float> h(B);
+        cudaMemcpyAsync(h.data(), lt, sizeof(float) * B, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        double s = 0;
+        for (float t : h) s += t;
+        return s / (double)B;
+    }
+};
+
+}  // namespace
+
+}  // namespace plens_gpu
+
+using namespace plens_gpu;
+
+extern "C" {
+
+int plens_gpu_mlp_loss_grad(const float* x, const float* y, int64_t n, const float* params, float alpha_max,
+                            float* loss, float* grad)
+{
+    if (!x || !y || !params || n <= 0) return PLENS_GPU_E_INVALID;
+    Trainer t(n);
+    if (!t.ok) return PLENS_GPU_E_CUDA;
+    cudaMemcpy(t.x, x, sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice);
+    cudaMemcpy(t.y, y, sizeof(float) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(t.p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice);
+    t.run(n, alpha_max, true);
+    if (loss) *loss = (float)t.loss(n);
+    if (grad) cudaMemcpy(grad, t.g, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost);
+    return cudaGetLastError() == cudaSuccess ? 0 : PLENS_GPU_E_CUDA;
+}
+
+int plens_gpu_mlp_infer(const float* x, int64_t n, const float* params, float alpha_max, float* alpha)
+{
+    if (!x || !params || !alpha || n <= 0) return PLENS_GPU_E_INVALID;
+    Trainer t(n);
+    if (!t.ok) return PLENS_GPU_E_CUDA;
+    cudaMemcpy(t.x, x, sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice);
+    cudaMemcpy(t.p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice);
+    t.run(n, alpha_max, false);
+    cudaStreamSynchronize(t.st);
+    cudaMemcpy(alpha, t.alpha, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    return cudaGetLastError() == cudaSuccess ? 0 : PLENS_GPU_E_CUDA;
+}
+
+int plens_gpu_mlp_train(const float* x, const float* y, int64_t n, float* params, int32_t epochs, int32_t batch,
+                        float lr, float alpha_max, uint64_t seed, float* loss_out)
+{
+    if (!x || !y || !params || n <= 0 || epochs < 0 || batch <= 0) return PLENS_GPU_E_INVALID;
+    const int64_t B = std::min<int64_t>(batch, n);
+    Trainer t(B);
+    if (!t.ok) return PLENS_GPU_E_CUDA;
+    float *dX = nullptr, *dY = nullptr;
+    int64_t* dIdx = nullptr;
+    if (cudaMalloc(&dX, sizeof(float) * n * kMlpIn) != cudaSuccess) return PLENS_GPU_E_CUDA;
+    cudaMalloc(&dY, sizeof(float) * n);
+    cudaMalloc(&dIdx, sizeof(int64_t) * n);
+    cudaMemcpy(dX, x, sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice);
+    cudaMemcpy(dY, y, sizeof(float) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(t.p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice);
+    cudaMemset(t.m, 0, sizeof(float) * kMlpParams);
+    cudaMemset(t.v, 0, sizeof(float) * kMlpParams);
+    std::vector<int64_t> perm(n);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::mt19937_64 rng(seed);
+    int64_t step = 0;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (int ep = 0; ep < epochs; ++ep) {
+        std::shuffle(perm.begin(), perm.end(), rng);
+        cudaMemcpyAsync(dIdx, perm.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, t.st);
+        double ls = 0;
+        int64_t seen = 0;
+        for (int64_t off = 0; off < n; off += B) {
+            const int64_t bsz = std::min<int64_t>(B, n - off);
+            k_gather<<<(unsigned)((bsz * kMlpIn + 255) / 256), 256, 0, t.st>>>(dX, dY, dIdx + off, bsz, t.x, t.y);
+            t.run(bsz, alpha_max, true);
+            ++step;
+            const float c1 = 1.0f - std::pow(b1, (float)step), c2 = 1.0f - std::pow(b2, (float)step);
+            k_adam<<<(kMlpParams + 255) / 256, 256, 0, t.st>>>(t.p, t.g, t.m, t.v, kMlpParams, lr, b1, b2, eps, c1, c2);
+            ls += t.loss(bsz) * (double)bsz;
+            seen += bsz;
+        }
+        if (loss_out) loss_out[ep] = (float)(ls / (double)seen);
+    }
+    cudaStreamSynchronize(t.st);
+    cudaMemcpy(params, t.p, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost);
+    cudaFree(dX);
+    cudaFree(dY);
+    cudaFree(dIdx);
+    return cudaGetLastError() == cudaSuccess ? 0 : PLENS_GPU_E_CUDA;
+}
+
+}  // extern "C"

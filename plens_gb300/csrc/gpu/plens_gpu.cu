@@ -1,0 +1,646 @@
+// plens_gpu.cu -- the C ABI of include/plens_gpu.h: context lifecycle, device buffers and the
+// stage orchestration of PLENS::update / update_rk4 / update_rk3 / calc_rhs
+// (dgsem/plens.cc:3688-3779, 4334-4518) on one CUDA stream.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "launch.cuh"
+#include "mlp.cuh"
+#include "plens_gpu.h"
+
+namespace plens_gpu {
+LaunchTable table_fp64_2(); LaunchTable table_fp64_3(); LaunchTable table_fp64_4();
+LaunchTable table_fp64_5(); LaunchTable table_fp64_6();
+LaunchTable table_mixed_2(); LaunchTable table_mixed_3(); LaunchTable table_mixed_4();
+LaunchTable table_mixed_5(); LaunchTable table_mixed_6();
+
+static LaunchTable pick_table(int P, bool mixed)
+{
+    switch (P) {
+    case 2: return mixed ? table_mixed_2() : table_fp64_2();
+    case 3: return mixed ? table_mixed_3() : table_fp64_3();
+    case 4: return mixed ? table_mixed_4() : table_fp64_4();
+    case 5: return mixed ? table_mixed_5() : table_fp64_5();
+    case 6: return mixed ? table_mixed_6() : table_fp64_6();
+    default: return LaunchTable{};
+    }
+}
+
+// ------------------------------------------------------------------- 1D operators (host)
+static void gll(int n, std::vector<double>& x01, std::vector<double>& w01)
+{
+    const int N = n - 1;
+    std::vector<long double> x(n);
+    for (int i = 0; i < n; ++i) x[i] = std::cos(M_PI * (long double)i / N);
+    for (int it = 0; it < 200; ++it) {
+        long double diff = 0;
+        for (int i = 0; i < n; ++i) {
+            long double a = 1, b = x[i];
+            for (int k = 2; k <= N; ++k) { const long double c = ((2 * k - 1) * x[i] * b - (k - 1) * a) / k; a = b; b = c; }
+            if (N == 1) a = 1;
+            const long double xn = x[i] - (x[i] * b - a) / (n * b);
+            diff = std::max(diff, std::fabs(xn - x[i]));
+            x[i] = xn;
+        }
+        if (diff < 1e-19L) break;
+    }
+    x01.assign(n, 0);
+    w01.assign(n, 0);
+    for (int i = 0; i < n; ++i) {
+        long double a = 1, b = x[i];
+        for (int k = 2; k <= N; ++k) { const long double c = ((2 * k - 1) * x[i] * b - (k - 1) * a) / k; a = b; b = c; }
+        x01[n - 1 - i] = (double)((x[i] + 1) / 2);
+        w01[n - 1 - i] = (double)(1.0L / (N * n * b * b));
+    }
+    x01[0] = 0;
+    x01[n - 1] = 1;
+}
+
+static double legendre01(int k, double x)  // orthonormal Legendre polynomial on [0,1]
+{
+    if (k == 0) return 1.0;
+    const double t = 2 * x - 1;
+    double a = 1, b = t;
+    for (int j = 2; j <= k; ++j) { const double c = ((2 * j - 1) * t * b - (j - 1) * a) / j; a = b; b = c; }
+    return std::sqrt(2.0 * k + 1) * b;
+}
+
+static Ops make_ops(int P)
+{
+    Ops o;
+    std::memset(&o, 0, sizeof(o));
+    std::vector<double> xi, w;
+    gll(P, xi, w);
+    for (int i = 0; i < P; ++i) o.w[i] = w[i];
+    for (int i = 0; i < P; ++i)
+        for (int j = 0; j < P; ++j) {
+            double s = 0;
+            for (int k = 0; k < P; ++k) {
+                if (k == j) continue;
+                double t = 1.0 / (xi[j] - xi[k]);
+                for (int m = 0; m < P; ++m)
+                    if (m != j && m != k) t *= (xi[i] - xi[m]) / (xi[j] - xi[m]);
+                s += t;
+            }
+            o.D[i * P + j] = s;
+            o.Q[i * P + j] = w[i] * s;
+        }
+    // Gauss rule with P points on [0,1]
+    std::vector<double> gx(P), gw(P);
+    for (int i = 0; i < P; ++i) {
+        long double x = std::cos(M_PI * (i + 0.75L) / (P + 0.5L)), dp = 0;
+        for (int it = 0; it < 100; ++it) {
+            long double a = 1, b = x;
+            for (int k = 2; k <= P; ++k) { const long double c = ((2 * k - 1) * x * b - (k - 1) * a) / k; a = b; b = c; }
+            dp = P * (x * b - a) / (x * x - 1);
+            const long double dx = b / dp;
+            x -= dx;
+            if (std::fabs(dx) < 1e-20L) break;
+        }
+        gx[P - 1 - i] = (double)((x + 1) / 2);
+        gw[P - 1 - i] = (double)(1.0L / ((1 - x * x) * dp * dp));
+    }
+    for (int a = 0; a < P; ++a)
+        for (int i = 0; i < P; ++i) {
+            double s = 0;
+            for (int g = 0; g < P; ++g) {
+                double l = 1;
+                for (int m = 0; m < P; ++m)
+                    if (m != i) l *= (gx[g] - xi[m]) / (xi[i] - xi[m]);
+                s += gw[g] * legendre01(a, gx[g]) * l;
+            }
+            o.C1[a * P + i] = s;
+        }
+    o.tv[0] = 0.0;
+    if (P > 1) o.tv[1] = std::fabs(legendre01(1, 1) - legendre01(1, 0));
+    for (int ip = 2; ip < P; ++ip) {
+        std::vector<double> qx, qw;
+        gll(ip + 1, qx, qw);
+        double tv = 0;
+        for (int k = 0; k < ip; ++k) tv += std::fabs(legendre01(ip, qx[k + 1]) - legendre01(ip, qx[k]));
+        o.tv[ip] = tv;
+    }
+    return o;
+}
+
+}  // namespace plens_gpu
+
+using namespace plens_gpu;
+
+struct plens_ctx {
+    int P = 0, N = 0;
+    int64_t nc = 0, nd = 0, ntask = 0, nslot = 0;
+    bool viscous = false, mixed = false, learned = false;
+    plens_params prm{};
+    Dev dv{};
+    Ops ops{};
+    GasP gas{};
+    BlendP bp{};
+    LaunchTable tab{};
+    double N15 = 1;
+    cudaStream_t stream = nullptr;
+    int64_t launches = 0;
+    std::string err = "no error";
+    std::vector<void*> allocs;
+    double* R[3] = {nullptr, nullptr, nullptr};
+    double* Rout = nullptr;
+    Scalars* sc = nullptr;
+    MlpDevice mlp{};
+    int64_t bad_dof_host = -1;
+    // volume-kernel timing
+    bool timing = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+    size_t ev_used = 0;
+    double vol_ms = 0;
+    int64_t vol_n = 0;
+};
+
+namespace {
+
+int fail(plens_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(plens_ctx* c, cudaError_t e, const char* what)
+{
+    return fail(c, PLENS_GPU_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                         \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+    } while (0)
+
+template <class T>
+int dalloc(plens_ctx* c, T** p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+    c->allocs.push_back(*p);
+    return 0;
+}
+
+template <class T>
+int dupload(plens_ctx* c, const T** dst, const T* src, size_t n)
+{
+    T* p = nullptr;
+    if (int r = dalloc(c, &p, n)) return r;
+    if (src && n) {
+        cudaError_t e = cudaMemcpy(p, src, n * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemcpy H2D");
+    }
+    *dst = p;
+    return 0;
+}
+
+int check_launch(plens_ctx* c, const char* what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, what);
+    return 0;
+}
+
+// One RHS of the current stage: calc_rhs without the final store (dgsem/plens.cc:3688-3779).
+// The volume kernel of `sa` blends and either stores or advances the registers.
+int launch_rhs(plens_ctx* c, const StageArgs& sa)
+{
+    cudaStream_t st = c->stream;
+    if (c->viscous) {
+        c->launches += c->tab.surface(1, c->dv, c->gas, c->dv.sf, st);
+        c->launches += c->tab.aux(c->dv, c->ops, c->gas, st);
+    }
+    if (c->learned) {
+        c->launches += mlp_sensor_launch(c->mlp, c->dv, c->ops, c->gas, c->bp, c->P, st);
+    } else {
+        c->launches += c->tab.blender(c->dv, c->ops, c->gas, c->bp, st);
+        k_alpha_smooth<<<(unsigned)((c->nc + 127) / 128), 128, 0, st>>>(c->dv, c->bp);
+        ++c->launches;
+    }
+    if (c->viscous) c->launches += c->tab.surface(3, c->dv, c->gas, c->dv.sf3, st);
+    c->launches += c->tab.surface(2, c->dv, c->gas, c->dv.sf, st);
+    if (c->timing) {
+        if (c->ev_used == c->ev_pool.size()) {
+            cudaEvent_t a, b;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            c->ev_pool.emplace_back(a, b);
+        }
+        cudaEventRecord(c->ev_pool[c->ev_used].first, st);
+        c->launches += c->tab.volume(c->viscous, c->dv, c->ops, c->gas, sa, st);
+        cudaEventRecord(c->ev_pool[c->ev_used].second, st);
+        ++c->ev_used;
+    } else {
+        c->launches += c->tab.volume(c->viscous, c->dv, c->ops, c->gas, sa, st);
+    }
+    return check_launch(c, "rhs kernels");
+}
+
+int launch_time_step(plens_ctx* c)
+{
+    k_courant<<<1, 1, 0, c->stream>>>(c->dv, c->prm.expr_courant);
+    c->launches += 1;
+    c->launches += c->tab.time_step(c->dv, c->gas, c->N15, c->N, c->stream);
+    k_dt_finalize<<<1, 1, 0, c->stream>>>(c->dv);
+    c->launches += 1;
+    return check_launch(c, "time step kernels");
+}
+
+// RK4(3)5[3R+]N coefficients of Kennedy, Carpenter & Lewis (2000) as used by the reference
+// (dgsem/rk4_stage5_register3.cc:12-36)
+const double kB[5] = {314199625218.0 / 7198350928319, 6410344372641.0 / 17000082738695,
+                      292278564125.0 / 5593752632744, 5010207514426.0 / 21876007855139,
+                      5597675544274.0 / 18784428342765};
+const double kAo[5] = {4745337637855.0 / 22386579876409, 6808157035527.0 / 13197844641179,
+                       4367509502613.0 / 10454198590847, 1236962429870.0 / 3429868089329,
+                       5597675544274.0 / 18784428342765};
+const double kAi[4] = {546509042554.0 / 9152262712923, 625707605167.0 / 5316659119056,
+                       582400652113.0 / 7078426004906, 5010207514426.0 / 21876007855139};
+
+int launch_step(plens_ctx* c, double end_time)
+{
+    cudaStream_t st = c->stream;
+    k_step_begin<<<1, 1, 0, st>>>(c->dv, end_time);
+    c->launches += 1;
+    if (c->learned) {
+        c->launches += mlp_step_begin(c->mlp, c->dv, c->prm.judge_every, st);
+    }
+    if (int r = launch_time_step(c)) return r;
+    if (c->prm.rk_order == 4) {
+        // registers rotate: stage s writes dt*R into R[w]; R1 = previous, R0 = previous-previous
+        int w = 0, r1 = -1, r0 = -1;
+        for (int s = 1; s <= 5; ++s) {
+            StageArgs sa{};
+            sa.mode = 1;
+            sa.stage = s;
+            sa.Rw = c->R[w];
+            sa.R1 = (r1 >= 0) ? c->R[r1] : nullptr;
+            sa.R0 = (r0 >= 0) ? c->R[r0] : nullptr;
+            if (s == 1) {
+                sa.c2 = kAo[0];
+            } else if (s == 2) {
+                sa.c1 = kAi[0] - kAo[0];
+                sa.c2 = kAo[1];
+            } else {
+                sa.c0 = kB[s - 3] - kAi[s - 3];
+                sa.c1 = kAi[s - 2] - kAo[s - 2];
+                sa.c2 = kAo[s - 1];
+            }
+            if (int r = launch_rhs(c, sa)) return r;
+            r0 = r1;
+            r1 = w;
+            w = (w + 1) % 3;
+        }
+    } else {
+        cudaError_t e = cudaMemcpyAsync(c->dv.U0, c->dv.U, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(c, e, "U0 copy");
+        for (int s = 1; s <= 3; ++s) {
+            StageArgs sa{};
+            sa.mode = 2;
+            sa.stage = s;
+            if (int r = launch_rhs(c, sa)) return r;
+        }
+    }
+    if (c->learned) c->launches += mlp_step_end(c->mlp, c->dv, st);
+    k_clock<<<1, 1, 0, st>>>(c->dv);
+    c->launches += 1;
+    return check_launch(c, "step kernels");
+}
+
+int sync_and_check(plens_ctx* c)
+{
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamSynchronize");
+    for (size_t i = 0; i < c->ev_used; ++i) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev_pool[i].first, c->ev_pool[i].second);
+        c->vol_ms += ms;
+        ++c->vol_n;
+    }
+    c->ev_used = 0;
+    Scalars h;
+    e = cudaMemcpy(&h, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "read scalars");
+    if (h.err == PLENS_GPU_E_POSITIVITY) {
+        c->bad_dof_host = h.bad_dof;
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "Positivity assertion failed at dof %lld", h.bad_dof);
+        return fail(c, PLENS_GPU_E_POSITIVITY, buf);
+    }
+    if (h.err) return fail(c, h.err, "device error " + std::to_string(h.err));
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens_ctx** out)
+{
+    if (!out) return PLENS_GPU_E_INVALID;
+    *out = nullptr;
+    if (!mesh || !prm) return PLENS_GPU_E_INVALID;
+    plens_ctx* c = new plens_ctx();
+    *out = c;
+    if (mesh->degree < 1 || mesh->degree > kMaxP - 1 || mesh->degree != prm->degree)
+        return fail(c, PLENS_GPU_E_INVALID, "degree must lie in [1,5] and match the parameters");
+    if (mesh->n_cells <= 0 || mesh->n_cells > INT32_MAX) return fail(c, PLENS_GPU_E_INVALID, "bad n_cells");
+    if (prm->rk_order != 3 && prm->rk_order != 4) return fail(c, PLENS_GPU_E_INVALID, "RK order must be 3 or 4");
+    if (prm->blender_function != 0 && prm->blender_function != 1)
+        return fail(c, PLENS_GPU_E_INVALID, "blender function must be Hennemann or linear");
+    if (prm->inv_surf_flux < 0 || prm->inv_surf_flux > PLENS_ISF_CHANDRASHEKHAR || prm->inv_surf_flux == PLENS_ISF_MODIFIED_SW)
+        return fail(c, PLENS_GPU_E_INVALID, "inviscid surface flux scheme not supported on the GPU path");
+    if (prm->inv_vol_flux < 0 || prm->inv_vol_flux > PLENS_IVF_ISMAIL_ROE)
+        return fail(c, PLENS_GPU_E_INVALID, "bad inviscid volume flux scheme");
+    for (int b = 0; b < prm->n_bc; ++b)
+        if (prm->bcs[b].type < PLENS_BC_NONE || prm->bcs[b].type > PLENS_BC_ZPG_INFLOW)
+            return fail(c, PLENS_GPU_E_INVALID, "bad boundary condition type");
+    c->P = mesh->degree + 1;
+    c->N = mesh->degree;
+    c->nc = mesh->n_cells;
+    const int P2 = c->P * c->P, P3 = P2 * c->P;
+    c->nd = c->nc * P3;
+    c->ntask = mesh->n_face_tasks;
+    c->nslot = c->nc * 6 * P2;
+    c->prm = *prm;
+    c->viscous = !(prm->mu0 < 1e-16);
+    c->mixed = prm->precision == PLENS_PRECISION_MIXED;
+    c->learned = prm->sensor == PLENS_SENSOR_LEARNED;
+    c->tab = pick_table(c->P, c->mixed);
+    if (!c->tab.volume) return fail(c, PLENS_GPU_E_INVALID, "no kernels for this degree");
+    c->ops = make_ops(c->P);
+    c->N15 = std::pow(c->N, 1.5);
+    c->gas = GasP{prm->gamma, prm->R, prm->Pr, prm->mu0, prm->T0, prm->S,
+                  prm->const_viscosity, c->viscous ? 0 : 1, prm->inv_surf_flux, prm->inv_vol_flux, prm->plens_2d};
+    c->bp.thr = prm->threshold_factor * std::pow(10, -prm->threshold_exp_factor * (std::pow(c->N + 1, 0.25)));
+    c->bp.sharp = prm->sharpness_factor;
+    c->bp.amin = prm->alpha_min;
+    c->bp.amax = prm->alpha_max;
+    c->bp.func = prm->blender_function;
+    c->bp.var = prm->blender_variable;
+    c->bp.expr_wall = prm->expr_wall_blender_limit;
+    c->bp.expr_vis = prm->expr_vis_blending_region;
+    c->bp.expr_courant = prm->expr_courant;
+    c->bp.do_filter = prm->do_filtering;
+
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    const int64_t nd = c->nd, nc = c->nc, nt = c->ntask;
+    Dev& d = c->dv;
+    d.nc = nc;
+    d.nd = nd;
+    d.ntask = nt;
+    d.nslot = c->nslot;
+    int r = 0;
+    if ((r = dupload(c, &d.detJ, mesh->detJ, nd)) || (r = dupload(c, &d.Ja, mesh->Ja, 9 * nd)) ||
+        (r = dupload(c, &d.Jinv, mesh->Jinv, 9 * nd)) || (r = dupload(c, &d.h_min, mesh->h_min, nc)) ||
+        (r = dupload(c, &d.center, mesh->cell_center, 3 * nc)) || (r = dupload(c, &d.cell_nbr, mesh->cell_nbr, 6 * nc)) ||
+        (r = dupload(c, &d.ft_cell, mesh->ft_cell, nt)) || (r = dupload(c, &d.ft_face, mesh->ft_face, nt)) ||
+        (r = dupload(c, &d.ft_nbr_cell, mesh->ft_nbr_cell, nt)) || (r = dupload(c, &d.ft_nbr_face, mesh->ft_nbr_face, nt)) ||
+        (r = dupload(c, &d.ft_bc, mesh->ft_bc, nt)) || (r = dupload(c, &d.ft_nbr_fdof, mesh->ft_nbr_fdof, nt * P2)) ||
+        (r = dupload(c, &d.ft_normal, mesh->ft_normal, nt * P2 * 3)) || (r = dupload(c, &d.ft_xyz, mesh->ft_xyz, nt * P2 * 3)) ||
+        (r = dupload(c, &d.bcs, prm->bcs, prm->n_bc)) ||
+        (r = dupload(c, &d.expr_code, prm->expr_code, prm->n_expr_insn)) ||
+        (r = dupload(c, &d.expr_off, prm->expr_offset, prm->n_expr)) ||
+        (r = dupload(c, &d.expr_len, prm->expr_length, prm->n_expr)))
+        return r;
+    d.n_bc = prm->n_bc;
+    d.n_expr = prm->n_expr;
+    // wall cells: a boundary face of type uniform temp wall or insulated wall
+    // (dgsem/plens.cc:2909-2920)
+    {
+        std::vector<uint8_t> wall(nc, 0);
+        for (int64_t cc = 0; cc < nc; ++cc)
+            for (int f = 0; f < 6; ++f) {
+                const int b = mesh->cell_face_bc[6 * cc + f];
+                if (b >= 0 && b < prm->n_bc &&
+                    (prm->bcs[b].type == PLENS_BC_UNIFORM_TEMP_WALL || prm->bcs[b].type == PLENS_BC_INSULATED_WALL))
+                    wall[cc] = 1;
+            }
+        if ((r = dupload(c, &d.cell_wall, wall.data(), nc))) return r;
+    }
+    if ((r = dalloc(c, &d.U, 5 * nd)) || (r = dalloc(c, &d.alpha_raw, nc)) || (r = dalloc(c, &d.alpha, nc)) ||
+        (r = dalloc(c, &d.alpha_d, nc)) || (r = dalloc(c, &d.sf, 5 * c->nslot)) || (r = dalloc(c, &c->sc, 1)) ||
+        (r = dalloc(c, &c->Rout, 5 * nd)))
+        return r;
+    if (prm->do_filtering && (r = dalloc(c, &d.tvstat, 3 * nc))) return r;
+    if (prm->rk_order == 4) {
+        for (int k = 0; k < 3; ++k)
+            if ((r = dalloc(c, &c->R[k], 5 * nd))) return r;
+    } else if ((r = dalloc(c, &d.U0, 5 * nd))) {
+        return r;
+    }
+    if (c->viscous) {
+        if ((r = dalloc(c, &d.sf3, 5 * c->nslot)) || (r = dalloc(c, &d.avars, 9 * nd))) return r;
+        CK(cudaMemset(d.avars, 0, sizeof(double) * 9 * nd));
+    }
+    if (c->learned) {
+        if ((r = dalloc(c, &d.lo_list, nc)) || (r = dalloc(c, &d.lo_count, 1))) return r;
+        if ((r = mlp_create(c->mlp, nc, c->allocs))) return fail(c, PLENS_GPU_E_CUDA, "mlp buffers");
+        c->mlp.tol = prm->judge_alpha_tol;
+    }
+    d.sc = c->sc;
+    CK(cudaMemset(d.alpha, 0, sizeof(double) * nc));
+    CK(cudaMemset(d.alpha_raw, 0, sizeof(double) * nc));
+    CK(cudaMemset(d.alpha_d, 0, sizeof(double) * nc));
+    Scalars h{};
+    h.time = 0;
+    h.bad_dof = INT64_MAX;
+    h.dtmin = ord_double_host(1e6);
+    CK(cudaMemcpy(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int plens_gpu_set_kernel_timing(plens_ctx* c, int enable)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    if (int r = sync_and_check(c)) return r;
+    c->timing = enable != 0;
+    c->vol_ms = 0;
+    c->vol_n = 0;
+    return 0;
+}
+
+int plens_gpu_kernel_timing(plens_ctx* c, double* volume_ms, int64_t* volume_launches)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    if (int r = sync_and_check(c)) return r;
+    if (volume_ms) *volume_ms = c->vol_ms;
+    if (volume_launches) *volume_launches = c->vol_n;
+    return 0;
+}
+
+int plens_gpu_destroy(plens_ctx* c)
+{
+    if (!c) return 0;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& pr : c->ev_pool) {
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    for (void* p : c->allocs) cudaFree(p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return 0;
+}
+
+const char* plens_gpu_last_error(const plens_ctx* c) { return c ? c->err.c_str() : "null context"; }
+int64_t plens_gpu_kernel_launches(const plens_ctx* c) { return c ? c->launches : 0; }
+void* plens_gpu_stream(const plens_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int plens_gpu_set_state(plens_ctx* c, const double* U)
+{
+    if (!c || !U || !c->dv.U) return PLENS_GPU_E_INVALID;
+    CK(cudaMemcpyAsync(c->dv.U, U, sizeof(double) * 5 * c->nd, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int plens_gpu_get_state(plens_ctx* c, double* U)
+{
+    if (!c || !U || !c->dv.U) return PLENS_GPU_E_INVALID;
+    CK(cudaMemcpyAsync(U, c->dv.U, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int plens_gpu_set_time(plens_ctx* c, double t, int64_t n_steps)
+{
+    if (!c || !c->sc) return PLENS_GPU_E_INVALID;
+    CK(cudaStreamSynchronize(c->stream));
+    Scalars h;
+    CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+    h.time = t;
+    h.n_steps = n_steps;
+    h.err = 0;
+    h.bad_dof = INT64_MAX;
+    CK(cudaMemcpy(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int plens_gpu_get_time(plens_ctx* c, double* t, int64_t* n_steps, double* last_dt)
+{
+    if (!c || !c->sc) return PLENS_GPU_E_INVALID;
+    CK(cudaStreamSynchronize(c->stream));
+    Scalars h;
+    CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+    if (t) *t = h.time;
+    if (n_steps) *n_steps = h.n_steps;
+    if (last_dt) *last_dt = h.dt;
+    return 0;
+}
+
+int plens_gpu_rhs(plens_ctx* c, double* R_out)
+{
+    if (!c || !c->dv.U) return PLENS_GPU_E_INVALID;
+    k_step_begin<<<1, 1, 0, c->stream>>>(c->dv, 1e300);
+    c->launches += 1;
+    if (c->learned) c->launches += mlp_step_begin(c->mlp, c->dv, 1, c->stream);
+    StageArgs sa{};
+    sa.mode = 0;
+    sa.Rout = c->Rout;
+    if (int r = launch_rhs(c, sa)) return r;
+    if (int r = sync_and_check(c)) return r;
+    if (R_out) CK(cudaMemcpy(R_out, c->Rout, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int plens_gpu_time_step(plens_ctx* c, double* dt_out)
+{
+    if (!c || !c->dv.U) return PLENS_GPU_E_INVALID;
+    k_step_begin<<<1, 1, 0, c->stream>>>(c->dv, 1e300);
+    c->launches += 1;
+    if (int r = launch_time_step(c)) return r;
+    if (int r = sync_and_check(c)) return r;
+    Scalars h;
+    CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+    if (dt_out) *dt_out = h.dt_update;
+    return 0;
+}
+
+int plens_gpu_advance_async(plens_ctx* c, int64_t n_steps, double end_time)
+{
+    if (!c || !c->dv.U || n_steps < 0) return PLENS_GPU_E_INVALID;
+    if (c->learned && !c->mlp.weights_set) return fail(c, PLENS_GPU_E_INVALID, "learned sensor: weights not set");
+    for (int64_t s = 0; s < n_steps; ++s)
+        if (int r = launch_step(c, end_time)) return r;
+    return 0;
+}
+
+int plens_gpu_synchronize(plens_ctx* c)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    return sync_and_check(c);
+}
+
+int plens_gpu_advance(plens_ctx* c, int64_t n_steps, double end_time)
+{
+    if (int r = plens_gpu_advance_async(c, n_steps, end_time)) return r;
+    return sync_and_check(c);
+}
+
+int plens_gpu_get_cell_scalars(plens_ctx* c, double* alpha, double* alpha_d, double* dt_cell)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    CK(cudaStreamSynchronize(c->stream));
+    if (alpha) CK(cudaMemcpy(alpha, c->dv.alpha, sizeof(double) * c->nc, cudaMemcpyDeviceToHost));
+    if (alpha_d) CK(cudaMemcpy(alpha_d, c->dv.alpha_d, sizeof(double) * c->nc, cudaMemcpyDeviceToHost));
+    if (dt_cell) {
+        Scalars h;
+        CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < c->nc; ++i) dt_cell[i] = h.dt_update;
+    }
+    return 0;
+}
+
+int plens_gpu_get_avars(plens_ctx* c, double* avars)
+{
+    if (!c || !avars) return PLENS_GPU_E_INVALID;
+    if (!c->viscous) return fail(c, PLENS_GPU_E_INVALID, "inviscid run has no auxiliary variables");
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(avars, c->dv.avars, sizeof(double) * 9 * c->nd, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int plens_gpu_first_bad_dof(const plens_ctx* c, int64_t* dof)
+{
+    if (!c || !dof) return PLENS_GPU_E_INVALID;
+    *dof = c->bad_dof_host;
+    return 0;
+}
+
+int plens_gpu_set_sensor_weights(plens_ctx* c, const float* params)
+{
+    if (!c || !params) return PLENS_GPU_E_INVALID;
+    if (!c->learned) return fail(c, PLENS_GPU_E_INVALID, "context was created without the learned sensor");
+    if (mlp_set_weights(c->mlp, params, c->stream)) return fail(c, PLENS_GPU_E_CUDA, "weight upload");
+    return 0;
+}
+
+int plens_gpu_sensor_stats(plens_ctx* c, int64_t* judged, int64_t* fallbacks, double* max_alpha_err, int64_t* lo_cells)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    CK(cudaStreamSynchronize(c->stream));
+    Scalars h;
+    CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+    if (judged) *judged = h.judged;
+    if (fallbacks) *fallbacks = h.fallbacks;
+    if (max_alpha_err) *max_alpha_err = h.max_alpha_err;
+    if (lo_cells) *lo_cells = h.lo_cells;
+    return 0;
+}
+
+int plens_gpu_sensor_pairs(plens_ctx* c, float* x, float* y)
+{
+    if (!c || !x || !y) return PLENS_GPU_E_INVALID;
+    if (int r = mlp_pairs(c->dv, c->ops, c->gas, c->bp, c->P, x, y, c->stream, c->launches)) return fail(c, r, "sensor pairs");
+    return 0;
+}
+
+}  // extern "C"
