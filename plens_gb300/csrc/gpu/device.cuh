@@ -19,7 +19,29 @@ struct Ops {
     double Q[kMaxP * kMaxP];
     double C1[kMaxP * kMaxP];
     double tv[kMaxP];  // total variation of the 1D Legendre modes (blender_calculator.cc:69-86)
+    // FP32 copies for the mixed form (the operators are consumed in the arithmetic type)
+    float fw[kMaxP];
+    float fD[kMaxP * kMaxP];
+    float fQ[kMaxP * kMaxP];
 };
+
+template <class T> __device__ __forceinline__ T opD(const Ops& o, int i)
+{
+    if constexpr (sizeof(T) == 8) return o.D[i]; else return o.fD[i];
+}
+// 2*D_ij: scaling by 2 is exact, so (2*D)*norm equals the reference's 2*D*norm bitwise
+template <class T> __device__ __forceinline__ T opD2(const Ops& o, int i)
+{
+    if constexpr (sizeof(T) == 8) return 2.0 * o.D[i]; else return 2.0f * o.fD[i];
+}
+template <class T> __device__ __forceinline__ T opQ(const Ops& o, int i)
+{
+    if constexpr (sizeof(T) == 8) return o.Q[i]; else return o.fQ[i];
+}
+template <class T> __device__ __forceinline__ T opW(const Ops& o, int i)
+{
+    if constexpr (sizeof(T) == 8) return o.w[i]; else return o.fw[i];
+}
 
 struct GasP {
     double gamma, R, Pr, mu0, T0, S;

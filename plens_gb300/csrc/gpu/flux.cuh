@@ -27,13 +27,21 @@ template <> __device__ __forceinline__ float dpow<float>(float x, float y) { ret
 template <class T> __device__ __forceinline__ T dabs(T x) { return fabs(x); }
 template <> __device__ __forceinline__ float dabs<float>(float x) { return fabsf(x); }
 
+// Division and logarithm: IEEE division / libm log in FP64 (the plain form reproduces the
+// reference's arithmetic); the fast hardware approximations in FP32 (the mixed form, whose
+// accuracy target is a relative L1 error of 1e-4).
+template <class T> __device__ __forceinline__ T fdiv(T a, T b) { return a / b; }
+template <> __device__ __forceinline__ float fdiv<float>(float a, float b) { return __fdividef(a, b); }
+template <class T> __device__ __forceinline__ T flog(T x) { return log(x); }
+template <> __device__ __forceinline__ float flog<float>(float x) { return __logf(x); }
+
 template <class T>
 __device__ __forceinline__ T get_p(const T c[5], T gma)  // navier_stokes.cc:375-383
 {
     T ske = c[1] * c[1];
     ske += c[2] * c[2];
     ske += c[3] * c[3];
-    ske *= T(0.5) / c[0];
+    ske *= fdiv(T(0.5), c[0]);
     return (gma - 1) * (c[4] - ske);
 }
 
@@ -52,16 +60,22 @@ __device__ __forceinline__ T get_e(const T c[5])  // navier_stokes.cc:349-359
 template <class T>
 __device__ __forceinline__ T log_avg(T xl, T xr)
 {
-    const T xi = xl / xr, f = (xi - 1) / (xi + 1), u = f * f;
-    const T F = (u < T(1e-2)) ? T(1) + u / T(3) + u * u / T(5) + u * u * u / T(7) : T(0.5) * dlog(xi) / f;
-    return T(0.5) * (xl + xr) / F;
+    const T xi = fdiv(xl, xr), f = fdiv(xi - 1, xi + 1), u = f * f;
+    T F;
+    if constexpr (sizeof(T) == 8) {
+        F = (u < T(1e-2)) ? T(1) + u / T(3) + u * u / T(5) + u * u * u / T(7) : T(0.5) * dlog(xi) / f;
+    } else {
+        F = (u < T(1e-2)) ? T(1) + u * T(1.0 / 3) + u * u * T(0.2) + u * u * u * T(1.0 / 7)
+                          : fdiv(T(0.5) * flog(xi), f);
+    }
+    return fdiv(T(0.5) * (xl + xr), F);
 }
 
 // physical inviscid flux along a unit direction (navier_stokes.cc:424-442)
 template <class T>
 __device__ __forceinline__ void inv_flux(const T c[5], const T dir[3], T gma, T f[5])
 {
-    const T ri = T(1.0) / c[0];
+    const T ri = fdiv(T(1.0), c[0]);
     const T v0 = c[1] * ri, v1 = c[2] * ri, v2 = c[3] * ri;
     const T p = get_p(c, gma);
     T vn = v0 * dir[0];
@@ -80,7 +94,7 @@ template <class T>
 __device__ __forceinline__ void chandrashekhar_vol(const T q1[7], const T q2[7], const T dir[3], T gma, T f[5])
 {
     const T beta_ln = log_avg(q1[6], q2[6]);
-    const T p_hat = T(0.5) * (q1[0] + q2[0]) / (q1[6] + q2[6]);
+    const T p_hat = fdiv(T(0.5) * (q1[0] + q2[0]), q1[6] + q2[6]);
     const T rho_ln = log_avg(q1[0], q2[0]);
     T va[3], vsq[3];
 #pragma unroll
@@ -88,7 +102,34 @@ __device__ __forceinline__ void chandrashekhar_vol(const T q1[7], const T q2[7],
         va[d] = T(0.5) * (q1[2 + d] + q2[2 + d]);
         vsq[d] = T(0.5) * (q1[2 + d] * q1[2 + d] + q2[2 + d] * q2[2 + d]);
     }
-    T H = T(0.5) / ((gma - 1) * beta_ln) + p_hat / rho_ln;
+    T H = fdiv(T(0.5), (gma - 1) * beta_ln) + fdiv(p_hat, rho_ln);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) H += va[d] * va[d] - T(0.5) * vsq[d];
+    T vn = va[0] * dir[0];
+    vn += va[1] * dir[1];
+    vn += va[2] * dir[2];
+    f[0] = vn * rho_ln;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) f[1 + d] = rho_ln * vn * va[d] + p_hat * dir[d];
+    f[4] = rho_ln * vn * H;
+}
+
+// The same flux for two identical states (the m = i term of the volume sum). log_avg(x, x)
+// returns x exactly (x/x = 1, f = 0, series branch, 0.5*(x+x)/1 = x), so skipping the two
+// logarithmic means is bitwise identical to chandrashekhar_vol(q, q, ...).
+template <class T>
+__device__ __forceinline__ void chandrashekhar_vol_same(const T q[7], const T dir[3], T gma, T f[5])
+{
+    const T beta_ln = q[6];
+    const T p_hat = fdiv(T(0.5) * (q[0] + q[0]), q[6] + q[6]);
+    const T rho_ln = q[0];
+    T va[3], vsq[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        va[d] = T(0.5) * (q[2 + d] + q[2 + d]);
+        vsq[d] = T(0.5) * (q[2 + d] * q[2 + d] + q[2 + d] * q[2 + d]);
+    }
+    T H = fdiv(T(0.5), (gma - 1) * beta_ln) + fdiv(p_hat, rho_ln);
 #pragma unroll
     for (int d = 0; d < 3; ++d) H += va[d] * va[d] - T(0.5) * vsq[d];
     T vn = va[0] * dir[0];
@@ -165,11 +206,11 @@ __device__ __forceinline__ void hllc_x(const T l[5], const T r[5], T gma, T f[5]
 {
     const T pl = get_p(l, gma), pr = get_p(r, gma);
     const T pmin = (pl < pr) ? pl : pr, pmax = (pl < pr) ? pr : pl;
-    const T ul = l[1] / l[0], ur = r[1] / r[0];
-    const T al = dsqrt(gma * pl / l[0]), ar = dsqrt(gma * pr / r[0]);
+    const T ul = fdiv(l[1], l[0]), ur = fdiv(r[1], r[0]);
+    const T al = dsqrt(fdiv(gma * pl, l[0])), ar = dsqrt(fdiv(gma * pr, r[0]));
     const T p_pvrs = T(0.5) * (pl + pr) - T(0.5) * (ur - ul) * T(0.5) * (l[0] + r[0]) * T(0.5) * (al + ar);
     T ps;
-    if (pmax / pmin < T(2) && pmin <= p_pvrs && p_pvrs <= pmax) {
+    if (fdiv(pmax, pmin) < T(2) && pmin <= p_pvrs && p_pvrs <= pmax) {
         ps = p_pvrs;
     } else if (p_pvrs < pmin) {
         const T z = (gma - 1) / (T(2) * gma);
@@ -183,19 +224,19 @@ __device__ __forceinline__ void hllc_x(const T l[5], const T r[5], T gma, T f[5]
     const T ql = (ps <= pl) ? T(1) : dsqrt(T(1) + (gma + 1) / (T(2) * gma) * (ps / pl - T(1)));
     const T qr = (ps <= pr) ? T(1) : dsqrt(T(1) + (gma + 1) / (T(2) * gma) * (ps / pr - T(1)));
     const T sl = ul - al * ql, sr = ur + ar * qr;
-    const T s = (pr - pl + l[1] * (sl - ul) - r[1] * (sr - ur)) / (l[0] * (sl - ul) - r[0] * (sr - ur));
+    const T s = fdiv(pr - pl + l[1] * (sl - ul) - r[1] * (sr - ur), l[0] * (sl - ul) - r[0] * (sr - ur));
     if (sl > T(0)) {
         xflux_phys(l, gma, f);
     } else if (s > T(0)) {
-        const T t = (sl - ul) / (sl - s);
-        const T ss[5] = {t * l[0], t * l[0] * s, t * l[2], t * l[3], t * (l[4] + (s - ul) * (l[0] * s + pl / (sl - ul)))};
+        const T t = fdiv(sl - ul, sl - s);
+        const T ss[5] = {t * l[0], t * l[0] * s, t * l[2], t * l[3], t * (l[4] + (s - ul) * (l[0] * s + fdiv(pl, sl - ul)))};
         T lf[5];
         xflux_phys(l, gma, lf);
 #pragma unroll
         for (int v = 0; v < 5; ++v) f[v] = lf[v] + sl * (ss[v] - l[v]);
     } else if (sr > T(0)) {
-        const T t = (sr - ur) / (sr - s);
-        const T ss[5] = {t * r[0], t * r[0] * s, t * r[2], t * r[3], t * (r[4] + (s - ur) * (r[0] * s + pr / (sr - ur)))};
+        const T t = fdiv(sr - ur, sr - s);
+        const T ss[5] = {t * r[0], t * r[0] * s, t * r[2], t * r[3], t * (r[4] + (s - ur) * (r[0] * s + fdiv(pr, sr - ur)))};
         T rf[5];
         xflux_phys(r, gma, rf);
 #pragma unroll
@@ -358,7 +399,7 @@ __device__ __forceinline__ void inv_surf_flux(const T o[5], const T nb[5], const
     const T M = dsqrt(M2);
     T R[3][3];
     if (M > T(1e-3)) {
-        m0 /= M; m1 /= M; m2 /= M;
+        m0 = fdiv(m0, M); m1 = fdiv(m1, M); m2 = fdiv(m2, M);
         const T c = T(1) * n[0] + T(0) * n[1] + T(0) * n[2], t = T(1) - c, s = dsqrt(T(1) - c * c);
         R[0][0] = t * m0 * m0 + c;      R[0][1] = t * m0 * m1 - s * m2; R[0][2] = t * m0 * m2 + s * m1;
         R[1][0] = t * m0 * m1 + s * m2; R[1][1] = t * m1 * m1 + c;      R[1][2] = t * m1 * m2 - s * m0;

@@ -272,7 +272,7 @@ __device__ __forceinline__ void prim_to_cons_t(T rho, const T v[3], T p, T gma, 
 }
 
 template <class T>
-__device__ void bc_ghost(int stage, const Dev& dv, const GasP& g, const plens_bc_desc& b,
+__device__ __forceinline__ void bc_ghost(int stage, const Dev& dv, const GasP& g, const plens_bc_desc& b,
                          const T c[5], const T av[9], const T n[3], const double* xyz, double t,
                          int64_t partner_dof, T cg[5], T ag[9])
 {
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
             for (int md = 0; md < 3; ++md) {
                 const int lo = (md == 0) ? m + P * ti[1] + P2 * ti[2] : (md == 1) ? ti[0] + P * m + P2 * ti[2] : ti[0] + P * ti[1] + P2 * m;
                 const T jc = J[(md * 3 + gd) * P3 + lo];
-                const T dvl = (T)ops.D[ti[md] * P + m];
+                const T dvl = opD<T>(ops, ti[md] * P + m);
 #pragma unroll
                 for (int v = 0; v < 5; ++v) acc[v] += dvl * E[v * P3 + lo] * jc;
             }
@@ -560,16 +560,16 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
                 const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
                 const T jc = J[(sd * 3 + gd) * P3 + node];
                 const T sgn = lr ? T(-1) : T(1);
-                const T wend = (T)ops.w[lr * N];
+                const T wend = opW<T>(ops, lr * N);
 #pragma unroll
                 for (int v = 0; v < 5; ++v) {
                     const T fin = E[v * P3 + node] * jc;
                     const T fsu = sEf[((cl * 6 + f) * 5 + v) * P2 + q] * jc;
-                    acc[v] -= sgn * (fsu - fin) / wend;
+                    acc[v] -= fdiv(sgn * (fsu - fin), wend);
                 }
             }
         }
-        const T jinv = T(1.0) / (T)dv.detJ[cell * P3 + node];
+        const T jinv = fdiv(T(1.0), (T)dv.detJ[cell * P3 + node]);
 #pragma unroll
         for (int v = 0; v < 5; ++v) grad[gd][v] = acc[v] * jinv;
     }
@@ -629,7 +629,7 @@ struct VolSmem {
 };
 
 template <int P, class T, bool VISC>
-__global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops ops, GasP g, StageArgs sa)
+__global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1)) k_volume(Dev dv, Ops ops, GasP g, StageArgs sa)
 {
     using CB = CellBlock<P>;
     constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1, NQ = 7;
@@ -700,20 +700,18 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
                 const T ci[5] = {Cc[ni], Cc[P3 + ni], Cc[2 * P3 + ni], Cc[3 * P3 + ni], Cc[4 * P3 + ni]};
                 // diagonal term m = i (the pair flux of a state with itself)
                 {
-                    T nv[3] = {J[(dir * 3) * P3 + ni], J[(dir * 3 + 1) * P3 + ni], J[(dir * 3 + 2) * P3 + ni]};
-                    nv[0] = T(0.5) * (nv[0] + nv[0]);
-                    nv[1] = T(0.5) * (nv[1] + nv[1]);
-                    nv[2] = T(0.5) * (nv[2] + nv[2]);
+                    // 0.5*(Ja_i + Ja_i) = Ja_i exactly
+                    const T nv[3] = {J[(dir * 3) * P3 + ni], J[(dir * 3 + 1) * P3 + ni], J[(dir * 3 + 2) * P3 + ni]};
                     T nn = nv[0] * nv[0];
                     nn += nv[1] * nv[1];
                     nn += nv[2] * nv[2];
                     nn = dsqrt(nn);
-                    const T dn[3] = {nv[0] / nn, nv[1] / nn, nv[2] / nn};
+                    const T dn[3] = {fdiv(nv[0], nn), fdiv(nv[1], nn), fdiv(nv[2], nn)};
                     T F[5];
-                    if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) chandrashekhar_vol(qi, qi, dn, gm, F);
+                    if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) chandrashekhar_vol_same(qi, dn, gm, F);
                     else if (g.ivf == PLENS_IVF_KENNEDY_GRUBER) kennedy_gruber_vol(qi, qi, get_e(ci), get_e(ci), dn, gm, F);
                     else ismail_roe_vol(ci, ci, dn, gm, F);
-                    const T dvn = T(2) * (T)ops.D[i * P + i] * nn;
+                    const T dvn = opD2<T>(ops, i * P + i) * nn;
 #pragma unroll
                     for (int v = 0; v < 5; ++v) acc[i][v] += dvn * F[v];
                 }
@@ -730,7 +728,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
                     nn += nv[1] * nv[1];
                     nn += nv[2] * nv[2];
                     nn = dsqrt(nn);
-                    const T dn[3] = {nv[0] / nn, nv[1] / nn, nv[2] / nn};
+                    const T dn[3] = {fdiv(nv[0], nn), fdiv(nv[1], nn), fdiv(nv[2], nn)};
                     T F[5];
                     if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) {
                         chandrashekhar_vol(qi, qm, dn, gm, F);
@@ -741,7 +739,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
                         const T cm[5] = {Cc[nm], Cc[P3 + nm], Cc[2 * P3 + nm], Cc[3 * P3 + nm], Cc[4 * P3 + nm]};
                         ismail_roe_vol(ci, cm, dn, gm, F);
                     }
-                    const T di = T(2) * (T)ops.D[i * P + m] * nn, dm = T(2) * (T)ops.D[m * P + i] * nn;
+                    const T di = opD2<T>(ops, i * P + m) * nn, dm = opD2<T>(ops, m * P + i) * nn;
 #pragma unroll
                     for (int v = 0; v < 5; ++v) {
                         acc[i][v] += di * F[v];
@@ -780,19 +778,19 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
                 nn += dn[2] * dn[2];
                 nn = dsqrt(nn);
 #pragma unroll
-                for (int d = 0; d < 3; ++d) dn[d] /= nn;
+                for (int d = 0; d < 3; ++d) dn[d] = fdiv(dn[d], nn);
                 T fin[5];
                 inv_flux(ci, dn, gm, fin);
                 const T ss = lr ? T(-1) : T(1);
-                const T wend = (T)ops.w[lr * N];
+                const T wend = opW<T>(ops, lr * N);
 #pragma unroll
                 for (int v = 0; v < 5; ++v) {
                     const T fs = -ss * (T)dv.sf[v * dv.nslot + (cell * 6 + f) * P2 + q];
-                    ho[v] += -ss * (fs - fin[v]) * nn / wend;
+                    ho[v] += fdiv(-ss * (fs - fin[v]) * nn, wend);
                 }
             }
         }
-        const T js = T(1) / (T(-1) * (T)detJ);
+        const T js = fdiv(T(1), T(-1) * (T)detJ);
 #pragma unroll
         for (int v = 0; v < 5; ++v) ho[v] *= js;
     }
@@ -814,7 +812,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
                 nn += dn[2] * dn[2];
                 nn = dsqrt(nn);
 #pragma unroll
-                for (int d = 0; d < 3; ++d) dn[d] /= nn;
+                for (int d = 0; d < 3; ++d) dn[d] = fdiv(dn[d], nn);
                 T F[5];
                 dif_flux(ci, av, dn, F);
 #pragma unroll
@@ -827,7 +825,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
 #pragma unroll
                 for (int md = 0; md < 3; ++md) {
                     const int lo = (md == 0) ? m + P * ti[1] + P2 * ti[2] : (md == 1) ? ti[0] + P * m + P2 * ti[2] : ti[0] + P * ti[1] + P2 * m;
-                    const T dvl = (T)ops.D[ti[md] * P + m];
+                    const T dvl = opD<T>(ops, ti[md] * P + m);
 #pragma unroll
                     for (int v = 0; v < 5; ++v) hd[v] += dvl * Acc[(md * 5 + v) * P3 + lo];
                 }
@@ -849,19 +847,19 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
                     nn += dn[2] * dn[2];
                     nn = dsqrt(nn);
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) dn[d] /= nn;
+                    for (int d = 0; d < 3; ++d) dn[d] = fdiv(dn[d], nn);
                     T fin[5];
                     dif_flux(ci, av, dn, fin);
                     const T ss = lr ? T(-1) : T(1);
-                    const T wend = (T)ops.w[lr * N];
+                    const T wend = opW<T>(ops, lr * N);
 #pragma unroll
                     for (int v = 0; v < 5; ++v) {
                         const T fs = -ss * (T)dv.sf3[v * dv.nslot + (cell * 6 + f) * P2 + q];
-                        hd[v] += -ss * (fs - fin[v]) * nn / wend;
+                        hd[v] += fdiv(-ss * (fs - fin[v]) * nn, wend);
                     }
                 }
             }
-            const T js = T(1) / (T(1) * (T)detJ);
+            const T js = fdiv(T(1), T(1) * (T)detJ);
 #pragma unroll
             for (int v = 0; v < 5; ++v) hd[v] *= js;
         }
@@ -896,7 +894,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
 #pragma unroll
                     for (int m = 0; m < P; ++m) {
                         const int nm = line_node<P>(dir, la, lb, m);
-                        const T qlm = (T)ops.Q[(id - 1) * P + m];
+                        const T qlm = opQ<T>(ops, (id - 1) * P + m);
 #pragma unroll
                         for (int d = 0; d < 3; ++d) sn[d] += qlm * J[(dir * 3 + d) * P3 + nm];
                     }
@@ -905,16 +903,16 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
                     nn += sn[1] * sn[1];
                     nn += sn[2] * sn[2];
                     nn = dsqrt(nn);
-                    const T dn[3] = {sn[0] / nn, sn[1] / nn, sn[2] / nn};
+                    const T dn[3] = {fdiv(sn[0], nn), fdiv(sn[1], nn), fdiv(sn[2], nn)};
                     const T cL[5] = {Cc[nl], Cc[P3 + nl], Cc[2 * P3 + nl], Cc[3 * P3 + nl], Cc[4 * P3 + nl]};
                     const T cR[5] = {Cc[nr], Cc[P3 + nr], Cc[2 * P3 + nr], Cc[3 * P3 + nr], Cc[4 * P3 + nr]};
                     T F[5];
                     inv_surf_flux(cL, cR, dn, gm, g.isf, fb, F);
-                    const T wl = (T)ops.w[id - 1], wr = (T)ops.w[id];
+                    const T wl = opW<T>(ops, id - 1), wr = opW<T>(ops, id);
 #pragma unroll
                     for (int v = 0; v < 5; ++v) {
-                        acc[id - 1][v] += F[v] * nn / wl;
-                        acc[id][v] -= F[v] * nn / wr;
+                        acc[id - 1][v] += fdiv(F[v] * nn, wl);
+                        acc[id][v] -= fdiv(F[v] * nn, wr);
                     }
                 }
                 // cell-face terms at both ends of the line
@@ -929,11 +927,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
                     nn += J[(dir * 3 + 2) * P3 + ni] * J[(dir * 3 + 2) * P3 + ni];
                     nn = dsqrt(nn);
                     const T sg = lr ? T(1) : T(-1);  // contrib_sign and flux_sign
-                    const T wend = (T)ops.w[lr * N];
+                    const T wend = opW<T>(ops, lr * N);
 #pragma unroll
                     for (int v = 0; v < 5; ++v) {
                         const T fl = sg * (T)dv.sf[v * dv.nslot + (cell * 6 + f) * P2 + q];
-                        acc[i][v] += sg * fl * nn / wend;
+                        acc[i][v] += fdiv(sg * fl * nn, wend);
                     }
                 }
 #pragma unroll
@@ -947,7 +945,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_volume(Dev dv, Ops op
         __syncthreads();
         if (do_lo) {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) lo[v] = (Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node]) / (T)(-detJ);
+            for (int v = 0; v < 5; ++v) lo[v] = fdiv(Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node], (T)(-detJ));
         }
     }
     if (!valid) return;

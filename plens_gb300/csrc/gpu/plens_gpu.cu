@@ -114,6 +114,11 @@ static Ops make_ops(int P)
             }
             o.C1[a * P + i] = s;
         }
+    for (int i = 0; i < P; ++i) o.fw[i] = (float)o.w[i];
+    for (int i = 0; i < P * P; ++i) {
+        o.fD[i] = (float)o.D[i];
+        o.fQ[i] = (float)o.Q[i];
+    }
     o.tv[0] = 0.0;
     if (P > 1) o.tv[1] = std::fabs(legendre01(1, 1) - legendre01(1, 0));
     for (int ip = 2; ip < P; ++ip) {
@@ -539,6 +544,7 @@ int plens_gpu_get_time(plens_ctx* c, double* t, int64_t* n_steps, double* last_d
 int plens_gpu_rhs(plens_ctx* c, double* R_out)
 {
     if (!c || !c->dv.U) return PLENS_GPU_E_INVALID;
+    if (c->learned && !c->mlp.weights_set) return fail(c, PLENS_GPU_E_INVALID, "learned sensor: weights not set");
     k_step_begin<<<1, 1, 0, c->stream>>>(c->dv, 1e300);
     c->launches += 1;
     if (c->learned) c->launches += mlp_step_begin(c->mlp, c->dv, 1, c->stream);

@@ -1,0 +1,85 @@
+"""Learned troubled-cell sensor: the CUDA forward / backward / Adam kernels against the FP64
+numpy oracle, training on (nodal rho*p -> alpha) pairs logged from plain runs, and the sensor
+inside the RHS with its judge and fallback."""
+import numpy as np
+import pytest
+
+from helpers import make, rel_l1
+from oracle import mlp_oracle
+from oracle.pyoracle import Oracle
+from plens_gb300 import configs
+from plens_gb300.api import GpuSolver, mlp_infer, mlp_loss_grad, mlp_train
+
+pytestmark = pytest.mark.gpu
+
+
+def _data(n, seed=1):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0, 0.3, (n, 64)).astype(np.float32)
+    y = (0.5 / (1 + np.exp(-8 * (np.abs(x).mean(1) - 0.24)))).astype(np.float32)
+    return x, y
+
+
+def test_mlp_forward_matches_oracle():
+    p = mlp_oracle.init_params(3)
+    x, _ = _data(333)
+    a_gpu = mlp_infer(x, p)
+    a_ref, _ = mlp_oracle.forward(p, x)
+    np.testing.assert_allclose(a_gpu, a_ref, rtol=2e-4, atol=2e-6)
+
+
+def test_mlp_gradient_matches_oracle():
+    p = mlp_oracle.init_params(4)
+    p[-1] = 0.0  # sigmoid in its sensitive range
+    x, y = _data(517, seed=2)
+    loss_g, g_gpu = mlp_loss_grad(x, y, p)
+    loss_r, g_ref = mlp_oracle.loss_grad(p, x, y)
+    assert abs(loss_g - loss_r) <= 1e-4 * abs(loss_r)
+    scale = np.abs(g_ref).max()
+    assert np.abs(g_gpu - g_ref).max() <= 1e-3 * scale
+    # per block: W1, W2, w3 are all exercised
+    assert np.abs(g_ref[:4096]).max() > 0 and np.abs(g_ref[4160:8256]).max() > 0
+
+
+def test_mlp_training_reduces_loss():
+    x, y = _data(8192, seed=5)
+    p0 = mlp_oracle.init_params(6)
+    p, loss = mlp_train(x, y, p0, epochs=20, batch=4096, lr=1e-3, seed=7)
+    assert loss[-1] < 0.5 * loss[0], loss
+    l_ref, _ = mlp_oracle.loss_grad(p, x, y)
+    assert abs(l_ref - loss[-1]) < 0.5 * loss[-1] + 1e-4
+
+
+def test_learned_sensor_in_the_rhs():
+    """Pairs from the plain blender on an evolving DMR state -> train -> run with the learned
+    sensor: judged steps happen, the result stays within the accuracy bound of the FP64 oracle."""
+    base = make(configs.dmr(nx=24, ny=6))
+    o = Oracle(base)
+    o.set_state(base.initial_state(), 0.0)
+    g = GpuSolver(base)
+    xs, ys = [], []
+    for _ in range(6):
+        o.advance(5)
+        U, t, _, _ = o.get_state()
+        g.set_state(U, t)
+        x, y = g.sensor_pairs()
+        xs.append(x)
+        ys.append(y)
+    x = np.concatenate(xs)
+    y = np.concatenate(ys)
+    assert (y > 0).any()
+    p, loss = mlp_train(x, y, mlp_oracle.init_params(0), epochs=200, batch=256, lr=1e-3, seed=1)
+    assert loss[-1] < loss[0]
+    spec = configs.dmr(nx=24, ny=6, precision="mixed", sensor="learned")
+    case = make(spec)
+    gl = GpuSolver(case)
+    gl.set_sensor_weights(p)
+    gl.set_state(case.initial_state(), 0.0)
+    gl.advance(30)
+    st = gl.sensor_stats()
+    assert st["judged"] >= 2
+    ref = Oracle(base)
+    ref.set_state(base.initial_state(), 0.0)
+    ref.advance(30)
+    err = rel_l1(gl.get_state(), ref.get_state()[0])
+    assert err[0] <= 1e-4, (err, st)

@@ -155,8 +155,11 @@ def test_viscous_cylinder_rhs_parity():
     g.set_state(U, t)
     Rg = g.rhs()
     Ag = g.avars()
-    sc = np.abs(Ao).max(axis=1, keepdims=True)
-    assert (np.abs(Ag - Ao) / np.where(sc > 0, sc, 1)).max() <= RHS_TOL
+    # stress components measured against the largest stress, heat-flux components against the
+    # largest heat flux (z components are round-off noise in this 2D flow)
+    d = np.abs(Ag - Ao)
+    assert d[:6].max() / np.abs(Ao[:6]).max() <= RHS_TOL
+    assert d[6:].max() / np.abs(Ao[6:]).max() <= RHS_TOL
     assert max_rel_err(Rg, Ro) <= RHS_TOL
 
 
