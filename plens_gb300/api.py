@@ -68,6 +68,20 @@ class Params(C.Structure):
     ]
 
 
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("degree", C.c_int32), ("n_cells", C.c_int64),
+        ("detJ", C.POINTER(C.c_double)), ("Ja", C.POINTER(C.c_double)), ("Jinv", C.POINTER(C.c_double)),
+        ("h_min", C.POINTER(C.c_double)), ("cell_center", C.POINTER(C.c_double)),
+        ("cell_nbr", C.POINTER(C.c_int32)), ("cell_face_bc", C.POINTER(C.c_int32)),
+        ("n_face_tasks", C.c_int64),
+        ("ft_cell", C.POINTER(C.c_int32)), ("ft_face", C.POINTER(C.c_int32)),
+        ("ft_nbr_cell", C.POINTER(C.c_int32)), ("ft_nbr_face", C.POINTER(C.c_int32)),
+        ("ft_bc", C.POINTER(C.c_int32)), ("ft_nbr_fdof", C.POINTER(C.c_int32)),
+        ("ft_normal", C.POINTER(C.c_double)), ("ft_xyz", C.POINTER(C.c_double)),
+    ]
+
+
 _host = None
 _gpu = None
 
@@ -189,6 +203,26 @@ class Case:
     @property
     def params(self) -> Params:
         return self._L.plens_case_params_mut(self._h).contents
+
+    def mesh_arrays(self) -> dict:
+        """Copies of the mesh-description arrays (metric terms, neighbour and face tables)."""
+        m = C.cast(C.c_void_p(self.mesh_ptr), C.POINTER(MeshDesc)).contents
+        P = m.degree + 1
+        nd, nc, nt = self.n_dofs, m.n_cells, m.n_face_tasks
+        arr = lambda p, n: np.ctypeslib.as_array(p, shape=(n,)).copy()  # noqa: E731
+        return {
+            "degree": m.degree, "n_cells": nc, "n_face_tasks": nt,
+            "detJ": arr(m.detJ, nd), "Ja": arr(m.Ja, 9 * nd).reshape(3, 3, nd),
+            "Jinv": arr(m.Jinv, 9 * nd).reshape(3, 3, nd), "h_min": arr(m.h_min, nc),
+            "cell_center": arr(m.cell_center, 3 * nc).reshape(nc, 3),
+            "cell_nbr": arr(m.cell_nbr, 6 * nc).reshape(nc, 6),
+            "cell_face_bc": arr(m.cell_face_bc, 6 * nc).reshape(nc, 6),
+            "ft_cell": arr(m.ft_cell, nt), "ft_face": arr(m.ft_face, nt),
+            "ft_nbr_cell": arr(m.ft_nbr_cell, nt), "ft_nbr_face": arr(m.ft_nbr_face, nt),
+            "ft_bc": arr(m.ft_bc, nt), "ft_nbr_fdof": arr(m.ft_nbr_fdof, nt * P * P).reshape(nt, P * P),
+            "ft_normal": arr(m.ft_normal, nt * P * P * 3).reshape(nt, P * P, 3),
+            "ft_xyz": arr(m.ft_xyz, nt * P * P * 3).reshape(nt, P * P, 3),
+        }
 
     def initial_state(self) -> np.ndarray:
         U = np.empty((5, self.n_dofs), dtype=np.float64)

@@ -44,7 +44,7 @@ def test_mlp_gradient_matches_oracle():
 def test_mlp_training_reduces_loss():
     x, y = _data(8192, seed=5)
     p0 = mlp_oracle.init_params(6)
-    p, loss = mlp_train(x, y, p0, epochs=20, batch=4096, lr=1e-3, seed=7)
+    p, loss = mlp_train(x, y, p0, epochs=20, batch=256, lr=1e-3, seed=7)
     assert loss[-1] < 0.5 * loss[0], loss
     l_ref, _ = mlp_oracle.loss_grad(p, x, y)
     assert abs(l_ref - loss[-1]) < 0.5 * loss[-1] + 1e-4
