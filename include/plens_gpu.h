@@ -202,6 +202,24 @@ int plens_gpu_rhs(plens_ctx* ctx, double* R_out);
  * stepping: dt = min over dofs of Co/(N^1.5 (max_k (Jinv^T u)_k + a/h + N^2 mu/(h^2 rho))). */
 int plens_gpu_time_step(plens_ctx* ctx, double* dt_out);
 
+/* Stable time step of a caller-owned state, allocating nothing. No counterpart in the reference:
+ * it is for callers that may not allocate device memory -- a framework that owns all GPU memory
+ * through its own pool and forbids libraries from calling cudaMalloc, or a loop that must not
+ * allocate while it runs. Same result as plens_gpu_time_step, but on device arrays the caller
+ * passes: U [5][ndof], Jinv [9][ndof] and h_min [n_cells] in the layouts of plens_mesh_desc, the
+ * gas of `params`, the Courant number `courant` (capped to 0.9 when >= 1), and dt_out, one
+ * double in device memory that receives the step (before any end-time clip). Runs on `stream`
+ * (a cudaStream_t, may be NULL) and returns without synchronising.
+ * Scratch: the per-cell steps go to a library-owned device array of PLENS_GPU_NOALLOC_MAX_CELLS
+ * doubles (2 MiB) that every GPU using the library keeps until the process exits; larger meshes
+ * return PLENS_GPU_E_INVALID. All calls share that array: calls that overlap on the GPU race.
+ * The first call on each device looks the array up (cudaGetSymbolAddress); make that first call
+ * before any stream capture. */
+#define PLENS_GPU_NOALLOC_MAX_CELLS (1 << 18)
+int plens_gpu_time_step_noalloc(const double* U, const double* Jinv, const double* h_min, int64_t n_cells,
+                                int32_t degree, const plens_params* params, double courant, double* dt_out,
+                                void* stream);
+
 /* n_steps calls of PLENS::update (dgsem/plens.cc:4484-4518): each step computes dt on the device
  * at stage 1, clips it to end_time - t (dgsem/plens.cc:4341), runs the RK stages
  * (update_rk4 dgsem/plens.cc:4334-4403 or update_rk3 4420-4475) and advances the device clock.
