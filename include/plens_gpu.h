@@ -239,19 +239,25 @@ int plens_gpu_first_bad_dof(const plens_ctx* ctx, int64_t* dof);
 
 /* ----------------------------------------------------- learned troubled-cell sensor
  * New component (no counterpart in the reference): an MLP (64 -> 64 -> 64 -> 1, GELU,
- * sigmoid*alpha_max) that replaces BlenderCalculator::get_blender and the neighbour smoothing
- * (dgsem/blender_calculator.cc:123-177, dgsem/plens.cc:2926-2947). Weights are FP32, laid out
- * W1[64][64], b1[64], W2[64][64], b2[64], W3[64], b3[1] (row-major, out x in). */
+ * sigmoid*alpha_max) that replaces the modal indicator BlenderCalculator::get_blender
+ * (dgsem/blender_calculator.cc:123-177); the neighbour smoothing (dgsem/plens.cc:2926-2947) then
+ * runs on its output and also emits the compacted troubled-cell list. Values below
+ * max(alpha_min, 0.01) are set to 0. Weights are FP32, laid out W1[64][64], b1[64], W2[64][64],
+ * b2[64], W3[64], b3[1] (row-major, out x in). */
 #define PLENS_MLP_IN 64
 #define PLENS_MLP_HIDDEN 64
 #define PLENS_MLP_N_PARAMS (64 * 64 + 64 + 64 * 64 + 64 + 64 + 1)
 int plens_gpu_set_sensor_weights(plens_ctx* ctx, const float* params /* [PLENS_MLP_N_PARAMS] */);
-/* Learned-sensor statistics: steps judged, judged steps that fell back, max per-cell alpha
- * error seen, and the number of cells the subcell kernel ran on in the last RHS. */
+/* Learned-sensor statistics: steps judged; fallbacks = cells handed back to the plain modal
+ * indicator, summed over the judged steps (a cell whose alpha error exceeds the judge tolerance
+ * keeps the plain indicator until the next judged step; a step redone after a positivity
+ * failure counts every cell); the max per-cell alpha error seen; and the number of cells the
+ * subcell kernel ran on in the last RHS. */
 int plens_gpu_sensor_stats(plens_ctx* ctx, int64_t* judged, int64_t* fallbacks,
                            double* max_alpha_err, int64_t* lo_cells_last);
-/* Appends (per-cell nodal rho*p interpolated to 4^3 GLL nodes -> final alpha) training pairs of
- * the current state to host buffers: x [n_cells][64] FP32, y [n_cells] FP32. */
+/* Training pairs of the current state: x [n_cells][64] FP32, the sensor input (nodal rho*p
+ * interpolated to the 4^3 GLL nodes, divided by its mean, minus 1); y [n_cells] FP32, the modal
+ * indicator's alpha before neighbour smoothing (with the wall override). */
 int plens_gpu_sensor_pairs(plens_ctx* ctx, float* x, float* y);
 
 /* MLP training on the device with the library's own forward, backward and Adam kernels.

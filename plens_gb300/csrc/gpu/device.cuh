@@ -23,7 +23,13 @@ struct Ops {
     float fw[kMaxP];
     float fD[kMaxP * kMaxP];
     float fQ[kMaxP * kMaxP];
+    float fC1[kMaxP * kMaxP];
 };
+
+template <class T> __device__ __forceinline__ T opC1(const Ops& o, int i)
+{
+    if constexpr (sizeof(T) == 8) return o.C1[i]; else return o.fC1[i];
+}
 
 template <class T> __device__ __forceinline__ T opD(const Ops& o, int i)
 {
@@ -55,6 +61,7 @@ struct BlendP {
     int expr_wall, expr_vis, expr_courant;
     int do_filter;
     int gate;      // 1: the plain blender runs only while the learned sensor is in fallback
+    const uint8_t* mask;  // if set (and not in fallback): the plain blender runs only on cells with mask 1
 };
 
 // Device scalars of one context, in one allocation.

@@ -118,20 +118,32 @@ static __global__ void k_courant(Dev dv, int expr_courant)
 // ------------------------------------------------------------------------------- blender
 // calc_blender's first half + BlenderCalculator::get_blender / get_trouble
 // (dgsem/plens.cc:2858-2924, dgsem/blender_calculator.cc:123-177, 277-303), with
-// assert_positivity (dgsem/plens.cc:2531-2546) fused in.
-template <int P>
+// assert_positivity (dgsem/plens.cc:2531-2546) fused in. The modal transform and the mode
+// energies run in T (FP64 in the plain form and for the learned sensor's judge, FP32 in the
+// mixed form); the positivity check and alpha are FP64.
+template <int P, class T>
 __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_blender(Dev dv, Ops ops, GasP g, BlendP bp)
 {
     using CB = CellBlock<P>;
     constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1;
-    __shared__ double sA[CPB][P3];
-    __shared__ double sB[CPB][P3];
+    __shared__ T sA[CPB][P3];
+    __shared__ T sB[CPB][P3];
     Scalars* s = dv.sc;
     if (!s->active) return;
-    if (bp.gate && !s->sensor_fallback) return;
+    if (bp.gate && !s->sensor_fallback && !bp.mask) return;
+    const bool masked = bp.mask && !s->sensor_fallback;
+    if (masked) {  // learned sensor: only the cells the judge handed back to this indicator
+        bool any = false;
+#pragma unroll
+        for (int q = 0; q < CPB; ++q) {
+            const int64_t cq = (int64_t)blockIdx.x * CPB + q;
+            any |= (cq < dv.nc) && bp.mask[cq];
+        }
+        if (!any) return;
+    }
     const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
     const int64_t cell = (int64_t)blockIdx.x * CPB + cl;
-    const bool valid = (cl < CPB) && (cell < dv.nc);
+    const bool valid = (cl < CPB) && (cell < dv.nc) && (!masked || bp.mask[cell]);
     const int i = node % P, j = (node / P) % P, k = node / P2;
     if (valid) {
         const int64_t dof = cell * P3 + node;
@@ -142,51 +154,61 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_blender(Dev dv, Ops o
             atomicMin(&s->bad_dof, (long long)dof);
             s->err = PLENS_GPU_E_POSITIVITY;
         }
-        const double p = get_p(c, g.gamma);
-        sA[cl][node] = (bp.var == 2) ? c[0] : (bp.var == 1) ? p : p * c[0];
+        if constexpr (sizeof(T) == 8) {
+            const double p = get_p(c, g.gamma);
+            sA[cl][node] = (bp.var == 2) ? c[0] : (bp.var == 1) ? p : p * c[0];
+        } else {
+            T cf[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) cf[v] = (T)c[v];
+            const T p = get_p(cf, (T)g.gamma);
+            sA[cl][node] = (bp.var == 2) ? cf[0] : (bp.var == 1) ? p : p * cf[0];
+        }
     }
     __syncthreads();
     // separable nodal -> modal transform: x, then y, then z
     if (valid) {
-        double acc = 0;
+        T acc = 0;
 #pragma unroll
-        for (int m = 0; m < P; ++m) acc += ops.C1[i * P + m] * sA[cl][m + P * j + P2 * k];
+        for (int m = 0; m < P; ++m) acc += opC1<T>(ops, i * P + m) * sA[cl][m + P * j + P2 * k];
         sB[cl][node] = acc;
     }
     __syncthreads();
     if (valid) {
-        double acc = 0;
+        T acc = 0;
 #pragma unroll
-        for (int m = 0; m < P; ++m) acc += ops.C1[j * P + m] * sB[cl][i + P * m + P2 * k];
+        for (int m = 0; m < P; ++m) acc += opC1<T>(ops, j * P + m) * sB[cl][i + P * m + P2 * k];
         sA[cl][node] = acc;
     }
     __syncthreads();
     if (valid) {
-        double acc = 0;
+        T acc = 0;
 #pragma unroll
-        for (int m = 0; m < P; ++m) acc += ops.C1[k * P + m] * sA[cl][i + P * j + P2 * m];
+        for (int m = 0; m < P; ++m) acc += opC1<T>(ops, k * P + m) * sA[cl][i + P * j + P2 * m];
         sB[cl][node] = acc;
     }
     __syncthreads();
     if (valid && node == 0) {
-        double et = 0, e1 = 0, e2 = 0, asum = 0, ub = 0, tl = 0;
+        // sums in mode-index order, as the reference's loops over the mode index sets
+        T et = 0, e1 = 0, e2 = 0;
+        double asum = 0, ub = 0, tl = 0;
         for (int m = 0; m < P3; ++m) {
-            const double md = sB[cl][m];
+            const T md = sB[cl][m];
             const int mi = m % P, mj = (m / P) % P, mk = m / P2;
             et += md * md;
             if (mi < N && mj < N && mk < N) e1 += md * md;
             if (mi < N - 1 && mj < N - 1 && mk < N - 1) e2 += md * md;
             if (bp.do_filter) {
-                const double t = fabs(md);
+                const double t = fabs((double)md);
                 asum += t;
                 const double x = t * (ops.tv[mi] + ops.tv[mj] + ops.tv[mk]);
                 ub += x;
                 if (mi <= 1 && mj <= 1 && mk <= 1) tl += x;
             }
         }
-        double trouble = 1 - e1 / et;
+        double trouble = 1 - (double)(e1 / et);
         if (N > 2) {
-            const double t2 = 1 - e2 / e1;
+            const double t2 = 1 - (double)(e2 / e1);
             if (t2 > trouble) trouble = t2;
         }
         double alpha;

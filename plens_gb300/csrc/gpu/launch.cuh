@@ -26,7 +26,7 @@ struct Launch {
 
     static int blender(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
     {
-        k_blender<P><<<grid_cells(dv.nc), CB::THREADS, 0, st>>>(dv, ops, g, bp);
+        k_blender<P, T><<<grid_cells(dv.nc), CB::THREADS, 0, st>>>(dv, ops, g, bp);
         return 1;
     }
     static int surface(int stage, const Dev& dv, const GasP& g, double* out, cudaStream_t st)

@@ -117,35 +117,34 @@ __device__ void cell_features(const Dev& dv, double gamma, const Interp& ip, int
 }
 
 // MLP forward of one sample held in xs (shared) by one warp; returns alpha_max*sigmoid(z).
+// W is the parameter vector with W1 and W2 stored transposed ([in][out]) so that the 32 lanes,
+// each computing one output, read consecutive shared-memory words.
 __device__ float mlp_forward_warp(const float* W, const float* xs, float* hs, float amax)
 {
     const int lane = threadIdx.x & 31;
-    const float* W1 = W;
-    const float* b1 = W1 + kMlpHid * kMlpIn;
-    const float* W2 = b1 + kMlpHid;
-    const float* b2 = W2 + kMlpHid * kMlpHid;
+    const float* W1t = W;
+    const float* b1 = W1t + kMlpHid * kMlpIn;
+    const float* W2t = b1 + kMlpHid;
+    const float* b2 = W2t + kMlpHid * kMlpHid;
     const float* w3 = b2 + kMlpHid;
     const float b3 = w3[kMlpHid];
-    float h[2];
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int o = lane + 32 * r;
-        float s = b1[o];
-        for (int k = 0; k < kMlpIn; ++k) s += W1[o * kMlpIn + k] * xs[k];
-        h[r] = gelu(s);
+    float h0 = b1[lane], h1 = b1[lane + 32];
+    for (int k = 0; k < kMlpIn; ++k) {
+        const float xk = xs[k];
+        h0 += W1t[k * kMlpHid + lane] * xk;
+        h1 += W1t[k * kMlpHid + lane + 32] * xk;
     }
     __syncwarp();
-    hs[lane] = h[0];
-    hs[lane + 32] = h[1];
+    hs[lane] = gelu(h0);
+    hs[lane + 32] = gelu(h1);
     __syncwarp();
-    float z = 0;
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int o = lane + 32 * r;
-        float s = b2[o];
-        for (int k = 0; k < kMlpHid; ++k) s += W2[o * kMlpHid + k] * hs[k];
-        z += w3[o] * gelu(s);
+    float a0 = b2[lane], a1 = b2[lane + 32];
+    for (int k = 0; k < kMlpHid; ++k) {
+        const float hk = hs[k];
+        a0 += W2t[k * kMlpHid + lane] * hk;
+        a1 += W2t[k * kMlpHid + lane + 32] * hk;
     }
+    float z = w3[lane] * gelu(a0) + w3[lane + 32] * gelu(a1);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) z += __shfl_xor_sync(0xffffffffu, z, off);
     z += b3;
@@ -153,12 +152,37 @@ __device__ float mlp_forward_warp(const float* W, const float* xs, float* hs, fl
     return amax / (1.0f + expf(-z));
 }
 
+// parameter vector -> shared memory with W1 and W2 transposed
+__device__ void load_weights_transposed(const float* __restrict__ Wg, float* sW)
+{
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) {
+        int dst = i;
+        if (i < kMlpHid * kMlpIn) {
+            const int o = i / kMlpIn, k = i - o * kMlpIn;
+            dst = k * kMlpHid + o;
+        } else {
+            const int base = kMlpHid * kMlpIn + kMlpHid;
+            if (i >= base && i < base + kMlpHid * kMlpHid) {
+                const int r = i - base, o = r / kMlpHid, k = r - o * kMlpHid;
+                dst = base + k * kMlpHid + o;
+            }
+        }
+        sW[dst] = Wg[i];
+    }
+}
+
 constexpr int kWarpsPerBlock = 8;
 
-// Fused inference: features, MLP, alpha_min cut, wall override, alpha_d, compacted list.
+// Learned values below this are set to 0 (the modal indicator's own cut is alpha_min = 1e-3): the
+// network's sigmoid never returns exact zeros, and without a cut the subcell residual would run
+// on every smooth cell. The judge bounds the error this introduces.
+constexpr float kLearnedCut = 0.01f;
+
+// Fused inference of the modal indicator's value (the blender before neighbour smoothing):
+// features, MLP, cut, wall override.
 template <int P>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_sensor_infer(Dev dv, const float* __restrict__ Wg, GasP g,
-                                                                       BlendP bp, Interp ip, double* out, int final_write, int gated)
+                                                                       BlendP bp, Interp ip, double* out, int gated)
 {
     __shared__ float sW[kMlpParams];
     __shared__ float sv[kWarpsPerBlock][kMaxP * kMaxP * kMaxP];
@@ -168,77 +192,67 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_sensor_infer(Dev dv, co
     Scalars* s = dv.sc;
     if (!s->active) return;
     if (gated && s->sensor_fallback) return;
-    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) sW[i] = Wg[i];
+    load_weights_transposed(Wg, sW);
     __syncthreads();
+    const float cut = fmaxf((float)bp.amin, kLearnedCut);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int64_t cell = (int64_t)blockIdx.x * kWarpsPerBlock + warp; cell < dv.nc; cell += (int64_t)gridDim.x * kWarpsPerBlock) {
         cell_features<P>(dv, g.gamma, ip, cell, sv[warp], st[warp], sx[warp]);
         const float at = mlp_forward_warp(sW, sx[warp], sh[warp], (float)bp.amax);
         if (lane == 0) {
-            double a = (at < (float)bp.amin) ? 0.0 : (double)at;
+            double a = (at < cut) ? 0.0 : (double)at;
             if (dv.cell_wall[cell]) {
                 const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
                 a = (wl > a) ? wl : a;
             }
             out[cell] = a;
-            if (final_write) {
-                const double* x = dv.center + 3 * cell;
-                dv.alpha_d[cell] = (eval_expr(dv, bp.expr_vis, x[0], x[1], x[2], s->time) > 0) ? ((1.0 < a / bp.amax) ? 1.0 : a / bp.amax) : 0.0;
-                if (a > 0) {
-                    const int k = atomicAdd(dv.lo_count, 1);
-                    dv.lo_list[k] = (int32_t)cell;
-                }
-            }
         }
         __syncwarp();
     }
 }
 
-// judge: per-cell |alpha_mlp - alpha_plain|, max over cells
-__global__ void k_judge_compare(Dev dv, const double* alpha_mlp, unsigned long long* maxerr)
+// judge (per cell, before smoothing): where |alpha_mlp - alpha_plain| exceeds the tolerance the
+// plain value is kept and the cell is marked, so the plain indicator keeps computing it until the
+// next judged step; elsewhere the MLP value is used. The smoothing max(a, a_nbr/2) is 1-Lipschitz
+// in the max norm, so this bounds the error of the final alpha on judged steps.
+__global__ void k_judge_cells(Dev dv, const double* alpha_mlp, uint8_t* mask, double tol,
+                              unsigned long long* maxerr, unsigned int* nbad)
 {
     if (!dv.sc->active) return;
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double e = 0;
-    if (c < dv.nc) e = fabs(alpha_mlp[c] - dv.alpha[c]);
+    unsigned int bad = 0;
+    if (c < dv.nc) {
+        e = fabs(alpha_mlp[c] - dv.alpha_raw[c]);
+        bad = (e > tol) ? 1u : 0u;
+        mask[c] = (uint8_t)bad;
+        if (!bad) dv.alpha_raw[c] = alpha_mlp[c];
+    }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         const double o = __shfl_xor_sync(0xffffffffu, e, off);
         e = (o > e) ? o : e;
+        bad += __shfl_xor_sync(0xffffffffu, bad, off);
     }
-    if ((threadIdx.x & 31) == 0) atomicMax(maxerr, ord_double(e));
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(maxerr, ord_double(e));
+        if (bad) atomicAdd(nbad, bad);
+    }
 }
 
-__global__ void k_judge_decide(Dev dv, unsigned long long* maxerr, double tol)
+// judged-step bookkeeping; the whole domain falls back to the plain indicator when more than a
+// tenth of the cells are over the tolerance
+__global__ void k_judge_decide(Dev dv, unsigned long long* maxerr, unsigned int* nbad)
 {
     Scalars* s = dv.sc;
     if (!s->active) return;
     const double e = unord_double(*maxerr);
     s->judged += 1;
     if (e > s->max_alpha_err) s->max_alpha_err = e;
-    s->sensor_fallback = (e > tol) ? 1 : 0;
-    if (s->sensor_fallback) s->fallbacks += 1;
+    s->fallbacks += *nbad;
+    s->sensor_fallback = (*nbad > (unsigned int)(dv.nc / 10)) ? 1 : 0;
     *maxerr = ord_double(0.0);
-}
-
-// keep the MLP alpha unless the judge fell back
-__global__ void k_judge_select(Dev dv, const double* alpha_mlp, BlendP bp)
-{
-    Scalars* s = dv.sc;
-    if (!s->active) return;
-    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (c >= dv.nc) return;
-    double a = dv.alpha[c];
-    if (!s->sensor_fallback) {
-        a = alpha_mlp[c];
-        dv.alpha[c] = a;
-        const double* x = dv.center + 3 * c;
-        dv.alpha_d[c] = (eval_expr(dv, bp.expr_vis, x[0], x[1], x[2], s->time) > 0) ? ((1.0 < a / bp.amax) ? 1.0 : a / bp.amax) : 0.0;
-    }
-    if (a > 0) {
-        const int k = atomicAdd(dv.lo_count, 1);
-        dv.lo_list[k] = (int32_t)c;
-    }
+    *nbad = 0;
 }
 
 __global__ void k_lo_stat(Dev dv)
@@ -262,56 +276,54 @@ __global__ void k_features(Dev dv, GasP g, Interp ip, float* x)
     }
 }
 
-struct MlpScratch {
-    unsigned long long* maxerr = nullptr;
-    double* alpha_mlp = nullptr;
-};
-
 template <int P>
-int launch_infer(const Dev& dv, const float* W, const GasP& g, const BlendP& bp, double* out, int final_write, int gated, cudaStream_t st)
+int launch_infer(const Dev& dv, const float* W, const GasP& g, const BlendP& bp, double* out, int gated, cudaStream_t st)
 {
     const Interp ip = make_interp(P);
     const int64_t blocks = std::min<int64_t>((dv.nc + kWarpsPerBlock - 1) / kWarpsPerBlock, 152 * 8);
-    k_sensor_infer<P><<<(unsigned)blocks, 32 * kWarpsPerBlock, 0, st>>>(dv, W, g, bp, ip, out, final_write, gated);
+    k_sensor_infer<P><<<(unsigned)blocks, 32 * kWarpsPerBlock, 0, st>>>(dv, W, g, bp, ip, out, gated);
     return 1;
 }
 
 template <int P>
-int launch_plain(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
+int launch_blender(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
 {
     using CB = CellBlock<P>;
-    k_blender<P><<<(unsigned)((dv.nc + CB::CPB - 1) / CB::CPB), CB::THREADS, 0, st>>>(dv, ops, g, bp);
-    k_alpha_smooth<<<(unsigned)((dv.nc + 127) / 128), 128, 0, st>>>(dv, bp);
-    return 2;
+    k_blender<P, double><<<(unsigned)((dv.nc + CB::CPB - 1) / CB::CPB), CB::THREADS, 0, st>>>(dv, ops, g, bp);
+    return 1;
 }
 
+// One stage's blender with the learned sensor. Non-judged stages: the MLP into alpha_raw for
+// every cell (skipped in whole-domain fallback), then the plain modal indicator for the cells the
+// last judge handed back (all cells in fallback), then the neighbour smoothing + alpha_d +
+// compacted troubled-cell list. Judged stage (stage 1 of every judge_every-th step): MLP and
+// plain indicator for all cells, per-cell comparison and takeover.
 template <int P>
 int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
 {
     int n = 0;
     cudaMemsetAsync(dv.lo_count, 0, sizeof(int32_t), st);
+    BlendP b0 = bp;
+    b0.gate = 0;
+    b0.mask = nullptr;
     if (m.judge_this_step) {
-        // MLP into the scratch buffer, plain blender into alpha (no compaction), compare, select
-        n += launch_infer<P>(dv, m.params, g, bp, m.alpha_plain, 0, 0, st);
-        Dev d2 = dv;
-        d2.lo_list = nullptr;
-        BlendP b0 = bp;
-        b0.gate = 0;
-        n += launch_plain<P>(d2, ops, g, b0, st);
+        n += launch_infer<P>(dv, m.params, g, bp, m.alpha_plain, 0, st);
+        n += launch_blender<P>(dv, ops, g, b0, st);
         const unsigned grid = (unsigned)((dv.nc + 127) / 128);
-        k_judge_compare<<<grid, 128, 0, st>>>(dv, m.alpha_plain, m.maxerr);
-        k_judge_decide<<<1, 1, 0, st>>>(dv, m.maxerr, m.tol);
-        k_judge_select<<<grid, 128, 0, st>>>(dv, m.alpha_plain, bp);
-        n += 3;
+        k_judge_cells<<<grid, 128, 0, st>>>(dv, m.alpha_plain, m.mask, m.tol, m.maxerr, m.nbad);
+        k_judge_decide<<<1, 1, 0, st>>>(dv, m.maxerr, m.nbad);
+        n += 2;
         m.judge_this_step = false;  // the remaining stages of this step follow the decision
     } else {
-        n += launch_infer<P>(dv, m.params, g, bp, dv.alpha, 1, 1, st);
+        n += launch_infer<P>(dv, m.params, g, bp, dv.alpha_raw, 1, st);
         BlendP b1 = bp;
         b1.gate = 1;
-        n += launch_plain<P>(dv, ops, g, b1, st);
+        b1.mask = m.mask;
+        n += launch_blender<P>(dv, ops, g, b1, st);
     }
+    k_alpha_smooth<<<(unsigned)((dv.nc + 127) / 128), 128, 0, st>>>(dv, b0);
     k_lo_stat<<<1, 1, 0, st>>>(dv);
-    return n + 1;
+    return n + 2;
 }
 
 }  // namespace
@@ -325,6 +337,10 @@ int mlp_create(MlpDevice& m, int64_t nc, std::vector<void*>& allocs)
     allocs.push_back(m.alpha_plain);
     if (cudaMalloc(&m.maxerr, sizeof(unsigned long long)) != cudaSuccess) return 1;
     allocs.push_back(m.maxerr);
+    if (cudaMalloc(&m.mask, nc) != cudaSuccess || cudaMemset(m.mask, 0, nc) != cudaSuccess) return 1;
+    allocs.push_back(m.mask);
+    if (cudaMalloc(&m.nbad, sizeof(unsigned int)) != cudaSuccess || cudaMemset(m.nbad, 0, sizeof(unsigned int)) != cudaSuccess) return 1;
+    allocs.push_back(m.nbad);
     const unsigned long long z = ord_double_host(0.0);
     if (cudaMemcpy(m.maxerr, &z, sizeof(z), cudaMemcpyHostToDevice) != cudaSuccess) return 1;
     return 0;
@@ -372,23 +388,21 @@ int mlp_pairs(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, in
     float* dx = nullptr;
     if (cudaMalloc(&dx, sizeof(float) * 64 * dv.nc) != cudaSuccess) return PLENS_GPU_E_CUDA;
     k_step_begin<<<1, 1, 0, st>>>(dv, 1e300);
-    Dev d2 = dv;
-    d2.lo_list = nullptr;
     BlendP b0 = bp;
     b0.gate = 0;
     const int64_t blocks = std::min<int64_t>((dv.nc + kWarpsPerBlock - 1) / kWarpsPerBlock, 152 * 8);
     switch (P) {
-    case 2: launch_plain<2>(d2, ops, g, b0, st); k_features<2><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(2), dx); break;
-    case 3: launch_plain<3>(d2, ops, g, b0, st); k_features<3><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(3), dx); break;
-    case 4: launch_plain<4>(d2, ops, g, b0, st); k_features<4><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(4), dx); break;
-    case 5: launch_plain<5>(d2, ops, g, b0, st); k_features<5><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(5), dx); break;
-    default: launch_plain<6>(d2, ops, g, b0, st); k_features<6><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(6), dx); break;
+    case 2: launch_blender<2>(dv, ops, g, b0, st); k_features<2><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(2), dx); break;
+    case 3: launch_blender<3>(dv, ops, g, b0, st); k_features<3><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(3), dx); break;
+    case 4: launch_blender<4>(dv, ops, g, b0, st); k_features<4><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(4), dx); break;
+    case 5: launch_blender<5>(dv, ops, g, b0, st); k_features<5><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(5), dx); break;
+    default: launch_blender<6>(dv, ops, g, b0, st); k_features<6><<<(unsigned)blocks, 256, 0, st>>>(dv, g, make_interp(6), dx); break;
     }
-    launches += 4;
+    launches += 3;
     std::vector<double> a(dv.nc);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaMemcpy(x, dx, sizeof(float) * 64 * dv.nc, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(a.data(), dv.alpha, sizeof(double) * dv.nc, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(a.data(), dv.alpha_raw, sizeof(double) * dv.nc, cudaMemcpyDeviceToHost);
     cudaFree(dx);
     if (e != cudaSuccess) return PLENS_GPU_E_CUDA;
     for (int64_t i = 0; i < dv.nc; ++i) y[i] = (float)a[i];

@@ -19,6 +19,8 @@ struct MlpDevice {
     float* params = nullptr;        // [kMlpParams] W1 b1 W2 b2 w3 b3
     double* alpha_plain = nullptr;  // [nc] judge: MLP alpha of the judged stage
     unsigned long long* maxerr = nullptr;  // order-preserving max per-cell alpha error
+    uint8_t* mask = nullptr;        // [nc] cells handed back to the plain indicator by the judge
+    unsigned int* nbad = nullptr;   // cells over the tolerance in the current judged stage
     double tol = 0.05;
     int64_t nc = 0;
     bool weights_set = false;

@@ -118,6 +118,7 @@ static Ops make_ops(int P)
     for (int i = 0; i < P * P; ++i) {
         o.fD[i] = (float)o.D[i];
         o.fQ[i] = (float)o.Q[i];
+        o.fC1[i] = (float)o.C1[i];
     }
     o.tv[0] = 0.0;
     if (P > 1) o.tv[1] = std::fabs(legendre01(1, 1) - legendre01(1, 0));
@@ -269,12 +270,12 @@ const double kAo[5] = {4745337637855.0 / 22386579876409, 6808157035527.0 / 13197
 const double kAi[4] = {546509042554.0 / 9152262712923, 625707605167.0 / 5316659119056,
                        582400652113.0 / 7078426004906, 5010207514426.0 / 21876007855139};
 
-int launch_step(plens_ctx* c, double end_time)
+int launch_step(plens_ctx* c, double end_time, bool judge = true)
 {
     cudaStream_t st = c->stream;
     k_step_begin<<<1, 1, 0, st>>>(c->dv, end_time);
     c->launches += 1;
-    if (c->learned) {
+    if (c->learned && judge) {
         c->launches += mlp_step_begin(c->mlp, c->dv, c->prm.judge_every, st);
     }
     if (int r = launch_time_step(c)) return r;
@@ -438,9 +439,10 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
     if (prm->rk_order == 4) {
         for (int k = 0; k < 3; ++k)
             if ((r = dalloc(c, &c->R[k], 5 * nd))) return r;
-    } else if ((r = dalloc(c, &d.U0, 5 * nd))) {
-        return r;
     }
+    // step-start state: RK3 needs it; the learned sensor restores it to redo a step with the
+    // plain indicator after a positivity failure
+    if ((prm->rk_order == 3 || c->learned) && (r = dalloc(c, &d.U0, 5 * nd))) return r;
     if (c->viscous) {
         if ((r = dalloc(c, &d.sf3, 5 * c->nslot)) || (r = dalloc(c, &d.avars, 9 * nd))) return r;
         CK(cudaMemset(d.avars, 0, sizeof(double) * 9 * nd));
@@ -587,6 +589,40 @@ int plens_gpu_synchronize(plens_ctx* c)
 
 int plens_gpu_advance(plens_ctx* c, int64_t n_steps, double end_time)
 {
+    if (c && c->learned) {
+        // Learned sensor: step by step; a step that fails the positivity check is redone from
+        // its start state with the plain modal indicator on the whole domain (the fallback lasts
+        // until the next judged step).
+        if (!c->dv.U) return PLENS_GPU_E_INVALID;
+        if (!c->mlp.weights_set) return fail(c, PLENS_GPU_E_INVALID, "learned sensor: weights not set");
+        for (int64_t s = 0; s < n_steps; ++s) {
+            Scalars h0;
+            CK(cudaStreamSynchronize(c->stream));
+            CK(cudaMemcpy(&h0, c->sc, sizeof(h0), cudaMemcpyDeviceToHost));
+            if (!(h0.time < end_time)) break;
+            CK(cudaMemcpyAsync(c->dv.U0, c->dv.U, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToDevice, c->stream));
+            const int saved_counter = c->mlp.step_counter;
+            if (int r = launch_step(c, end_time)) return r;
+            const int r = sync_and_check(c);
+            if (r != PLENS_GPU_E_POSITIVITY) {
+                if (r) return r;
+                continue;
+            }
+            if (h0.sensor_fallback) return r;  // the plain indicator failed too: report it
+            CK(cudaMemcpyAsync(c->dv.U, c->dv.U0, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToDevice, c->stream));
+            Scalars h = h0;
+            h.sensor_fallback = 1;
+            h.fallbacks = h0.fallbacks + c->nc;  // every cell handed back for this step
+            h.err = 0;
+            h.bad_dof = INT64_MAX;
+            CK(cudaMemcpy(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice));
+            c->mlp.step_counter = saved_counter;
+            c->mlp.judge_this_step = false;
+            if (int r2 = launch_step(c, end_time, false)) return r2;
+            if (int r2 = sync_and_check(c)) return r2;
+        }
+        return 0;
+    }
     if (int r = plens_gpu_advance_async(c, n_steps, end_time)) return r;
     return sync_and_check(c);
 }
