@@ -149,13 +149,27 @@ def _sensor_weights():
     return None
 
 
-def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_index: int, weights=None):
+def _spec(workload: str, precision: str, sensor: str):
+    from plens_gb300 import configs
+    if workload == "dmr":
+        return configs.dmr(precision=precision, sensor=sensor, end_time=1e9)
+    if workload == "sod":
+        return configs.sod(precision=precision, sensor=sensor, end_time=1e9)
+    if workload == "cylinder":
+        return configs.cylinder(precision=precision, sensor=sensor)
+    if workload == "shock_vortex":
+        return configs.shock_vortex(precision=precision, sensor=sensor)
+    raise ValueError(workload)
+
+
+def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_index: int, weights=None,
+                 workload: str = "dmr"):
     import torch
 
     from plens_gb300 import configs
     from plens_gb300.api import GpuSolver
 
-    case = configs.make_case(configs.dmr(precision=precision, sensor=sensor, end_time=1e9))
+    case = configs.make_case(_spec(workload, precision, sensor))
     U0 = case.initial_state()
     g = GpuSolver(case)
     if sensor == "learned":
@@ -245,6 +259,68 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_workload_report(args):
+    """One JSON line per configuration: DOF-stage/s of the FP64 plain form, the FP32 form with
+    the modal and with the learned sensor, the oracle on the host cores, and the relative L1
+    errors of the FP32 forms against the FP64 form (itself equal to the oracle to 1e-10, see the
+    parity tests) after --accuracy-steps steps from the initial condition."""
+    import torch
+
+    from plens_gb300 import configs
+    from plens_gb300.api import GpuSolver, PlensError
+
+    torch.cuda.set_device(0)
+    weights = _sensor_weights()
+    forms = [("fp64_plain", "fp64", "modal"), ("fp32_modal", "mixed", "modal")]
+    if weights is not None:
+        forms.append(("fp32_learned", "mixed", "learned"))
+    out = {"workload": args.workload}
+    states = {}
+    for name, prec, sensor in forms:
+        r = measure_form(prec, sensor, args.steps, args.warmup, 0, weights, workload=args.workload)
+        nd = r["case"].n_dofs
+        out[name] = {"dof_stage_per_s": nd * 5 * args.steps / (r["ms"] / 1e3), "ms_per_step": r["ms"] / args.steps,
+                     "volume_kernel_ms": r["vol_ms"] / max(r["vol_n"], 1), "n_dofs": nd}
+        if r["stats"]:
+            out[name]["sensor_stats"] = r["stats"]
+        # accuracy run from the initial condition
+        case = configs.make_case(_spec(args.workload, prec, sensor))
+        g = GpuSolver(case)
+        if sensor == "learned":
+            g.set_sensor_weights(weights)
+        g.set_state(case.initial_state(), case.start_time)
+        t0 = time.perf_counter()
+        try:
+            g.advance(args.accuracy_steps)
+            states[name] = g.get_state()
+            out[name]["accuracy_run"] = {"steps": args.accuracy_steps, "seconds": time.perf_counter() - t0,
+                                         "t_end": g.get_time()[0]}
+        except PlensError as e:
+            out[name]["accuracy_run"] = {"error": str(e)}
+        if sensor == "learned":
+            st = g.sensor_stats()
+            st["fallback_rate"] = st["fallbacks"] / max(st["judged"] * case.n_cells, 1)
+            out[name]["accuracy_run"]["sensor_stats"] = st
+        g.close()
+    for name in ("fp32_modal", "fp32_learned"):
+        if name in states and "fp64_plain" in states:
+            out[name]["rel_l1_vs_fp64"] = dict(zip(("rho", "momentum", "rhoE"), _rel_l1(states[name], states["fp64_plain"])))
+    if not args.no_cpu_baseline:
+        from oracle.pyoracle import Oracle, max_threads
+        case = configs.make_case(_spec(args.workload, "fp64", "modal"))
+        o = Oracle(case)
+        o.set_state(case.initial_state(), case.start_time)
+        t0 = time.perf_counter()
+        o.advance(1)
+        t1 = time.perf_counter() - t0
+        n = max(1, min(args.steps, int(20.0 / max(t1, 1e-3))))
+        t0 = time.perf_counter()
+        o.advance(n)
+        dt = time.perf_counter() - t0
+        out["cpu_oracle"] = {"dof_stage_per_s": case.n_dofs * 5 * n / dt, "cores": max_threads(), "steps": n}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -252,10 +328,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="", choices=["", "sod", "dmr", "cylinder", "shock_vortex"],
+                    help="per-configuration report (throughput of every form, accuracy after --accuracy-steps) "
+                         "instead of the benchmark line")
+    ap.add_argument("--accuracy-steps", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload:
+        run_workload_report(args)
         return
 
     import torch

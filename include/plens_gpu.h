@@ -236,6 +236,11 @@ int plens_gpu_get_cell_scalars(plens_ctx* ctx, double* alpha, double* alpha_d, d
 int plens_gpu_get_avars(plens_ctx* ctx, double* avars);
 /* First dof that failed the positivity check of the last failing call (-1 if none). */
 int plens_gpu_first_bad_dof(const plens_ctx* ctx, int64_t* dof);
+/* Self-test of the mixed form's integer-pipe FP64 <-> FP32 conversions (no reference
+ * counterpart; test hook): n seeded samples (raw encodings, values in and around the float
+ * range, rounding ties) converted both by them and by the hardware conversions on the device;
+ * *mismatches receives the number of results whose encodings differ (NaN compared as NaN). */
+int plens_gpu_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
 
 /* ----------------------------------------------------- learned troubled-cell sensor
  * New component (no counterpart in the reference): an MLP (64 -> 64 -> 64 -> 1, GELU,

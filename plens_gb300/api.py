@@ -160,6 +160,7 @@ def gpu_lib() -> C.CDLL:
         L.plens_gpu_mlp_train.argtypes = [vp, vp, i64, vp, i32, i32, C.c_float, C.c_float, C.c_uint64, vp]
         L.plens_gpu_mlp_loss_grad.argtypes = [vp, vp, i64, vp, C.c_float, C.POINTER(C.c_float), vp]
         L.plens_gpu_mlp_infer.argtypes = [vp, i64, vp, C.c_float, vp]
+        L.plens_gpu_selftest_conversions.argtypes = [i64, C.c_uint64, C.POINTER(i64)]
         L.plens_gpu_set_kernel_timing.argtypes = [vp, C.c_int]
         L.plens_gpu_kernel_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(i64)]
         _gpu = L
@@ -415,3 +416,14 @@ def mlp_infer(x: np.ndarray, params: np.ndarray, alpha_max=0.5) -> np.ndarray:
     if rc != 0:
         raise PlensError(f"plens_gpu_mlp_infer failed with status {rc}")
     return out
+
+
+def selftest_conversions(n: int = 1 << 24, seed: int = 1) -> int:
+    """Mismatches between the mixed form's integer-pipe FP64 <-> FP32 conversions and the
+    hardware conversions over n seeded samples (0 when they agree)."""
+    L = gpu_lib()
+    bad = C.c_int64(0)
+    rc = L.plens_gpu_selftest_conversions(n, seed, C.byref(bad))
+    if rc != 0:
+        raise PlensError(f"plens_gpu_selftest_conversions failed with status {rc}")
+    return bad.value

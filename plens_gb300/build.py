@@ -119,7 +119,9 @@ def build_gpu() -> Path:
             # every product and sum as written, like the reference's x86-64 build (which has no
             # FMA), and matches the oracle to ~1e-15 even in stretched curved cells where the
             # residual cancels by four orders of magnitude. The mixed form keeps FMA.
-            extra = ["--fmad=false"] if prec == "fp64" else []
+            # The mixed form's FP32 divisions and square roots use the approximate instructions
+            # (2 ulp); the FP64 arithmetic is unaffected by these flags.
+            extra = ["--fmad=false"] if prec == "fp64" else ["-prec-div=false", "-prec-sqrt=false"]
             jobs.append([nvcc, *flags, *extra, f"-DPLENS_P={P}", f"-DPLENS_REAL={real}",
                          f"-DPLENS_TABLE=table_{prec}_{P}", "-c", str(src), "-o", str(obj)])
     if jobs:

@@ -24,6 +24,7 @@ struct Ops {
     float fD[kMaxP * kMaxP];
     float fQ[kMaxP * kMaxP];
     float fC1[kMaxP * kMaxP];
+    float ftv[kMaxP];
 };
 
 template <class T> __device__ __forceinline__ T opC1(const Ops& o, int i)
@@ -81,6 +82,8 @@ struct Scalars {
     double max_alpha_err;
     int sensor_fallback;       // 1: this step uses the plain blender
     int pad;
+    double time0;              // clock and step count at the start of the last step (learned
+    long long n_steps0;        // sensor: a step that fails the positivity check is redone)
 };
 
 struct Dev {
@@ -91,6 +94,10 @@ struct Dev {
     const uint8_t *cell_wall;
     const int32_t *ft_cell, *ft_face, *ft_nbr_cell, *ft_nbr_face, *ft_bc, *ft_nbr_fdof;
     const double *ft_normal, *ft_xyz;
+    // per face dof of a face task: the owner-side dof, the neighbour-side dof (interior faces
+    // and periodic partners; -1 otherwise), the owner's face slot and the neighbour's face slot
+    // (interior faces; -1 otherwise)
+    const int32_t *fd_own, *fd_nbr, *fs_own, *fs_nbr;
     const plens_bc_desc* bcs;
     int n_bc;
     const plens_expr_insn* expr_code;
@@ -99,6 +106,7 @@ struct Dev {
     // state
     double* U;
     double* U0;
+    float* Uf;  // mixed form: FP32 image of U (round to nearest), kept current by the update
     double *alpha_raw, *alpha, *alpha_d;
     double* tvstat;    // [3][nc] filter statistics of the modal indicator
     double *sf, *sf3;  // surface terms [5][nslot]
@@ -112,6 +120,110 @@ __device__ __forceinline__ double eval_expr(const Dev& dv, int idx, double x, do
 {
     if (idx < 0 || idx >= dv.n_expr) return 0.0 / 0.0;
     return plens::expr_eval(dv.expr_code + dv.expr_off[idx], dv.expr_len[idx], x, y, z, t);
+}
+
+// FP64 <-> FP32 conversions by integer arithmetic on the IEEE-754 encodings, with the results of
+// the hardware conversions (round to nearest, ties to even). GB300 runs FP64 instructions,
+// conversions included, at a small fraction of the FP32 and integer rates, and the mixed form
+// converts every FP64 state, metric and register value it reads; these keep that work on the
+// integer pipes. Zero and every value whose result is a normal float take the integer path;
+// subnormal results, infinities and NaNs (never met on a valid state) use the hardware
+// conversion.
+__device__ __forceinline__ float f64_to_f32(double x)
+{
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    const unsigned int hi = static_cast<unsigned int>(b >> 32);
+    const unsigned int ah = hi & 0x7fffffffu;
+    const unsigned int sgn = hi ^ ah;
+    // biased FP64 exponent in [897, 1150]: the result is a normal float (or rounds up to inf)
+    if (ah - 0x38100000u < 0x0fe00000u) {
+        unsigned long long a = b & 0x7fffffffffffffffULL;
+        a += 0x0fffffffULL + ((a >> 29) & 1ULL);  // round the 29 dropped bits to nearest even
+        return __uint_as_float(sgn | static_cast<unsigned int>((a >> 29) - (896ULL << 23)));
+    }
+    if (ah < 0x36900000u) return __uint_as_float(sgn);  // |x| < 2^-150 (zero included): rounds to 0
+    return __double2float_rn(x);
+}
+
+__device__ __forceinline__ double f32_to_f64(float x)
+{
+    const unsigned int u = __float_as_uint(x);
+    const unsigned int au = u & 0x7fffffffu;
+    const unsigned int sgn = u ^ au;
+    if (au - 0x00800000u < 0x7f000000u)  // normal
+        return __hiloint2double(static_cast<int>(sgn | ((au >> 3) + (896u << 20))), static_cast<int>(au << 29));
+    if (au == 0) return __hiloint2double(static_cast<int>(sgn), 0);
+    return static_cast<double>(x);
+}
+
+// a stored FP64 value in the arithmetic type T, and back
+template <class T> __device__ __forceinline__ T to_real(double x)
+{
+    if constexpr (sizeof(T) == 8) return x; else return f64_to_f32(x);
+}
+template <class T> __device__ __forceinline__ double to_f64(T x)
+{
+    if constexpr (sizeof(T) == 8) return x; else return f32_to_f64(x);
+}
+
+// One node's state in the arithmetic type: the FP64 state (plain form) or its FP32 image (mixed).
+template <class T>
+__device__ __forceinline__ void load_state(const Dev& dv, int64_t dof, T c[5])
+{
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        if constexpr (sizeof(T) == 8) c[v] = dv.U[v * dv.nd + dof];
+        else c[v] = dv.Uf[v * dv.nd + dof];
+    }
+}
+
+// The face-value and auxiliary-variable buffers are intermediates of one RHS: the mixed form
+// stores them in FP32 inside the FP64-sized allocations.
+template <class T> __device__ __forceinline__ T* as_real(double* p) { return reinterpret_cast<T*>(p); }
+
+// assert_positivity (dgsem/plens.cc:2531-2546, navier_stokes.cc:326-337): rho > 0 and e > 0,
+// decided in FP64 with the reference's expressions.
+__device__ __forceinline__ bool positive_state_f64(const double c[5])
+{
+    if (!(c[0] > 0)) return false;
+    double ske = c[1] * c[1];
+    ske += c[2] * c[2];
+    ske += c[3] * c[3];
+    const double ri = 1.0 / c[0];
+    ske *= 0.5 * ri;
+    return (c[4] - ske) * ri > 0;
+}
+
+// The same decision for the mixed form: an FP32 screen on 2 rho (rho E) - |rho u|^2, whose
+// rounding error is below 1e-6 of the sum of the magnitudes of its terms, accepts the state
+// when it clears that sum by 1e-5; any other state is decided by the FP64 test above.
+__device__ __forceinline__ bool positive_screen_f32(const float cf[5])
+{
+    const float a = 2.0f * cf[0] * cf[4];
+    float m = cf[1] * cf[1];
+    m += cf[2] * cf[2];
+    m += cf[3] * cf[3];
+    return cf[0] > 0.0f && cf[4] > 0.0f && a - m > 1e-5f * (a + m);
+}
+__device__ __forceinline__ bool positive_state_screened(const double c[5], const float cf[5])
+{
+    return positive_screen_f32(cf) || positive_state_f64(c);
+}
+// the screen on the FP32 image; the FP64 state is read only when the screen does not decide
+__device__ __forceinline__ bool positive_dof_screened(const Dev& dv, int64_t dof, const float cf[5])
+{
+    if (positive_screen_f32(cf)) return true;
+    double c[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) c[v] = dv.U[v * dv.nd + dof];
+    return positive_state_f64(c);
+}
+
+// x > 0 for a stored FP64 value: compared in FP64 by the plain form, on the encoding by the
+// mixed form (sign clear and not zero)
+template <class T> __device__ __forceinline__ bool stored_gt0(double x)
+{
+    if constexpr (sizeof(T) == 8) return x > 0; else return __double_as_longlong(x) > 0;
 }
 
 __device__ __forceinline__ unsigned long long ord_double(double x)

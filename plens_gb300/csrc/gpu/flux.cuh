@@ -114,6 +114,57 @@ __device__ __forceinline__ void chandrashekhar_vol(const T q1[7], const T q2[7],
     f[4] = rho_ln * vn * H;
 }
 
+// ------------------------------------------------- mixed form: FP32 flux differencing kernels
+// Logarithmic mean of a, b with la = ln a, lb = ln b precomputed per node: the reference's series
+// for u = ((a-b)/(a+b))^2 < 1e-2 (navier_stokes.h:494-501), else (a-b)/(ln a - ln b), which is
+// the reference's non-series value 0.5(a+b)/(0.5 ln(a/b)/f) written without the per-pair logarithm
+// and without its two divisions. Both branches are formed and one is selected (no divergence).
+__device__ __forceinline__ float log_mean_f32(float a, float b, float la, float lb)
+{
+    const float s = a + b, d = a - b;
+    const float f = __fdividef(d, s), u = f * f;
+    const float F = 1.0f + u * (1.0f / 3 + u * (0.2f + u * (1.0f / 7)));
+    const bool series = u < 1e-2f;
+    return __fdividef(series ? 0.5f * s : d, series ? F : la - lb);
+}
+
+// Chandrashekhar two-point flux (navier_stokes.cc:1510-1542) along an unnormalised direction n:
+// the flux is linear in the direction, so F(n) = |n| F(n/|n|) and the volume term
+// 2 D_im |nbar| F(nbar/|nbar|) with nbar = (Ja_i + Ja_m)/2 equals D_im F(Ja_i + Ja_m); no
+// normalisation is needed. q = {rho, 1/rho, v0, v1, v2, p, beta, ln rho, ln beta, |v|^2};
+// hg = 1/(2(gamma-1)).
+__device__ __forceinline__ void chandrashekhar_pair_f32(const float qi[10], const float qm[10], const float n[3],
+                                                        float hg, float f[5])
+{
+    const float rho_ln = log_mean_f32(qi[0], qm[0], qi[7], qm[7]);
+    const float beta_ln = log_mean_f32(qi[6], qm[6], qi[8], qm[8]);
+    const float p_hat = __fdividef(0.5f * (qi[0] + qm[0]), qi[6] + qm[6]);
+    const float va0 = 0.5f * (qi[2] + qm[2]), va1 = 0.5f * (qi[3] + qm[3]), va2 = 0.5f * (qi[4] + qm[4]);
+    // sum_d (va_d^2 - vsq_d / 2) with vsq_d = (v_i,d^2 + v_m,d^2) / 2
+    const float H = __fdividef(hg, beta_ln) + __fdividef(p_hat, rho_ln) + (va0 * va0 + va1 * va1 + va2 * va2) -
+                    0.25f * (qi[9] + qm[9]);
+    const float vn = va0 * n[0] + va1 * n[1] + va2 * n[2];
+    const float rv = rho_ln * vn;
+    f[0] = rv;
+    f[1] = rv * va0 + p_hat * n[0];
+    f[2] = rv * va1 + p_hat * n[1];
+    f[3] = rv * va2 + p_hat * n[2];
+    f[4] = rv * H;
+}
+
+// The same flux for two identical states: the physical flux along n, with the enthalpy
+// gamma/(gamma-1) p/rho + |v|^2/2 (the pair formula's value for q_i = q_m). gf = gamma/(gamma-1).
+__device__ __forceinline__ void chandrashekhar_same_f32(const float q[10], const float n[3], float gf, float f[5])
+{
+    const float vn = q[2] * n[0] + q[3] * n[1] + q[4] * n[2];
+    const float rv = q[0] * vn;
+    f[0] = rv;
+    f[1] = rv * q[2] + q[5] * n[0];
+    f[2] = rv * q[3] + q[5] * n[1];
+    f[3] = rv * q[4] + q[5] * n[2];
+    f[4] = rv * (gf * q[5] * q[1] + 0.5f * q[9]);
+}
+
 // The same flux for two identical states (the m = i term of the volume sum). log_avg(x, x)
 // returns x exactly (x/x = 1, f = 0, series branch, 0.5*(x+x)/1 = x), so skipping the two
 // logarithmic means is bitwise identical to chandrashekhar_vol(q, q, ...).

@@ -16,6 +16,7 @@ struct StageArgs {
     const double* R0;
     const double* R1;
     double c0, c1, c2;
+    float fc0, fc1, fc2;  // the same coefficients for the mixed form's FP32 register combination
     int lo_from_list;  // 1: the subcell residual runs only on cells of the compacted list
 };
 
@@ -41,6 +42,31 @@ static __global__ void k_dt_finalize(Dev dv)
     s->dt = (dt > (s->end_time - s->time)) ? s->end_time - s->time : dt;
 }
 
+// mixed form: the FP32 image of the state after the host or a restore changed U
+static __global__ void k_state_image(Dev dv)
+{
+    const int64_t n = 5 * dv.nd;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dv.Uf[i] = f64_to_f32(dv.U[i]);
+}
+
+// step-start snapshot of the state and the clock (learned sensor): U0 = U
+static __global__ void k_snapshot(Dev dv)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const int64_t n2 = 5 * dv.nd / 2;  // nd = cells * P^3; 5 * nd may be odd
+    const double2* src = reinterpret_cast<const double2*>(dv.U);
+    double2* dst = reinterpret_cast<double2*>(dv.U0);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (5 * dv.nd > 2 * n2) dv.U0[5 * dv.nd - 1] = dv.U[5 * dv.nd - 1];
+        s->time0 = s->time;
+        s->n_steps0 = s->n_steps;
+    }
+}
+
 static __global__ void k_clock(Dev dv)
 {
     Scalars* s = dv.sc;
@@ -50,57 +76,75 @@ static __global__ void k_clock(Dev dv)
 }
 
 // --------------------------------------------------------------------------- time step
-// PLENS::calc_time_step (dgsem/plens.cc:3810-3912): per-dof stable step, min over dofs.
-template <int P>
+// PLENS::calc_time_step (dgsem/plens.cc:3810-3912): per-dof stable step, min over dofs. The
+// plain form evaluates it in FP64 with the reference's expressions; the mixed form in FP32 (the
+// step size is a CFL bound, not an accumulated quantity), from FP64 state and metrics converted on
+// the integer pipes.
+template <int P, class T>
 __global__ void __launch_bounds__(256) k_time_step(Dev dv, GasP g, double N15, int N)
 {
     Scalars* s = dv.sc;
     if (!s->active) return;
     constexpr int P3 = P * P * P;
-    __shared__ double s_red[8];
-    double local = 1e6;
+    __shared__ T s_red[8];
+    T local = T(1e6);
     const int64_t dof = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (dof < dv.nd) {
         const int64_t c = dof / P3;
-        double cs[5];
+        const T gm = to_real<T>(g.gamma);
+        T cs[5];
+        load_state<T>(dv, dof, cs);
+        T a, vel[3];
+        if constexpr (sizeof(T) == 8) {
+            a = sqrt(gm * get_p(cs, gm) / cs[0]);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) cs[v] = dv.U[v * dv.nd + dof];
-        const double a = sqrt(g.gamma * get_p(cs, g.gamma) / cs[0]);
-        const double vel[3] = {cs[1] / cs[0], cs[2] / cs[0], cs[3] / cs[0]};
-        double adv[3];
+            for (int d = 0; d < 3; ++d) vel[d] = cs[1 + d] / cs[0];
+        } else {
+            a = sqrtf(__fdividef(gm * get_p(cs, gm), cs[0]));
+            const T ri = __fdividef(1.0f, cs[0]);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) vel[d] = cs[1 + d] * ri;
+        }
+        T adv[3];
 #pragma unroll
         for (int row = 0; row < 3; ++row) {
-            double acc = 0.0;
+            T acc = T(0);
 #pragma unroll
-            for (int col = 0; col < 3; ++col) acc += dv.Jinv[(col * 3 + row) * dv.nd + dof] * vel[col];
+            for (int col = 0; col < 3; ++col) acc += to_real<T>(dv.Jinv[(col * 3 + row) * dv.nd + dof]) * vel[col];
             adv[row] = acc;
         }
-        double madv = adv[0];
+        T madv = adv[0];
         if (adv[1] > madv) madv = adv[1];
         if (adv[2] > madv) madv = adv[2];
-        double mu = 0.0;
+        T mu = T(0);
         if (!g.inviscid) {
-            const double T = get_e(cs) / (g.R / (g.gamma - 1));
-            mu = g.const_visc ? g.mu0 : g.mu0 * pow(T / g.T0, 1.5) * (g.T0 + g.S) / (T + g.S);
+            if constexpr (sizeof(T) == 8) {
+                const double Tk = get_e(cs) / (g.R / (g.gamma - 1));
+                mu = g.const_visc ? g.mu0 : g.mu0 * pow(Tk / g.T0, 1.5) * (g.T0 + g.S) / (Tk + g.S);
+            } else {
+                const float Tk = __fdividef(get_e(cs) * to_real<T>(g.gamma - 1), to_real<T>(g.R));
+                const float T0 = to_real<T>(g.T0), S = to_real<T>(g.S), x = __fdividef(Tk, T0);
+                mu = g.const_visc ? to_real<T>(g.mu0) : to_real<T>(g.mu0) * x * sqrtf(x) * __fdividef(T0 + S, Tk + S);
+            }
         }
-        const double h = dv.h_min[c];
-        const double Co = s->courant;
-        const double cur = Co / (N15 * (madv + a / h + (double)(N * N) * mu / (h * h * cs[0])));
+        const T h = to_real<T>(dv.h_min[c]);
+        const T Co = to_real<T>(s->courant);
+        const T cur = Co / (to_real<T>(N15) * (madv + a / h + (T)(N * N) * mu / (h * h * cs[0])));
         if (cur < local) local = cur;
     }
     // warp-shuffle min, then block min, then one atomic per block
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        const double o = __shfl_xor_sync(0xffffffffu, local, off);
+        const T o = __shfl_xor_sync(0xffffffffu, local, off);
         if (o < local) local = o;
     }
     if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = local;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double m = s_red[0];
+        T m = s_red[0];
         for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
             if (s_red[w] < m) m = s_red[w];
-        atomicMin(&s->dtmin, ord_double(m));
+        atomicMin(&s->dtmin, ord_double(to_f64<T>(m)));
     }
 }
 
@@ -121,47 +165,48 @@ static __global__ void k_courant(Dev dv, int expr_courant)
 // assert_positivity (dgsem/plens.cc:2531-2546) fused in. The modal transform and the mode
 // energies run in T (FP64 in the plain form and for the learned sensor's judge, FP32 in the
 // mixed form); the positivity check and alpha are FP64.
+// One tile of CPB cells (blk) of the blender; every thread of the block calls it.
 template <int P, class T>
-__global__ void __launch_bounds__(CellBlock<P>::THREADS) k_blender(Dev dv, Ops ops, GasP g, BlendP bp)
+__device__ __forceinline__ void blender_tile(const int64_t blk, const Dev& dv, const Ops& ops, const GasP& g,
+                                             const BlendP& bp, Scalars* s, const bool masked)
 {
     using CB = CellBlock<P>;
     constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1;
     __shared__ T sA[CPB][P3];
     __shared__ T sB[CPB][P3];
-    Scalars* s = dv.sc;
-    if (!s->active) return;
-    if (bp.gate && !s->sensor_fallback && !bp.mask) return;
-    const bool masked = bp.mask && !s->sensor_fallback;
     if (masked) {  // learned sensor: only the cells the judge handed back to this indicator
         bool any = false;
 #pragma unroll
         for (int q = 0; q < CPB; ++q) {
-            const int64_t cq = (int64_t)blockIdx.x * CPB + q;
+            const int64_t cq = blk * CPB + q;
             any |= (cq < dv.nc) && bp.mask[cq];
         }
         if (!any) return;
     }
     const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
-    const int64_t cell = (int64_t)blockIdx.x * CPB + cl;
+    const int64_t cell = blk * CPB + cl;
     const bool valid = (cl < CPB) && (cell < dv.nc) && (!masked || bp.mask[cell]);
     const int i = node % P, j = (node / P) % P, k = node / P2;
     if (valid) {
         const int64_t dof = cell * P3 + node;
-        double c[5];
-#pragma unroll
-        for (int v = 0; v < 5; ++v) c[v] = dv.U[v * dv.nd + dof];
-        if (!(c[0] > 0) || !(get_e(c) > 0)) {
-            atomicMin(&s->bad_dof, (long long)dof);
-            s->err = PLENS_GPU_E_POSITIVITY;
-        }
         if constexpr (sizeof(T) == 8) {
+            double c[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) c[v] = dv.U[v * dv.nd + dof];
+            if (!(c[0] > 0) || !(get_e(c) > 0)) {
+                atomicMin(&s->bad_dof, (long long)dof);
+                s->err = PLENS_GPU_E_POSITIVITY;
+            }
             const double p = get_p(c, g.gamma);
             sA[cl][node] = (bp.var == 2) ? c[0] : (bp.var == 1) ? p : p * c[0];
         } else {
             T cf[5];
-#pragma unroll
-            for (int v = 0; v < 5; ++v) cf[v] = (T)c[v];
-            const T p = get_p(cf, (T)g.gamma);
+            load_state<T>(dv, dof, cf);
+            if (!positive_dof_screened(dv, dof, cf)) {
+                atomicMin(&s->bad_dof, (long long)dof);
+                s->err = PLENS_GPU_E_POSITIVITY;
+            }
+            const T p = get_p(cf, f64_to_f32(g.gamma));
             sA[cl][node] = (bp.var == 2) ? cf[0] : (bp.var == 1) ? p : p * cf[0];
         }
     }
@@ -188,6 +233,71 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_blender(Dev dv, Ops o
         sB[cl][node] = acc;
     }
     __syncthreads();
+    if constexpr (sizeof(T) == 4) {
+        // mixed form: one warp per cell sums the mode energies (and the TV-filter statistics)
+        // with shuffles; lane 0 evaluates alpha in FP32
+        constexpr int NW = CB::THREADS / 32;
+        const int warp = tid >> 5, lane = tid & 31;
+        for (int q = warp; q < CPB; q += NW) {
+            const int64_t cq = blk * CPB + q;
+            if (cq >= dv.nc || (masked && !bp.mask[cq])) continue;
+            float e0 = 0, e1 = 0, e2 = 0, asum = 0, ub = 0, tl = 0;
+            for (int n = lane; n < P3; n += 32) {
+                const float md = sB[q][n];
+                const int mi = n % P, mj = (n / P) % P, mk = n / P2;
+                const float e = md * md;
+                e0 += e;
+                if (mi < N && mj < N && mk < N) e1 += e;
+                if (mi < N - 1 && mj < N - 1 && mk < N - 1) e2 += e;
+                if (bp.do_filter) {
+                    const float t = fabsf(md);
+                    asum += t;
+                    const float x = t * (ops.ftv[mi] + ops.ftv[mj] + ops.ftv[mk]);
+                    ub += x;
+                    if (mi <= 1 && mj <= 1 && mk <= 1) tl += x;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                e0 += __shfl_xor_sync(0xffffffffu, e0, off);
+                e1 += __shfl_xor_sync(0xffffffffu, e1, off);
+                e2 += __shfl_xor_sync(0xffffffffu, e2, off);
+                if (bp.do_filter) {
+                    asum += __shfl_xor_sync(0xffffffffu, asum, off);
+                    ub += __shfl_xor_sync(0xffffffffu, ub, off);
+                    tl += __shfl_xor_sync(0xffffffffu, tl, off);
+                }
+            }
+            if (lane == 0) {
+                float trouble = 1.0f - __fdividef(e1, e0);
+                if (N > 2) {
+                    const float t2 = 1.0f - __fdividef(e2, e1);
+                    if (t2 > trouble) trouble = t2;
+                }
+                const float thr = f64_to_f32(bp.thr), amin = f64_to_f32(bp.amin), amax = f64_to_f32(bp.amax);
+                float alpha;
+                if (bp.func == 0) {
+                    const float at = __fdividef(1.0f, 1.0f + __expf(-f64_to_f32(bp.sharp) * (__fdividef(trouble, thr) - 1.0f)));
+                    alpha = (at < amin) ? 0.0f : (at < amax ? at : amax);
+                } else {
+                    const float at = __fdividef(trouble, thr);
+                    alpha = (at > 1.0f) ? 1.0f : at;
+                }
+                double ad = f32_to_f64(alpha);
+                if (dv.cell_wall[cq]) {
+                    const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
+                    ad = (wl > ad) ? wl : ad;
+                }
+                dv.alpha_raw[cq] = ad;
+                if (bp.do_filter) {
+                    dv.tvstat[cq] = f32_to_f64(asum);
+                    dv.tvstat[dv.nc + cq] = f32_to_f64(ub);
+                    dv.tvstat[2 * dv.nc + cq] = f32_to_f64(tl);
+                }
+            }
+        }
+        return;
+    }
     if (valid && node == 0) {
         // sums in mode-index order, as the reference's loops over the mode index sets
         T et = 0, e1 = 0, e2 = 0;
@@ -229,6 +339,20 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_blender(Dev dv, Ops o
             dv.tvstat[dv.nc + cell] = ub;
             dv.tvstat[2 * dv.nc + cell] = tl;
         }
+    }
+}
+
+template <int P, class T>
+__global__ void __launch_bounds__(CellBlock<P>::THREADS) k_blender(Dev dv, Ops ops, GasP g, BlendP bp)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    if (bp.gate && !s->sensor_fallback && !bp.mask) return;
+    const bool masked = bp.mask && !s->sensor_fallback;
+    const int64_t nblk = (dv.nc + CellBlock<P>::CPB - 1) / CellBlock<P>::CPB;
+    for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+        blender_tile<P, T>(blk, dv, ops, g, bp, s, masked);
+        __syncthreads();  // shared tiles are reused by the next iteration
     }
 }
 
@@ -277,7 +401,7 @@ __device__ __forceinline__ void prim_to_cons_d(double rho, const double v[3], do
     }
     c[4] = c4;
 #pragma unroll
-    for (int v2 = 0; v2 < 5; ++v2) out[v2] = (T)c[v2];
+    for (int v2 = 0; v2 < 5; ++v2) out[v2] = to_real<T>(c[v2]);
 }
 
 template <class T>
@@ -298,16 +422,16 @@ __device__ __forceinline__ void bc_ghost(int stage, const Dev& dv, const GasP& g
                          const T c[5], const T av[9], const T n[3], const double* xyz, double t,
                          int64_t partner_dof, T cg[5], T ag[9])
 {
-    const T gm = (T)g.gamma;
+    const T gm = to_real<T>(g.gamma);
 #pragma unroll
     for (int v = 0; v < 9; ++v) ag[v] = av[v];
     switch (b.type) {
     case PLENS_BC_PERIODIC:
 #pragma unroll
-        for (int v = 0; v < 5; ++v) cg[v] = (T)dv.U[v * dv.nd + partner_dof];
+        for (int v = 0; v < 5; ++v) cg[v] = (sizeof(T) == 8) ? (T)dv.U[v * dv.nd + partner_dof] : (T)dv.Uf[v * dv.nd + partner_dof];
         if (stage == 3)
 #pragma unroll
-            for (int v = 0; v < 9; ++v) ag[v] = (T)dv.avars[v * dv.nd + partner_dof];
+            for (int v = 0; v < 9; ++v) ag[v] = as_real<T>(dv.avars)[v * dv.nd + partner_dof];
         return;
     case PLENS_BC_OUTFLOW: {
 #pragma unroll
@@ -319,17 +443,17 @@ __device__ __forceinline__ void bc_ghost(int stage, const Dev& dv, const GasP& g
             sp += (c[3] * c[3]) * (ri * ri);
             const T pin = get_p(c, gm);
             const T M = dsqrt(sp) / dsqrt(gm * pin / c[0]);
-            if (!(M >= T(1))) cg[4] += T(2) * ((T)b.p - pin) / (gm - 1);
+            if (!(M >= T(1))) cg[4] += T(2) * (to_real<T>(b.p) - pin) / (gm - 1);
         }
         return;
     }
     case PLENS_BC_UNIFORM_INFLOW:
         if (stage == 2) {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) cg[v] = (T)b.cons[v];
+            for (int v = 0; v < 5; ++v) cg[v] = to_real<T>(b.cons[v]);
         } else {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) cg[v] = T(2) * (T)b.cons[v] - c[v];
+            for (int v = 0; v < 5; ++v) cg[v] = T(2) * to_real<T>(b.cons[v]) - c[v];
         }
         return;
     case PLENS_BC_VARYING_INFLOW: {
@@ -351,7 +475,7 @@ __device__ __forceinline__ void bc_ghost(int stage, const Dev& dv, const GasP& g
     }
     case PLENS_BC_UNIFORM_TEMP_WALL:
     case PLENS_BC_INSULATED_WALL: {
-        const T vw[3] = {(T)b.vel[0], (T)b.vel[1], (T)b.vel[2]};
+        const T vw[3] = {to_real<T>(b.vel[0]), to_real<T>(b.vel[1]), to_real<T>(b.vel[2])};
         if (stage == 2) {
             cg[0] = c[0];
             cg[4] = c[4];
@@ -371,7 +495,7 @@ __device__ __forceinline__ void bc_ghost(int stage, const Dev& dv, const GasP& g
             return;
         }
         const T pin = get_p(c, gm);
-        const T rho_pr = (b.type == PLENS_BC_UNIFORM_TEMP_WALL) ? pin / ((T)g.R * (T)b.T) : c[0];
+        const T rho_pr = (b.type == PLENS_BC_UNIFORM_TEMP_WALL) ? pin / (to_real<T>(g.R) * to_real<T>(b.T)) : c[0];
         T cp[5];
         prim_to_cons_t(rho_pr, vw, pin, gm, cp);
 #pragma unroll
@@ -417,7 +541,7 @@ __device__ __forceinline__ void bc_ghost(int stage, const Dev& dv, const GasP& g
         return;
     }
     case PLENS_BC_ZPG_INFLOW: {
-        const T vw[3] = {(T)b.vel[0], (T)b.vel[1], (T)b.vel[2]};
+        const T vw[3] = {to_real<T>(b.vel[0]), to_real<T>(b.vel[1]), to_real<T>(b.vel[2])};
         T cp[5];
         prim_to_cons_t(c[0], vw, get_p(c, gm), gm, cp);
         if (stage == 2) {
@@ -443,52 +567,48 @@ __device__ __forceinline__ void bc_ghost(int stage, const Dev& dv, const GasP& g
 template <int P, class T, int STAGE>
 __global__ void __launch_bounds__(128) k_surface(Dev dv, GasP g, double* out)
 {
-    constexpr int P2 = P * P, P3 = P2 * P;
+    constexpr int P2 = P * P;
     Scalars* s = dv.sc;
     if (!s->active) return;
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= dv.ntask * P2) return;
     const int64_t ti = idx / P2;
     const int q = (int)(idx - ti * P2);
-    const int64_t c = dv.ft_cell[ti];
-    const int f = dv.ft_face[ti];
     const int bc = dv.ft_bc[ti];
-    const int64_t gd = c * P3 + face_node<P>(f, q);
-    const T gm = (T)g.gamma;
-    T cs[5], av[9] = {}, n[3];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) cs[v] = (T)dv.U[v * dv.nd + gd];
+    // precomputed dofs of both sides: the loads of the two states do not wait on each other
+    const int64_t gd = dv.fd_own[idx], gdn = dv.fd_nbr[idx];
+    const T gm = to_real<T>(g.gamma);
+    const T* avs = as_real<T>(dv.avars);
+    T cs[5], av[9] = {}, n[3], c2[5], a2[9] = {};
+    load_state<T>(dv, gd, cs);
+    if (gdn >= 0) load_state<T>(dv, gdn, c2);
     if (STAGE == 3) {
 #pragma unroll
-        for (int v = 0; v < 9; ++v) av[v] = (T)dv.avars[v * dv.nd + gd];
+        for (int v = 0; v < 9; ++v) av[v] = avs[v * dv.nd + gd];
+        if (gdn >= 0)
+#pragma unroll
+            for (int v = 0; v < 9; ++v) a2[v] = avs[v * dv.nd + gdn];
     }
 #pragma unroll
-    for (int d = 0; d < 3; ++d) n[d] = (T)dv.ft_normal[(ti * P2 + q) * 3 + d];
+    for (int d = 0; d < 3; ++d) n[d] = to_real<T>(dv.ft_normal[idx * 3 + d]);
     T fb = T(0);
     if (STAGE == 2) {
-        double a = (bc >= 0) ? dv.alpha[c] : 0.5 * (dv.alpha[c] + dv.alpha[dv.ft_nbr_cell[ti]]);
-        fb = (T)((a <= 0) ? 0.0 : (a <= 1 ? a : 1.0));
-    }
-    T c2[5], a2[9] = {};
-    int64_t slot_nb = -1;
-    if (bc >= 0) {
-        int64_t pd = -1;
-        const plens_bc_desc b = dv.bcs[bc];
-        if (b.type == PLENS_BC_PERIODIC)
-            pd = (int64_t)dv.ft_nbr_cell[ti] * P3 + face_node<P>(dv.ft_nbr_face[ti], dv.ft_nbr_fdof[ti * P2 + q]);
-        bc_ghost<T>(STAGE, dv, g, b, cs, av, n, dv.ft_xyz + (ti * P2 + q) * 3, s->time, pd, c2, a2);
-    } else {
-        const int64_t nb = dv.ft_nbr_cell[ti];
-        const int fn = dv.ft_nbr_face[ti];
-        const int qn = dv.ft_nbr_fdof[ti * P2 + q];
-        const int64_t gdn = nb * P3 + face_node<P>(fn, qn);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) c2[v] = (T)dv.U[v * dv.nd + gdn];
-        if (STAGE == 3) {
-#pragma unroll
-            for (int v = 0; v < 9; ++v) a2[v] = (T)dv.avars[v * dv.nd + gdn];
+        const int64_t c = dv.ft_cell[ti];
+        if constexpr (sizeof(T) == 8) {
+            double a = (bc >= 0) ? dv.alpha[c] : 0.5 * (dv.alpha[c] + dv.alpha[dv.ft_nbr_cell[ti]]);
+            fb = (a <= 0) ? 0.0 : (a <= 1 ? a : 1.0);
+        } else {
+            float a = f64_to_f32(dv.alpha[c]);
+            if (bc < 0) a = 0.5f * (a + f64_to_f32(dv.alpha[dv.ft_nbr_cell[ti]]));
+            fb = (a <= 0.0f) ? 0.0f : (a <= 1.0f ? a : 1.0f);
         }
-        slot_nb = (nb * 6 + fn) * P2 + qn;
+    }
+    const int64_t slot_nb = dv.fs_nbr[idx];
+    if (bc >= 0) {
+        const plens_bc_desc& b = dv.bcs[bc];
+        // periodic: the partner's state (and auxiliary variables) loaded above is the ghost
+        if (b.type != PLENS_BC_PERIODIC)
+            bc_ghost<T>(STAGE, dv, g, b, cs, av, n, dv.ft_xyz + idx * 3, s->time, -1, c2, a2);
     }
     T fl[5];
     if (STAGE == 1) {
@@ -503,13 +623,14 @@ __global__ void __launch_bounds__(128) k_surface(Dev dv, GasP g, double* out)
 #pragma unroll
         for (int v = 0; v < 5; ++v) fl[v] = T(0.5) * (f1[v] + f2[v]);
     }
-    const int64_t slot = (c * 6 + f) * P2 + q;
+    const int64_t slot = dv.fs_own[idx];
+    T* o = as_real<T>(out);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) out[v * dv.nslot + slot] = (double)fl[v];
+    for (int v = 0; v < 5; ++v) o[v * dv.nslot + slot] = fl[v];
     if (slot_nb >= 0) {
         const T sg = (STAGE == 1) ? T(1) : T(-1);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) out[v * dv.nslot + slot_nb] = (double)(sg * fl[v]);
+        for (int v = 0; v < 5; ++v) o[v * dv.nslot + slot_nb] = sg * fl[v];
     }
 }
 
@@ -530,25 +651,23 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
     const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
     const int64_t cell = (int64_t)blockIdx.x * CPB + cl;
     const bool valid = (cl < CPB) && (cell < dv.nc);
-    const T gm = (T)g.gamma;
-    double cd[5] = {1, 0, 0, 0, 1};
+    const T gm = to_real<T>(g.gamma);
+    T cd[5] = {1, 0, 0, 0, 1};  // the node's state in T (FP64 state, or its FP32 image)
     if (valid) {
         const int64_t dof = cell * P3 + node;
         T c[5], e[5];
+        load_state<T>(dv, dof, c);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
-            cd[v] = dv.U[v * dv.nd + dof];
-            c[v] = (T)cd[v];
-        }
+        for (int v = 0; v < 5; ++v) cd[v] = c[v];
         cons_to_entropy(c, gm, e);
 #pragma unroll
         for (int v = 0; v < 5; ++v) sE[(cl * 5 + v) * P3 + node] = e[v];
 #pragma unroll
-        for (int m = 0; m < 9; ++m) sJa[(cl * 9 + m) * P3 + node] = (T)dv.Ja[m * dv.nd + dof];
+        for (int m = 0; m < 9; ++m) sJa[(cl * 9 + m) * P3 + node] = to_real<T>(dv.Ja[m * dv.nd + dof]);
         for (int sl = node; sl < 6 * P2; sl += P3) {
             T fc[5], fe[5];
 #pragma unroll
-            for (int v = 0; v < 5; ++v) fc[v] = (T)dv.sf[v * dv.nslot + cell * 6 * P2 + sl];
+            for (int v = 0; v < 5; ++v) fc[v] = as_real<T>(dv.sf)[v * dv.nslot + cell * 6 * P2 + sl];
             cons_to_entropy(fc, gm, fe);
 #pragma unroll
             for (int v = 0; v < 5; ++v) sEf[((cl * 6 + sl / P2) * 5 + v) * P2 + (sl % P2)] = fe[v];
@@ -591,7 +710,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
                 }
             }
         }
-        const T jinv = fdiv(T(1.0), (T)dv.detJ[cell * P3 + node]);
+        const T jinv = fdiv(T(1.0), to_real<T>(dv.detJ[cell * P3 + node]));
 #pragma unroll
         for (int v = 0; v < 5; ++v) grad[gd][v] = acc[v] * jinv;
     }
@@ -600,7 +719,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
     {
         T c[5];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) c[v] = (T)cd[v];
+        for (int v = 0; v < 5; ++v) c[v] = cd[v];
         cons_to_entropy(c, gm, et);
     }
     T vg[3][3];
@@ -609,11 +728,22 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
 #pragma unroll
         for (int gd = 0; gd < 3; ++gd) vg[vd][gd] = (et[1 + vd] * grad[gd][4] / et[4] - grad[gd][1 + vd]) / et[4];
     const T tr = vg[0][0] + vg[1][1] + vg[2][2];
-    // mu and k in double from the double state (NavierStokes::get_mu / get_k, h:348-360)
-    const double e = get_e(cd);
-    const double Tk = e / (g.R / (g.gamma - 1));
-    const double mu = g.const_visc ? g.mu0 : g.mu0 * pow(Tk / g.T0, 1.5) * (g.T0 + g.S) / (Tk + g.S);
-    const double kk = mu * g.R * g.gamma / ((g.gamma - 1) * g.Pr);
+    // mu and k (NavierStokes::get_mu / get_k, h:348-360): FP64 from the FP64 state in the plain
+    // form, FP32 in the mixed form
+    T mu, kk;
+    if constexpr (sizeof(T) == 8) {
+        const double e = get_e(cd);
+        const double Tk = e / (g.R / (g.gamma - 1));
+        mu = g.const_visc ? g.mu0 : g.mu0 * pow(Tk / g.T0, 1.5) * (g.T0 + g.S) / (Tk + g.S);
+        kk = mu * g.R * g.gamma / ((g.gamma - 1) * g.Pr);
+    } else {
+        const T* c = cd;
+        const float Rg = to_real<T>(g.R), gm1 = to_real<T>(g.gamma - 1);
+        const float Tk = __fdividef(get_e(c) * gm1, Rg);
+        const float T0 = to_real<T>(g.T0), S = to_real<T>(g.S), x = __fdividef(Tk, T0);
+        mu = g.const_visc ? to_real<T>(g.mu0) : to_real<T>(g.mu0) * x * sqrtf(x) * __fdividef(T0 + S, Tk + S);
+        kk = mu * __fdividef(Rg * gm, gm1 * to_real<T>(g.Pr));
+    }
     T tau[6];
     int sid = 0;
 #pragma unroll
@@ -624,11 +754,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
             ++sid;
         }
 #pragma unroll
-    for (int v = 0; v < 6; ++v) dv.avars[v * dv.nd + dof] = (double)tau[v] * mu;
+    for (int v = 0; v < 6; ++v) as_real<T>(dv.avars)[v * dv.nd + dof] = tau[v] * mu;
 #pragma unroll
     for (int gd = 0; gd < 3; ++gd) {
-        const T tg = grad[gd][4] / (et[4] * et[4] * (T)g.R);
-        dv.avars[(6 + gd) * dv.nd + dof] = (double)(-tg) * kk;
+        const T tg = grad[gd][4] / (et[4] * et[4] * to_real<T>(g.R));
+        as_real<T>(dv.avars)[(6 + gd) * dv.nd + dof] = (-tg) * kk;
     }
 }
 
@@ -643,7 +773,8 @@ template <int P, class T>
 struct VolSmem {
     static constexpr int P3 = P * P * P;
     static constexpr int CPB = CellBlock<P>::CPB;
-    static constexpr int NQ = 7;  // rho, 1/rho, v0, v1, v2, p, beta
+    // rho, 1/rho, v0, v1, v2, p, beta (+ ln rho, ln beta, |v|^2 in the mixed form)
+    static constexpr int NQ = (sizeof(T) == 4) ? 10 : 7;
     static constexpr size_t bytes(bool visc)
     {
         return sizeof(T) * (size_t)CPB * P3 * (NQ + 5 + 9 + 15 + (visc ? 9 : 0) + 1);
@@ -654,7 +785,7 @@ template <int P, class T, bool VISC>
 __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1)) k_volume(Dev dv, Ops ops, GasP g, StageArgs sa)
 {
     using CB = CellBlock<P>;
-    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1, NQ = 7;
+    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1, NQ = VolSmem<P, T>::NQ;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sQ = reinterpret_cast<T*>(smem_raw);   // [CPB][NQ][P3]
     T* sC = sQ + CPB * NQ * P3;               // [CPB][5][P3]
@@ -668,20 +799,23 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
     const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
     const int64_t cell = (int64_t)blockIdx.x * CPB + cl;
     const bool valid = (cl < CPB) && (cell < dv.nc);
-    const T gm = (T)g.gamma;
+    const T gm = to_real<T>(g.gamma);
     T* Q = sQ + cl * NQ * P3;
     T* Cc = sC + cl * 5 * P3;
     T* J = sJ + cl * 9 * P3;
     T* Acc = sAcc + cl * 15 * P3;
     T* Av = sAv + cl * 9 * P3;
     const int64_t dof = cell * P3 + node;
+    // FP64 state of the node: kept in registers by the plain form; the mixed form reads it again
+    // for the update (an L2 hit), which frees ten registers through the flux phases
     double ud[5] = {0, 0, 0, 0, 0};
     if (valid) {
         T c[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
-            ud[v] = dv.U[v * dv.nd + dof];
-            c[v] = (T)ud[v];
+            const double u = dv.U[v * dv.nd + dof];
+            if constexpr (sizeof(T) == 8) ud[v] = u;
+            c[v] = to_real<T>(u);
             Cc[v * P3 + node] = c[v];
         }
         // per-node quantities with the reference's own expressions
@@ -694,18 +828,82 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
         Q[4 * P3 + node] = c[3] * ri;
         Q[5 * P3 + node] = p;
         Q[6 * P3 + node] = T(0.5) * c[0] / p;
+        if constexpr (sizeof(T) == 4) {
+            Q[7 * P3 + node] = __logf(c[0]);
+            Q[8 * P3 + node] = __logf(Q[6 * P3 + node]);
+            Q[9 * P3 + node] = Q[2 * P3 + node] * Q[2 * P3 + node] + Q[3 * P3 + node] * Q[3 * P3 + node] +
+                               Q[4 * P3 + node] * Q[4 * P3 + node];
+        }
 #pragma unroll
-        for (int m = 0; m < 9; ++m) J[m * P3 + node] = (T)dv.Ja[m * dv.nd + dof];
+        for (int m = 0; m < 9; ++m) J[m * P3 + node] = to_real<T>(dv.Ja[m * dv.nd + dof]);
         if (VISC) {
 #pragma unroll
-            for (int m = 0; m < 9; ++m) Av[m * P3 + node] = (T)dv.avars[m * dv.nd + dof];
+            for (int m = 0; m < 9; ++m) Av[m * P3 + node] = as_real<T>(dv.avars)[m * dv.nd + dof];
         }
     }
     __syncthreads();
     const double alpha = valid ? dv.alpha[cell] : 0.0;
+    const T alpha_t = to_real<T>(alpha);
 
     // ---- phase A: two-point volume fluxes per line
-    if (valid) {
+    bool fast_done = false;
+    if constexpr (sizeof(T) == 4) {
+        // mixed form, Chandrashekhar volume flux: unnormalised directions, per-node logarithms;
+        // the diagonal term is kept at the two end nodes only (D_ii = 0 at interior GLL nodes)
+        if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) {
+            fast_done = true;
+            const float hg = __fdividef(0.5f, gm - 1.0f), gf = __fdividef(gm, gm - 1.0f);
+            if (valid) {
+                for (int task = node; task < 3 * P2; task += P3) {
+                    const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
+                    float acc[P][5];
+#pragma unroll
+                    for (int i = 0; i < P; ++i)
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) acc[i][v] = 0.0f;
+#pragma unroll
+                    for (int i = 0; i < P; ++i) {
+                        const int ni = line_node<P>(dir, la, lb, i);
+                        float qi[10];
+#pragma unroll
+                        for (int k = 0; k < 10; ++k) qi[k] = Q[k * P3 + ni];
+                        const float ji[3] = {J[(dir * 3) * P3 + ni], J[(dir * 3 + 1) * P3 + ni], J[(dir * 3 + 2) * P3 + ni]};
+                        if (i == 0 || i == N) {
+                            float F[5];
+                            chandrashekhar_same_f32(qi, ji, gf, F);
+                            const float dd = opD2<float>(ops, i * P + i);
+#pragma unroll
+                            for (int v = 0; v < 5; ++v) acc[i][v] += dd * F[v];
+                        }
+#pragma unroll
+                        for (int m = i + 1; m < P; ++m) {
+                            const int nm = line_node<P>(dir, la, lb, m);
+                            float qm[10];
+#pragma unroll
+                            for (int k = 0; k < 10; ++k) qm[k] = Q[k * P3 + nm];
+                            const float nv[3] = {ji[0] + J[(dir * 3) * P3 + nm], ji[1] + J[(dir * 3 + 1) * P3 + nm],
+                                                 ji[2] + J[(dir * 3 + 2) * P3 + nm]};
+                            float F[5];
+                            chandrashekhar_pair_f32(qi, qm, nv, hg, F);
+                            const float di = opD<float>(ops, i * P + m), dm = opD<float>(ops, m * P + i);
+#pragma unroll
+                            for (int v = 0; v < 5; ++v) {
+                                acc[i][v] += di * F[v];
+                                acc[m][v] += dm * F[v];
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int i = 0; i < P; ++i) {
+                        const int ni = line_node<P>(dir, la, lb, i);
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) Acc[(dir * 5 + v) * P3 + ni] = acc[i][v];
+                    }
+                }
+            }
+        }
+    }
+    if (valid && !fast_done) {
         for (int task = node; task < 3 * P2; task += P3) {
             const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
             T acc[P][5];
@@ -782,6 +980,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
     // ---- phase B: HO inviscid = volume + surface, scaled by 1/(-detJ)
     const int ti[3] = {node % P, (node / P) % P, node / P2};
     const double detJ = valid ? dv.detJ[dof] : 1.0;
+    const T detJt = to_real<T>(detJ);
     T ho[5] = {0, 0, 0, 0, 0};
     if (valid) {
 #pragma unroll
@@ -807,12 +1006,12 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                 const T wend = opW<T>(ops, lr * N);
 #pragma unroll
                 for (int v = 0; v < 5; ++v) {
-                    const T fs = -ss * (T)dv.sf[v * dv.nslot + (cell * 6 + f) * P2 + q];
+                    const T fs = -ss * as_real<T>(dv.sf)[v * dv.nslot + (cell * 6 + f) * P2 + q];
                     ho[v] += fdiv(-ss * (fs - fin[v]) * nn, wend);
                 }
             }
         }
-        const T js = fdiv(T(1), T(-1) * (T)detJ);
+        const T js = fdiv(T(1), T(-1) * detJt);
 #pragma unroll
         for (int v = 0; v < 5; ++v) ho[v] *= js;
     }
@@ -876,12 +1075,12 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                     const T wend = opW<T>(ops, lr * N);
 #pragma unroll
                     for (int v = 0; v < 5; ++v) {
-                        const T fs = -ss * (T)dv.sf3[v * dv.nslot + (cell * 6 + f) * P2 + q];
+                        const T fs = -ss * as_real<T>(dv.sf3)[v * dv.nslot + (cell * 6 + f) * P2 + q];
                         hd[v] += fdiv(-ss * (fs - fin[v]) * nn, wend);
                     }
                 }
             }
-            const T js = fdiv(T(1), T(1) * (T)detJ);
+            const T js = fdiv(T(1), T(1) * detJt);
 #pragma unroll
             for (int v = 0; v < 5; ++v) hd[v] *= js;
         }
@@ -893,13 +1092,13 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
 #pragma unroll
     for (int k = 0; k < CPB; ++k) {
         const int64_t ck = (int64_t)blockIdx.x * CPB + k;
-        if (ck < dv.nc && dv.alpha[ck] > 0) any_lo = true;
+        if (ck < dv.nc && stored_gt0<T>(dv.alpha[ck])) any_lo = true;
     }
     if (any_lo) {
         __syncthreads();
-        const bool do_lo = valid && alpha > 0;
+        const bool do_lo = valid && stored_gt0<T>(alpha);
         if (do_lo) {
-            const T fb = (T)((alpha <= 0) ? 0.0 : (alpha <= 1 ? alpha : 1.0));
+            const T fb = (alpha_t <= T(0)) ? T(0) : (alpha_t <= T(1) ? alpha_t : T(1));
             for (int task = node; task < 3 * P2; task += P3) {
                 const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
                 T acc[P][5];
@@ -952,7 +1151,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                     const T wend = opW<T>(ops, lr * N);
 #pragma unroll
                     for (int v = 0; v < 5; ++v) {
-                        const T fl = sg * (T)dv.sf[v * dv.nslot + (cell * 6 + f) * P2 + q];
+                        const T fl = sg * as_real<T>(dv.sf)[v * dv.nslot + (cell * 6 + f) * P2 + q];
                         acc[i][v] += fdiv(sg * fl * nn, wend);
                     }
                 }
@@ -967,12 +1166,56 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
         __syncthreads();
         if (do_lo) {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) lo[v] = fdiv(Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node], (T)(-detJ));
+            for (int v = 0; v < 5; ++v) lo[v] = fdiv(Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node], -detJt);
         }
     }
     if (!valid) return;
 
     // ---- phase D: blend, then either store the residual or advance the RK registers
+    if constexpr (sizeof(T) == 4) {
+        // mixed form: blend and register combination in FP32 (the residual is an FP32 result),
+        // registers stored and the state accumulated in FP64
+        float R[5];
+        const float ad = VISC ? f64_to_f32(dv.alpha_d[cell]) : 0.0f;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            if (VISC) R[v] = (1.0f - ad) * hd[v] + alpha_t * lo[v] + (1.0f - alpha_t) * ho[v];
+            else R[v] = alpha_t * lo[v] + (1.0f - alpha_t) * ho[v];
+        }
+        if (g.plens_2d) R[3] = 0.0f;
+        if (sa.mode == 0) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) sa.Rout[v * dv.nd + dof] = f32_to_f64(R[v]);
+            return;
+        }
+        const float dtu = f64_to_f32(s->dt_update);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) ud[v] = dv.U[v * dv.nd + dof];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            const float Rs = R[v] * dtu;
+            const int64_t k = v * dv.nd + dof;
+            if (sa.mode == 1) {
+                float inc;
+                if (sa.stage == 1) inc = sa.fc2 * Rs;
+                else if (sa.stage == 2) inc = sa.fc1 * f64_to_f32(sa.R1[k]) + sa.fc2 * Rs;
+                else inc = sa.fc0 * f64_to_f32(sa.R0[k]) + sa.fc1 * f64_to_f32(sa.R1[k]) + sa.fc2 * Rs;
+                sa.Rw[k] = f32_to_f64(Rs);
+                const double un = ud[v] + f32_to_f64(inc);
+                dv.U[k] = un;
+                dv.Uf[k] = f64_to_f32(un);
+            } else {
+                const double Rsd = f32_to_f64(Rs);
+                double un;
+                if (sa.stage == 1) un = ud[v] + Rsd;
+                else if (sa.stage == 2) un = 0.75 * dv.U0[k] + 0.25 * ud[v] + 0.25 * Rsd;
+                else un = 1.0 / 3 * dv.U0[k] + 2.0 / 3 * ud[v] + 2.0 / 3 * Rsd;
+                dv.U[k] = un;
+                dv.Uf[k] = f64_to_f32(un);
+            }
+        }
+        return;
+    }
     double R[5];
     const double ad = VISC ? dv.alpha_d[cell] : 0.0;
 #pragma unroll

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "volume_mx.cuh"
 
 namespace plens_gpu {
 
@@ -49,8 +50,27 @@ struct Launch {
         k_aux<P, T><<<grid_cells(dv.nc), CB::THREADS, bytes, st>>>(dv, ops, g);
         return 1;
     }
+    template <bool VISC>
+    static void volume_mx(const Dev& dv, const Ops& ops, const GasP& g, const StageArgs& sa, cudaStream_t st)
+    {
+        if constexpr (P % 2 == 0) {
+            const size_t bytes = MxSmem<P, VISC>::bytes;
+            static bool attr = false;
+            if (!attr) {
+                cudaFuncSetAttribute(k_volume_mx<P, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+                attr = true;
+            }
+            k_volume_mx<P, VISC><<<grid_cells(dv.nc), CB::THREADS, bytes, st>>>(dv, ops, g, sa);
+        }
+    }
     static int volume(bool visc, const Dev& dv, const Ops& ops, const GasP& g, const StageArgs& sa, cudaStream_t st)
     {
+        // mixed form, even P: the TMA-staged kernel
+        if constexpr (sizeof(T) == 4 && P % 2 == 0) {
+            if (visc) volume_mx<true>(dv, ops, g, sa, st);
+            else volume_mx<false>(dv, ops, g, sa, st);
+            return 1;
+        }
         const size_t bytes = VolSmem<P, T>::bytes(visc);
         if (visc) {
             static bool attr = false;
@@ -72,7 +92,7 @@ struct Launch {
     static int time_step(const Dev& dv, const GasP& g, double N15, int N, cudaStream_t st)
     {
         const int grid = (int)((dv.nd + 255) / 256);
-        k_time_step<P><<<grid, 256, 0, st>>>(dv, g, N15, N);
+        k_time_step<P, T><<<grid, 256, 0, st>>>(dv, g, N15, N);
         return 1;
     }
     static LaunchTable table()

@@ -65,21 +65,13 @@ __device__ __forceinline__ float gelu_d(float x)
     return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 
-// Features of one cell into xs[64] (shared): rho*p at the nodes, interpolated to 4^3 GLL nodes,
-// normalised by its mean. Executed by one warp.
+// rho*p at the P^3 nodes (vs) -> interpolated to the 4^3 GLL nodes, divided by its mean, minus 1
+// (xs); one warp.
 template <int P>
-__device__ void cell_features(const Dev& dv, double gamma, const Interp& ip, int64_t cell, float* vs, float* ts, float* xs)
+__device__ void interp_normalise(const Interp& ip, float* vs, float* ts, float* xs)
 {
-    constexpr int P2 = P * P, P3 = P2 * P;
+    constexpr int P2 = P * P;
     const int lane = threadIdx.x & 31;
-    for (int n = lane; n < P3; n += 32) {
-        const int64_t dof = cell * P3 + n;
-        double c[5];
-#pragma unroll
-        for (int v = 0; v < 5; ++v) c[v] = dv.U[v * dv.nd + dof];
-        vs[n] = (float)(get_p(c, gamma) * c[0]);
-    }
-    __syncwarp();
     if (P == 4) {
         for (int n = lane; n < 64; n += 32) xs[n] = vs[n];
     } else {
@@ -114,6 +106,43 @@ __device__ void cell_features(const Dev& dv, double gamma, const Interp& ip, int
     xs[lane] = xs[lane] * inv - 1.0f;
     xs[lane + 32] = xs[lane + 32] * inv - 1.0f;
     __syncwarp();
+}
+
+
+// Features of one cell into xs[64] (shared): rho*p at the nodes, interpolated to 4^3 GLL nodes,
+// normalised by its mean. Executed by one warp. The state is read once here, so the positivity
+// assertion of the RHS (dgsem/plens.cc:2531-2546) is made here too, with the FP64 decision of the
+// mixed form.
+template <int P>
+__device__ void cell_features(const Dev& dv, double gamma, const Interp& ip, int64_t cell, float* vs, float* ts, float* xs)
+{
+    constexpr int P2 = P * P, P3 = P2 * P;
+    const int lane = threadIdx.x & 31;
+    const float gm = f64_to_f32(gamma);
+    for (int n = lane; n < P3; n += 32) {
+        const int64_t dof = cell * P3 + n;
+        float cf[5];
+        bool ok;
+        if (dv.Uf) {  // mixed form: the FP32 image of the state
+            load_state<float>(dv, dof, cf);
+            ok = positive_dof_screened(dv, dof, cf);
+        } else {
+            double c[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                c[v] = dv.U[v * dv.nd + dof];
+                cf[v] = f64_to_f32(c[v]);
+            }
+            ok = positive_state_screened(c, cf);
+        }
+        if (!ok) {
+            atomicMin(&dv.sc->bad_dof, (long long)dof);
+            dv.sc->err = PLENS_GPU_E_POSITIVITY;
+        }
+        vs[n] = get_p(cf, gm) * cf[0];
+    }
+    __syncwarp();
+    interp_normalise<P>(ip, vs, ts, xs);
 }
 
 // MLP forward of one sample held in xs (shared) by one warp; returns alpha_max*sigmoid(z).
@@ -152,25 +181,6 @@ __device__ float mlp_forward_warp(const float* W, const float* xs, float* hs, fl
     return amax / (1.0f + expf(-z));
 }
 
-// parameter vector -> shared memory with W1 and W2 transposed
-__device__ void load_weights_transposed(const float* __restrict__ Wg, float* sW)
-{
-    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) {
-        int dst = i;
-        if (i < kMlpHid * kMlpIn) {
-            const int o = i / kMlpIn, k = i - o * kMlpIn;
-            dst = k * kMlpHid + o;
-        } else {
-            const int base = kMlpHid * kMlpIn + kMlpHid;
-            if (i >= base && i < base + kMlpHid * kMlpHid) {
-                const int r = i - base, o = r / kMlpHid, k = r - o * kMlpHid;
-                dst = base + k * kMlpHid + o;
-            }
-        }
-        sW[dst] = Wg[i];
-    }
-}
-
 constexpr int kWarpsPerBlock = 8;
 
 // Learned values below this are set to 0 (the modal indicator's own cut is alpha_min = 1e-3): the
@@ -178,29 +188,164 @@ constexpr int kWarpsPerBlock = 8;
 // on every smooth cell. The judge bounds the error this introduces.
 constexpr float kLearnedCut = 0.01f;
 
-// Fused inference of the modal indicator's value (the blender before neighbour smoothing):
-// features, MLP, cut, wall override.
-template <int P>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_sensor_infer(Dev dv, const float* __restrict__ Wg, GasP g,
-                                                                       BlendP bp, Interp ip, double* out, int gated)
+// Per-warp shared scratch of the inference kernel (floats): nodal values, interpolation / modal
+// transform buffer, network input, hidden layer.
+constexpr int kScratchV = kMaxP * kMaxP * kMaxP, kScratch = 2 * kScratchV + 64 + 64;
+constexpr int kParamsPad = (kMlpParams + 3) / 4 * 4;  // float4 copies
+
+// This cell's FP32 state, the nodes lane, lane + 32, ... of the warp (NPL per lane).
+template <int P, int NPL>
+__device__ __forceinline__ void load_cell_f32(const Dev& dv, int64_t cell, int lane, float u[NPL][5])
 {
-    __shared__ float sW[kMlpParams];
-    __shared__ float sv[kWarpsPerBlock][kMaxP * kMaxP * kMaxP];
-    __shared__ float st[kWarpsPerBlock][4 * kMaxP * kMaxP];
-    __shared__ float sx[kWarpsPerBlock][64];
-    __shared__ float sh[kWarpsPerBlock][64];
+    constexpr int P3 = P * P * P;
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        const int n = lane + 32 * j;
+        if (n < P3) {
+            if (dv.Uf) {
+                load_state<float>(dv, cell * P3 + n, u[j]);
+            } else {  // FP64 form with the learned sensor: convert the state
+#pragma unroll
+                for (int v = 0; v < 5; ++v) u[j][v] = f64_to_f32(dv.U[v * dv.nd + cell * P3 + n]);
+            }
+        }
+    }
+}
+
+// The plain modal indicator of one cell by one warp in FP32 (the mixed form's k_blender: variable,
+// separable nodal -> modal transform, mode energies, Hennemann alpha), for the cells the judge
+// handed back; returns alpha before the wall override.
+template <int P, int NPL>
+__device__ float modal_alpha_warp(const Ops& ops, const BlendP& bp, float gm, const float u[NPL][5], float* a, float* b)
+{
+    constexpr int P2 = P * P, P3 = P2 * P, N = P - 1;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        const int n = lane + 32 * j;
+        if (n < P3) {
+            const float p = get_p(u[j], gm);
+            a[n] = (bp.var == 2) ? u[j][0] : (bp.var == 1) ? p : p * u[j][0];
+        }
+    }
+    __syncwarp();
+    for (int n = lane; n < P3; n += 32) {
+        const int i = n % P, j = (n / P) % P, k = n / P2;
+        float acc = 0;
+        for (int m = 0; m < P; ++m) acc += ops.fC1[i * P + m] * a[m + P * j + P2 * k];
+        b[n] = acc;
+    }
+    __syncwarp();
+    for (int n = lane; n < P3; n += 32) {
+        const int i = n % P, j = (n / P) % P, k = n / P2;
+        float acc = 0;
+        for (int m = 0; m < P; ++m) acc += ops.fC1[j * P + m] * b[i + P * m + P2 * k];
+        a[n] = acc;
+    }
+    __syncwarp();
+    float e0 = 0, e1 = 0, e2 = 0;
+    for (int n = lane; n < P3; n += 32) {
+        const int i = n % P, j = (n / P) % P, k = n / P2;
+        float md = 0;
+        for (int m = 0; m < P; ++m) md += ops.fC1[k * P + m] * a[i + P * j + P2 * m];
+        const float e = md * md;
+        e0 += e;
+        if (i < N && j < N && k < N) e1 += e;
+        if (i < N - 1 && j < N - 1 && k < N - 1) e2 += e;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        e0 += __shfl_xor_sync(0xffffffffu, e0, off);
+        e1 += __shfl_xor_sync(0xffffffffu, e1, off);
+        e2 += __shfl_xor_sync(0xffffffffu, e2, off);
+    }
+    __syncwarp();
+    float trouble = 1.0f - __fdividef(e1, e0);
+    if (N > 2) {
+        const float t2 = 1.0f - __fdividef(e2, e1);
+        if (t2 > trouble) trouble = t2;
+    }
+    const float thr = f64_to_f32(bp.thr), amin = f64_to_f32(bp.amin), amax = f64_to_f32(bp.amax);
+    if (bp.func == 0) {
+        const float at = __fdividef(1.0f, 1.0f + __expf(-f64_to_f32(bp.sharp) * (__fdividef(trouble, thr) - 1.0f)));
+        return (at < amin) ? 0.0f : (at < amax ? at : amax);
+    }
+    const float at = __fdividef(trouble, thr);
+    return (at > 1.0f) ? 1.0f : at;
+}
+
+// Network input of one cell from its FP32 state (rho*p at the nodes, interpolated to 4^3 GLL
+// nodes, normalised by the mean), with the positivity assertion of the RHS.
+template <int P, int NPL>
+__device__ void features_from_state(const Dev& dv, int64_t cell, float gm, const Interp& ip, const float u[NPL][5],
+                                    float* vs, float* ts, float* xs)
+{
+    constexpr int P2 = P * P, P3 = P2 * P;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        const int n = lane + 32 * j;
+        if (n < P3) {
+            const int64_t dof = cell * P3 + n;
+            if (!positive_dof_screened(dv, dof, u[j])) {
+                atomicMin(&dv.sc->bad_dof, (long long)dof);
+                dv.sc->err = PLENS_GPU_E_POSITIVITY;
+            }
+            vs[n] = get_p(u[j], gm) * u[j][0];
+        }
+    }
+    __syncwarp();
+    interp_normalise<P>(ip, vs, ts, xs);
+}
+
+// Fused inference of the modal indicator's value (the blender before neighbour smoothing):
+// features, MLP, cut, wall override; with `use_mask`, the cells the judge handed back get the
+// plain indicator instead, computed by the same warp. Persistent grid: each warp walks cells
+// with a stride and holds the next cell's state in registers while it evaluates the current one.
+template <int P>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_sensor_infer(Dev dv, const float* __restrict__ Wt, GasP g,
+                                                                       BlendP bp, Ops ops, Interp ip, double* out,
+                                                                       int gated, const uint8_t* mask)
+{
+    constexpr int P3 = P * P * P, NPL = (P3 + 31) / 32;
+    extern __shared__ __align__(16) float smem_f[];
+    float* sW = smem_f;                                   // [kParamsPad], W1 and W2 transposed
+    float* scr = sW + kParamsPad + (threadIdx.x >> 5) * kScratch;
+    float* sv = scr;
+    float* st = sv + kScratchV;
+    float* sx = st + kScratchV;
+    float* sh = sx + 64;
     Scalars* s = dv.sc;
     if (!s->active) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *dv.lo_count = 0;  // this stage's troubled-cell list
     if (gated && s->sensor_fallback) return;
-    load_weights_transposed(Wg, sW);
+    {
+        const float4* src = reinterpret_cast<const float4*>(Wt);
+        float4* dst = reinterpret_cast<float4*>(sW);
+        for (int i = threadIdx.x; i < kParamsPad / 4; i += blockDim.x) dst[i] = src[i];
+    }
     __syncthreads();
-    const float cut = fmaxf((float)bp.amin, kLearnedCut);
+    const float cut = fmaxf(f64_to_f32(bp.amin), kLearnedCut), amax = f64_to_f32(bp.amax);
+    const float gm = f64_to_f32(g.gamma);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int64_t cell = (int64_t)blockIdx.x * kWarpsPerBlock + warp; cell < dv.nc; cell += (int64_t)gridDim.x * kWarpsPerBlock) {
-        cell_features<P>(dv, g.gamma, ip, cell, sv[warp], st[warp], sx[warp]);
-        const float at = mlp_forward_warp(sW, sx[warp], sh[warp], (float)bp.amax);
+    const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlock;
+    int64_t cell = (int64_t)blockIdx.x * kWarpsPerBlock + warp;
+    float u[NPL][5];
+    if (cell < dv.nc) load_cell_f32<P, NPL>(dv, cell, lane, u);
+    for (; cell < dv.nc; cell += stride) {
+        float un[NPL][5];  // next cell's state, in flight during this cell's work
+        if (cell + stride < dv.nc) load_cell_f32<P, NPL>(dv, cell + stride, lane, un);
+        float at;
+        if (mask && mask[cell]) {
+            features_from_state<P, NPL>(dv, cell, gm, ip, u, sv, st, sx);  // positivity check
+            at = modal_alpha_warp<P, NPL>(ops, bp, gm, u, sv, st);
+        } else {
+            features_from_state<P, NPL>(dv, cell, gm, ip, u, sv, st, sx);
+            at = mlp_forward_warp(sW, sx, sh, amax);
+            if (at < cut) at = 0.0f;
+        }
         if (lane == 0) {
-            double a = (at < cut) ? 0.0 : (double)at;
+            double a = f32_to_f64(at);
             if (dv.cell_wall[cell]) {
                 const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
                 a = (wl > a) ? wl : a;
@@ -208,6 +353,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_sensor_infer(Dev dv, co
             out[cell] = a;
         }
         __syncwarp();
+#pragma unroll
+        for (int j = 0; j < NPL; ++j)
+#pragma unroll
+            for (int v = 0; v < 5; ++v) u[j][v] = un[j][v];
     }
 }
 
@@ -255,12 +404,6 @@ __global__ void k_judge_decide(Dev dv, unsigned long long* maxerr, unsigned int*
     *nbad = 0;
 }
 
-__global__ void k_lo_stat(Dev dv)
-{
-    if (!dv.sc->active) return;
-    dv.sc->lo_cells = *dv.lo_count;
-}
-
 template <int P>
 __global__ void k_features(Dev dv, GasP g, Interp ip, float* x)
 {
@@ -277,19 +420,35 @@ __global__ void k_features(Dev dv, GasP g, Interp ip, float* x)
 }
 
 template <int P>
-int launch_infer(const Dev& dv, const float* W, const GasP& g, const BlendP& bp, double* out, int gated, cudaStream_t st)
+int launch_infer(const Dev& dv, const float* Wt, const GasP& g, const BlendP& bp, const Ops& ops, double* out,
+                 int gated, const uint8_t* mask, cudaStream_t st)
 {
     const Interp ip = make_interp(P);
-    const int64_t blocks = std::min<int64_t>((dv.nc + kWarpsPerBlock - 1) / kWarpsPerBlock, 152 * 8);
-    k_sensor_infer<P><<<(unsigned)blocks, 32 * kWarpsPerBlock, 0, st>>>(dv, W, g, bp, ip, out, gated);
+    const size_t bytes = sizeof(float) * (kParamsPad + kWarpsPerBlock * kScratch);
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaFuncSetAttribute(k_sensor_infer<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sensor_infer<P>, 32 * kWarpsPerBlock, bytes);
+        per_sm = std::max(1, occ) * std::max(1, nsm);
+    }
+    const int64_t blocks = std::min<int64_t>((dv.nc + kWarpsPerBlock - 1) / kWarpsPerBlock, per_sm);
+    k_sensor_infer<P><<<(unsigned)blocks, 32 * kWarpsPerBlock, bytes, st>>>(dv, Wt, g, bp, ops, ip, out, gated, mask);
     return 1;
 }
 
+// plain indicator (FP64, the judge) on every cell; `limit` caps the grid (the block loop covers
+// the rest) for the launch that only runs in whole-domain fallback
 template <int P>
-int launch_blender(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
+int launch_blender(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st, int64_t limit = 0)
 {
     using CB = CellBlock<P>;
-    k_blender<P, double><<<(unsigned)((dv.nc + CB::CPB - 1) / CB::CPB), CB::THREADS, 0, st>>>(dv, ops, g, bp);
+    int64_t blocks = (dv.nc + CB::CPB - 1) / CB::CPB;
+    if (limit > 0 && blocks > limit) blocks = limit;
+    k_blender<P, double><<<(unsigned)blocks, CB::THREADS, 0, st>>>(dv, ops, g, bp);
     return 1;
 }
 
@@ -302,12 +461,11 @@ template <int P>
 int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
 {
     int n = 0;
-    cudaMemsetAsync(dv.lo_count, 0, sizeof(int32_t), st);
     BlendP b0 = bp;
     b0.gate = 0;
     b0.mask = nullptr;
     if (m.judge_this_step) {
-        n += launch_infer<P>(dv, m.params, g, bp, m.alpha_plain, 0, st);
+        n += launch_infer<P>(dv, m.params_t, g, bp, ops, m.alpha_plain, 0, nullptr, st);
         n += launch_blender<P>(dv, ops, g, b0, st);
         const unsigned grid = (unsigned)((dv.nc + 127) / 128);
         k_judge_cells<<<grid, 128, 0, st>>>(dv, m.alpha_plain, m.mask, m.tol, m.maxerr, m.nbad);
@@ -315,15 +473,16 @@ int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, con
         n += 2;
         m.judge_this_step = false;  // the remaining stages of this step follow the decision
     } else {
-        n += launch_infer<P>(dv, m.params, g, bp, dv.alpha_raw, 1, st);
+        // the cells the judge handed back get the plain indicator inside the inference kernel;
+        // the plain blender itself runs only in whole-domain fallback
+        n += launch_infer<P>(dv, m.params_t, g, bp, ops, dv.alpha_raw, 1, m.mask, st);
         BlendP b1 = bp;
         b1.gate = 1;
-        b1.mask = m.mask;
-        n += launch_blender<P>(dv, ops, g, b1, st);
+        b1.mask = nullptr;
+        n += launch_blender<P>(dv, ops, g, b1, st, 152 * 8);
     }
     k_alpha_smooth<<<(unsigned)((dv.nc + 127) / 128), 128, 0, st>>>(dv, b0);
-    k_lo_stat<<<1, 1, 0, st>>>(dv);
-    return n + 2;
+    return n + 1;
 }
 
 }  // namespace
@@ -333,6 +492,8 @@ int mlp_create(MlpDevice& m, int64_t nc, std::vector<void*>& allocs)
     m.nc = nc;
     if (cudaMalloc(&m.params, sizeof(float) * kMlpParams) != cudaSuccess) return 1;
     allocs.push_back(m.params);
+    if (cudaMalloc(&m.params_t, sizeof(float) * kParamsPad) != cudaSuccess) return 1;
+    allocs.push_back(m.params_t);
     if (cudaMalloc(&m.alpha_plain, sizeof(double) * (nc + 1)) != cudaSuccess) return 1;
     allocs.push_back(m.alpha_plain);
     if (cudaMalloc(&m.maxerr, sizeof(unsigned long long)) != cudaSuccess) return 1;
@@ -348,7 +509,24 @@ int mlp_create(MlpDevice& m, int64_t nc, std::vector<void*>& allocs)
 
 int mlp_set_weights(MlpDevice& m, const float* host_params, cudaStream_t st)
 {
+    // the inference kernel's copy: W1 and W2 transposed ([in][out]), padded to float4s
+    std::vector<float> t(kParamsPad, 0.0f);
+    for (int i = 0; i < kMlpParams; ++i) {
+        int dst = i;
+        if (i < kMlpHid * kMlpIn) {
+            const int o = i / kMlpIn, k = i - o * kMlpIn;
+            dst = k * kMlpHid + o;
+        } else {
+            const int base = kMlpHid * kMlpIn + kMlpHid;
+            if (i >= base && i < base + kMlpHid * kMlpHid) {
+                const int r = i - base, o = r / kMlpHid, k = r - o * kMlpHid;
+                dst = base + k * kMlpHid + o;
+            }
+        }
+        t[dst] = host_params[i];
+    }
     if (cudaMemcpyAsync(m.params, host_params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, st) != cudaSuccess) return 1;
+    if (cudaMemcpyAsync(m.params_t, t.data(), sizeof(float) * kParamsPad, cudaMemcpyHostToDevice, st) != cudaSuccess) return 1;
     if (cudaStreamSynchronize(st) != cudaSuccess) return 1;
     m.weights_set = true;
     return 0;

@@ -17,6 +17,7 @@ constexpr int kMlpParams = kMlpHid * kMlpIn + kMlpHid + kMlpHid * kMlpHid + kMlp
 
 struct MlpDevice {
     float* params = nullptr;        // [kMlpParams] W1 b1 W2 b2 w3 b3
+    float* params_t = nullptr;      // the same with W1, W2 transposed (inference kernel)
     double* alpha_plain = nullptr;  // [nc] judge: MLP alpha of the judged stage
     unsigned long long* maxerr = nullptr;  // order-preserving max per-cell alpha error
     uint8_t* mask = nullptr;        // [nc] cells handed back to the plain indicator by the judge

@@ -1,6 +1,7 @@
 // plens_gpu.cu -- the C ABI of include/plens_gpu.h: context lifecycle, device buffers and the
 // stage orchestration of PLENS::update / update_rk4 / update_rk3 / calc_rhs
 // (dgsem/plens.cc:3688-3779, 4334-4518) on one CUDA stream.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -129,6 +130,7 @@ static Ops make_ops(int P)
         for (int k = 0; k < ip; ++k) tv += std::fabs(legendre01(ip, qx[k + 1]) - legendre01(ip, qx[k]));
         o.tv[ip] = tv;
     }
+    for (int i = 0; i < P; ++i) o.ftv[i] = (float)o.tv[i];
     return o;
 }
 
@@ -214,6 +216,15 @@ int check_launch(plens_ctx* c, const char* what)
     return 0;
 }
 
+// mixed form: the FP32 image of the state after U was written outside the update kernels
+int refresh_image(plens_ctx* c)
+{
+    if (!c->dv.Uf) return 0;
+    k_state_image<<<(unsigned)std::min<int64_t>((5 * c->nd + 255) / 256, 152 * 16), 256, 0, c->stream>>>(c->dv);
+    c->launches += 1;
+    return check_launch(c, "state image");
+}
+
 // One RHS of the current stage: calc_rhs without the final store (dgsem/plens.cc:3688-3779).
 // The volume kernel of `sa` blends and either stores or advances the registers.
 int launch_rhs(plens_ctx* c, const StageArgs& sa)
@@ -275,8 +286,10 @@ int launch_step(plens_ctx* c, double end_time, bool judge = true)
     cudaStream_t st = c->stream;
     k_step_begin<<<1, 1, 0, st>>>(c->dv, end_time);
     c->launches += 1;
-    if (c->learned && judge) {
-        c->launches += mlp_step_begin(c->mlp, c->dv, c->prm.judge_every, st);
+    if (c->learned) {
+        k_snapshot<<<(unsigned)std::min<int64_t>((5 * c->nd / 2 + 255) / 256, 152 * 16), 256, 0, st>>>(c->dv);
+        c->launches += 1;
+        if (judge) c->launches += mlp_step_begin(c->mlp, c->dv, c->prm.judge_every, st);
     }
     if (int r = launch_time_step(c)) return r;
     if (c->prm.rk_order == 4) {
@@ -299,6 +312,9 @@ int launch_step(plens_ctx* c, double end_time, bool judge = true)
                 sa.c1 = kAi[s - 2] - kAo[s - 2];
                 sa.c2 = kAo[s - 1];
             }
+            sa.fc0 = (float)sa.c0;
+            sa.fc1 = (float)sa.c1;
+            sa.fc2 = (float)sa.c2;
             if (int r = launch_rhs(c, sa)) return r;
             r0 = r1;
             r1 = w;
@@ -418,6 +434,48 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         return r;
     d.n_bc = prm->n_bc;
     d.n_expr = prm->n_expr;
+    // per face dof: both sides' dofs and face slots (32-bit: the mesh must have fewer than 2^31
+    // dofs and face slots)
+    {
+        if (nd >= (int64_t)INT32_MAX || c->nslot >= (int64_t)INT32_MAX)
+            return fail(c, PLENS_GPU_E_INVALID, "mesh too large for 32-bit face tables");
+        const int P = c->P;
+        auto fnode = [P, P2](int f, int q) {
+            const int N = P - 1;
+            switch (f) {
+            case 0: return P * q;
+            case 1: return N + P * q;
+            case 2: return (q % P) + P2 * (q / P);
+            case 3: return P * N + (q % P) + P2 * (q / P);
+            case 4: return q;
+            default: return N * P2 + q;
+            }
+        };
+        const int64_t nfd = nt * P2;
+        std::vector<int32_t> own(nfd), nbr(nfd), sown(nfd), snbr(nfd);
+        for (int64_t t = 0; t < nt; ++t) {
+            const int64_t cc = mesh->ft_cell[t];
+            const int f = mesh->ft_face[t], bc = mesh->ft_bc[t];
+            const bool periodic = bc >= 0 && bc < prm->n_bc && prm->bcs[bc].type == PLENS_BC_PERIODIC;
+            for (int q = 0; q < P2; ++q) {
+                const int64_t k = t * P2 + q;
+                own[k] = (int32_t)(cc * P3 + fnode(f, q));
+                sown[k] = (int32_t)((cc * 6 + f) * P2 + q);
+                if (bc < 0 || periodic) {
+                    const int64_t nb = mesh->ft_nbr_cell[t];
+                    const int fn = mesh->ft_nbr_face[t], qn = mesh->ft_nbr_fdof[k];
+                    nbr[k] = (int32_t)(nb * P3 + fnode(fn, qn));
+                    snbr[k] = (bc < 0) ? (int32_t)((nb * 6 + fn) * P2 + qn) : -1;
+                } else {
+                    nbr[k] = -1;
+                    snbr[k] = -1;
+                }
+            }
+        }
+        if ((r = dupload(c, &d.fd_own, own.data(), nfd)) || (r = dupload(c, &d.fd_nbr, nbr.data(), nfd)) ||
+            (r = dupload(c, &d.fs_own, sown.data(), nfd)) || (r = dupload(c, &d.fs_nbr, snbr.data(), nfd)))
+            return r;
+    }
     // wall cells: a boundary face of type uniform temp wall or insulated wall
     // (dgsem/plens.cc:2909-2920)
     {
@@ -431,6 +489,7 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
             }
         if ((r = dupload(c, &d.cell_wall, wall.data(), nc))) return r;
     }
+    if (c->mixed && (r = dalloc(c, &d.Uf, 5 * nd))) return r;
     if ((r = dalloc(c, &d.U, 5 * nd)) || (r = dalloc(c, &d.alpha_raw, nc)) || (r = dalloc(c, &d.alpha, nc)) ||
         (r = dalloc(c, &d.alpha_d, nc)) || (r = dalloc(c, &d.sf, 5 * c->nslot)) || (r = dalloc(c, &c->sc, 1)) ||
         (r = dalloc(c, &c->Rout, 5 * nd)))
@@ -505,6 +564,7 @@ int plens_gpu_set_state(plens_ctx* c, const double* U)
 {
     if (!c || !U || !c->dv.U) return PLENS_GPU_E_INVALID;
     CK(cudaMemcpyAsync(c->dv.U, U, sizeof(double) * 5 * c->nd, cudaMemcpyHostToDevice, c->stream));
+    if (int r = refresh_image(c)) return r;
     CK(cudaStreamSynchronize(c->stream));
     return 0;
 }
@@ -590,36 +650,47 @@ int plens_gpu_synchronize(plens_ctx* c)
 int plens_gpu_advance(plens_ctx* c, int64_t n_steps, double end_time)
 {
     if (c && c->learned) {
-        // Learned sensor: step by step; a step that fails the positivity check is redone from
-        // its start state with the plain modal indicator on the whole domain (the fallback lasts
-        // until the next judged step).
-        if (!c->dv.U) return PLENS_GPU_E_INVALID;
+        // Learned sensor: steps are launched in batches; each step first snapshots its start
+        // state and clock on the device. A positivity failure deactivates the rest of the batch
+        // (k_step_begin), and the failed step is redone from its snapshot with the plain modal
+        // indicator on the whole domain (the fallback lasts until the next judged step).
+        if (!c->dv.U || n_steps < 0) return PLENS_GPU_E_INVALID;
         if (!c->mlp.weights_set) return fail(c, PLENS_GPU_E_INVALID, "learned sensor: weights not set");
-        for (int64_t s = 0; s < n_steps; ++s) {
+        constexpr int64_t kBatch = 64;
+        int64_t done = 0;
+        while (done < n_steps) {
             Scalars h0;
             CK(cudaStreamSynchronize(c->stream));
             CK(cudaMemcpy(&h0, c->sc, sizeof(h0), cudaMemcpyDeviceToHost));
             if (!(h0.time < end_time)) break;
-            CK(cudaMemcpyAsync(c->dv.U0, c->dv.U, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToDevice, c->stream));
-            const int saved_counter = c->mlp.step_counter;
-            if (int r = launch_step(c, end_time)) return r;
+            const int64_t nb = std::min<int64_t>(kBatch, n_steps - done);
+            const int counter0 = c->mlp.step_counter;
+            for (int64_t k = 0; k < nb; ++k)
+                if (int r = launch_step(c, end_time)) return r;
             const int r = sync_and_check(c);
             if (r != PLENS_GPU_E_POSITIVITY) {
                 if (r) return r;
+                done += nb;
                 continue;
             }
-            if (h0.sensor_fallback) return r;  // the plain indicator failed too: report it
+            Scalars h;
+            CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+            if (h.sensor_fallback) return r;  // the plain indicator was in use: report it
+            const int64_t ok_steps = h.n_steps0 - h0.n_steps;  // steps of the batch before the failed one
             CK(cudaMemcpyAsync(c->dv.U, c->dv.U0, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToDevice, c->stream));
-            Scalars h = h0;
+            if (int r2 = refresh_image(c)) return r2;
+            h.time = h.time0;
+            h.n_steps = h.n_steps0;
             h.sensor_fallback = 1;
-            h.fallbacks = h0.fallbacks + c->nc;  // every cell handed back for this step
+            h.fallbacks += c->nc;  // every cell handed back for this step
             h.err = 0;
             h.bad_dof = INT64_MAX;
             CK(cudaMemcpy(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice));
-            c->mlp.step_counter = saved_counter;
+            c->mlp.step_counter = counter0 + (int)ok_steps + 1;
             c->mlp.judge_this_step = false;
             if (int r2 = launch_step(c, end_time, false)) return r2;
             if (int r2 = sync_and_check(c)) return r2;
+            done += ok_steps + 1;
         }
         return 0;
     }
@@ -646,7 +717,64 @@ int plens_gpu_get_avars(plens_ctx* c, double* avars)
     if (!c || !avars) return PLENS_GPU_E_INVALID;
     if (!c->viscous) return fail(c, PLENS_GPU_E_INVALID, "inviscid run has no auxiliary variables");
     CK(cudaStreamSynchronize(c->stream));
+    if (c->mixed) {  // the mixed form keeps them in FP32
+        std::vector<float> f((size_t)(9 * c->nd));
+        CK(cudaMemcpy(f.data(), c->dv.avars, sizeof(float) * 9 * c->nd, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < f.size(); ++i) avars[i] = f[i];
+        return 0;
+    }
     CK(cudaMemcpy(avars, c->dv.avars, sizeof(double) * 9 * c->nd, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+namespace {
+
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x)
+{
+    x += 0x9e3779b97f4a7c15ULL;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
+    return x ^ (x >> 31);
+}
+
+__global__ void k_selftest_conversions(int64_t n, unsigned long long seed, unsigned long long* bad)
+{
+    unsigned long long nbad = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long h = splitmix64(seed + (unsigned long long)i);
+        unsigned long long b = h;
+        const int mode = (int)(i & 3);
+        if (mode) {  // exponent in [860, 1160): around and inside the normal float range
+            const unsigned long long e = 860 + (h >> 52) % 300;
+            b = (h & 0x800fffffffffffffULL) | (e << 52);
+            if (mode == 2) b = (b & ~0x1fffffffULL) | 0x10000000ULL;                       // exact tie
+            if (mode == 3) b = (b & ~0x1fffffffULL) | ((h & 1) ? 0x0fffffffULL : 0x10000001ULL);  // near tie
+        }
+        const double x = __longlong_as_double((long long)b);
+        const float a = f64_to_f32(x), r = __double2float_rn(x);
+        const bool ok1 = (a != a) ? (r != r) : (__float_as_uint(a) == __float_as_uint(r));
+        const float xf = __uint_as_float((unsigned int)(h >> 32));
+        const double c = f32_to_f64(xf), d = (double)xf;
+        const bool ok2 = (c != c) ? (d != d) : (__double_as_longlong(c) == __double_as_longlong(d));
+        nbad += (ok1 ? 0 : 1) + (ok2 ? 0 : 1);
+    }
+    if (nbad) atomicAdd(bad, nbad);
+}
+
+}  // namespace
+
+int plens_gpu_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches)
+{
+    if (n < 0 || !mismatches) return PLENS_GPU_E_INVALID;
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return PLENS_GPU_E_CUDA;
+    unsigned long long h = 0;
+    cudaMemset(d, 0, sizeof(*d));
+    k_selftest_conversions<<<152 * 4, 256>>>(n, seed, d);
+    const cudaError_t e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return PLENS_GPU_E_CUDA;
+    *mismatches = (int64_t)h;
     return 0;
 }
 
@@ -674,7 +802,11 @@ int plens_gpu_sensor_stats(plens_ctx* c, int64_t* judged, int64_t* fallbacks, do
     if (judged) *judged = h.judged;
     if (fallbacks) *fallbacks = h.fallbacks;
     if (max_alpha_err) *max_alpha_err = h.max_alpha_err;
-    if (lo_cells) *lo_cells = h.lo_cells;
+    if (lo_cells) {
+        int32_t n = 0;
+        if (c->dv.lo_count) CK(cudaMemcpy(&n, c->dv.lo_count, sizeof(n), cudaMemcpyDeviceToHost));
+        *lo_cells = n;
+    }
     return 0;
 }
 

@@ -1,0 +1,485 @@
+// volume_mx.cuh -- the mixed form's volume kernel for even P (N = 1, 3, 5): the same residual as
+// k_volume (calc_cell_ho_inv_residual, calc_cell_ho_dif_residual, calc_cell_lo_inv_residual, the
+// blend of calc_rhs and the register update; dgsem/plens.cc:3153-3583, 3753-3775, 4353-4400), with
+// every per-block input staged in shared memory by TMA bulk copies. For even P each cell's P^3
+// values of a variable are a multiple of 16 bytes, so a block's CPB cells are one contiguous,
+// 16-byte aligned chunk per variable: one thread issues the copies, two mbarriers signal them --
+// the state, metrics and Jacobians that the flux phase needs first, then the face values and the
+// RK registers, which arrive while the fluxes are computed.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace plens_gpu {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for phase 0 of a barrier; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait0(uint64_t* bar)
+{
+    for (int it = 0; it < (1 << 22); ++it)
+        if (mbar_try_wait(bar, 0)) return true;
+    return false;
+}
+// 1D bulk copy global -> shared (both 16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory layout of one block (bytes), all regions 16-byte aligned.
+template <int P, bool VISC>
+struct MxSmem {
+    static constexpr int P2 = P * P, P3 = P2 * P, CPB = CellBlock<P>::CPB, NB = CPB * P3, NF = CPB * 6 * P2;
+    static constexpr int NQ = 10;  // rho, 1/rho, v0, v1, v2, p, beta, ln rho, ln beta, |v|^2
+    static constexpr size_t up16(size_t x) { return (x + 15) / 16 * 16; }
+    // staged inputs (FP64 state/metrics/registers, FP32 face values and auxiliary variables)
+    static constexpr size_t oU = 0;                                   // double [5][NB]
+    static constexpr size_t oDet = oU + up16(8 * 5 * NB);             // double [NB]
+    static constexpr size_t oR0 = oDet + up16(8 * NB);                // double [5][NB]
+    static constexpr size_t oR1 = oR0 + up16(8 * 5 * NB);             // double [5][NB]
+    static constexpr size_t oSf = oR1 + up16(8 * 5 * NB);             // float [5][NF]
+    static constexpr size_t oSf3 = oSf + up16(4 * 5 * NF);            // float [5][NF] (viscous)
+    static constexpr size_t oAv = oSf3 + (VISC ? up16(4 * 5 * NF) : 0);  // float [9][NB] (viscous)
+    // Ja (double [9][NB]) is staged where the flux partial sums go once it is converted
+    static constexpr size_t oAcc = oAv + (VISC ? up16(4 * 9 * NB) : 0);
+    static constexpr size_t accBytes = (8 * 9 * NB > 4 * 15 * NB) ? 8 * 9 * NB : 4 * 15 * NB;
+    static constexpr size_t oQ = oAcc + up16(accBytes);               // float [CPB][NQ][P3]
+    static constexpr size_t oC = oQ + up16(4 * NQ * NB);              // float [CPB][5][P3]
+    static constexpr size_t oJ = oC + up16(4 * 5 * NB);               // float [CPB][9][P3]
+    static constexpr size_t bytes = oJ + up16(4 * 9 * NB);
+};
+
+template <int P, bool VISC>
+__global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, Ops ops, GasP g, StageArgs sa)
+{
+    static_assert(P % 2 == 0, "bulk staging needs 16-byte aligned per-cell chunks (even P)");
+    using CB = CellBlock<P>;
+    using L = MxSmem<P, VISC>;
+    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1, NQ = L::NQ, NB = L::NB, NF = L::NF;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bars[2];
+    double* stU = reinterpret_cast<double*>(smem_raw + L::oU);
+    double* stDet = reinterpret_cast<double*>(smem_raw + L::oDet);
+    double* stR0 = reinterpret_cast<double*>(smem_raw + L::oR0);
+    double* stR1 = reinterpret_cast<double*>(smem_raw + L::oR1);
+    float* stSf = reinterpret_cast<float*>(smem_raw + L::oSf);
+    float* stSf3 = reinterpret_cast<float*>(smem_raw + L::oSf3);
+    float* stAv = reinterpret_cast<float*>(smem_raw + L::oAv);
+    double* stJa = reinterpret_cast<double*>(smem_raw + L::oAcc);
+    float* sAcc = reinterpret_cast<float*>(smem_raw + L::oAcc);
+    float* sQ = reinterpret_cast<float*>(smem_raw + L::oQ);
+    float* sC = reinterpret_cast<float*>(smem_raw + L::oC);
+    float* sJ = reinterpret_cast<float*>(smem_raw + L::oJ);
+
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
+    const int64_t cell0 = (int64_t)blockIdx.x * CPB;
+    const int ncb = (int)((dv.nc - cell0 < CPB) ? dv.nc - cell0 : CPB);  // cells of this block
+    const int64_t cell = cell0 + cl;
+    const bool valid = (cl < ncb);
+    const bool need_r0 = sa.mode == 1 && sa.stage >= 3, need_r1 = sa.mode == 1 && sa.stage >= 2;
+
+    // ---- staging: one thread issues the bulk copies
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        const uint32_t bd = (uint32_t)(8 * ncb * P3), bf = (uint32_t)(4 * ncb * 6 * P2), bv = (uint32_t)(4 * ncb * P3);
+        const int64_t d0 = cell0 * P3, f0 = cell0 * 6 * P2;
+        mbar_arrive_expect_tx(&bars[0], bd * (5 + 9 + 1));
+#pragma unroll
+        for (int v = 0; v < 5; ++v) tma_load_1d(stU + v * NB, dv.U + v * dv.nd + d0, bd, &bars[0]);
+#pragma unroll
+        for (int m = 0; m < 9; ++m) tma_load_1d(stJa + m * NB, dv.Ja + m * dv.nd + d0, bd, &bars[0]);
+        tma_load_1d(stDet, dv.detJ + d0, bd, &bars[0]);
+        uint32_t late = bf * 5 + (need_r0 ? bd * 5 : 0) + (need_r1 ? bd * 5 : 0) + (VISC ? bf * 5 + bv * 9 : 0);
+        mbar_arrive_expect_tx(&bars[1], late);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) tma_load_1d(stSf + v * NF, as_real<float>(dv.sf) + v * dv.nslot + f0, bf, &bars[1]);
+        if (need_r0)
+#pragma unroll
+            for (int v = 0; v < 5; ++v) tma_load_1d(stR0 + v * NB, sa.R0 + v * dv.nd + d0, bd, &bars[1]);
+        if (need_r1)
+#pragma unroll
+            for (int v = 0; v < 5; ++v) tma_load_1d(stR1 + v * NB, sa.R1 + v * dv.nd + d0, bd, &bars[1]);
+        if (VISC) {
+#pragma unroll
+            for (int v = 0; v < 5; ++v) tma_load_1d(stSf3 + v * NF, as_real<float>(dv.sf3) + v * dv.nslot + f0, bf, &bars[1]);
+#pragma unroll
+            for (int m = 0; m < 9; ++m) tma_load_1d(stAv + m * NB, as_real<float>(dv.avars) + m * dv.nd + d0, bv, &bars[1]);
+        }
+    }
+    __syncthreads();  // barrier initialisation visible to every thread
+    // the block takes one decision: a wait that ran out anywhere ends the block (error status set,
+    // both copy groups waited for once more, bounded)
+    if (!__syncthreads_and(mbar_wait0(&bars[0]) ? 1 : 0)) {
+        if (tid == 0) s->err = PLENS_GPU_E_TIMEOUT;
+        mbar_wait0(&bars[0]);
+        mbar_wait0(&bars[1]);
+        return;
+    }
+
+    const float gm = f64_to_f32(g.gamma);
+    float* Q = sQ + cl * NQ * P3;
+    float* Cc = sC + cl * 5 * P3;
+    float* J = sJ + cl * 9 * P3;
+    float* Acc = sAcc + cl * 15 * P3;
+    const int64_t dof = cell * P3 + node;
+    const int bn = cl * P3 + node;  // node index within the block's staged chunks
+    if (valid) {
+        float c[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            c[v] = f64_to_f32(stU[v * NB + bn]);
+            Cc[v * P3 + node] = c[v];
+        }
+        const float p = get_p(c, gm);
+        const float ri = 1.0f / c[0];
+        const float v0 = c[1] * ri, v1 = c[2] * ri, v2 = c[3] * ri, beta = 0.5f * c[0] / p;
+        Q[0 * P3 + node] = c[0];
+        Q[1 * P3 + node] = ri;
+        Q[2 * P3 + node] = v0;
+        Q[3 * P3 + node] = v1;
+        Q[4 * P3 + node] = v2;
+        Q[5 * P3 + node] = p;
+        Q[6 * P3 + node] = beta;
+        Q[7 * P3 + node] = __logf(c[0]);
+        Q[8 * P3 + node] = __logf(beta);
+        Q[9 * P3 + node] = v0 * v0 + v1 * v1 + v2 * v2;
+#pragma unroll
+        for (int m = 0; m < 9; ++m) J[m * P3 + node] = f64_to_f32(stJa[m * NB + bn]);
+    }
+    __syncthreads();  // Ja staging is reused for the partial sums from here on
+    const double alpha = valid ? dv.alpha[cell] : 0.0;
+    const float alpha_t = f64_to_f32(alpha);
+
+    // ---- phase A: two-point volume fluxes per line
+    if (valid) {
+        const float hg = __fdividef(0.5f, gm - 1.0f), gf = __fdividef(gm, gm - 1.0f);
+        for (int task = node; task < 3 * P2; task += P3) {
+            const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
+            float acc[P][5];
+#pragma unroll
+            for (int i = 0; i < P; ++i)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) acc[i][v] = 0.0f;
+            if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) {
+                // unnormalised directions, per-node logarithms; the diagonal term only at the two
+                // end nodes (D_ii = 0 at interior GLL nodes)
+#pragma unroll
+                for (int i = 0; i < P; ++i) {
+                    const int ni = line_node<P>(dir, la, lb, i);
+                    float qi[10];
+#pragma unroll
+                    for (int k = 0; k < 10; ++k) qi[k] = Q[k * P3 + ni];
+                    const float ji[3] = {J[(dir * 3) * P3 + ni], J[(dir * 3 + 1) * P3 + ni], J[(dir * 3 + 2) * P3 + ni]};
+                    if (i == 0 || i == N) {
+                        float F[5];
+                        chandrashekhar_same_f32(qi, ji, gf, F);
+                        const float dd = opD2<float>(ops, i * P + i);
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) acc[i][v] += dd * F[v];
+                    }
+#pragma unroll
+                    for (int m = i + 1; m < P; ++m) {
+                        const int nm = line_node<P>(dir, la, lb, m);
+                        float qm[10];
+#pragma unroll
+                        for (int k = 0; k < 10; ++k) qm[k] = Q[k * P3 + nm];
+                        const float nv[3] = {ji[0] + J[(dir * 3) * P3 + nm], ji[1] + J[(dir * 3 + 1) * P3 + nm],
+                                             ji[2] + J[(dir * 3 + 2) * P3 + nm]};
+                        float F[5];
+                        chandrashekhar_pair_f32(qi, qm, nv, hg, F);
+                        const float di = opD<float>(ops, i * P + m), dm = opD<float>(ops, m * P + i);
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) {
+                            acc[i][v] += di * F[v];
+                            acc[m][v] += dm * F[v];
+                        }
+                    }
+                }
+            } else {
+                // other volume fluxes: the reference's normalised form
+#pragma unroll
+                for (int i = 0; i < P; ++i) {
+                    const int ni = line_node<P>(dir, la, lb, i);
+                    float qi[7];
+#pragma unroll
+                    for (int k = 0; k < 7; ++k) qi[k] = Q[k * P3 + ni];
+                    const float ci[5] = {Cc[ni], Cc[P3 + ni], Cc[2 * P3 + ni], Cc[3 * P3 + ni], Cc[4 * P3 + ni]};
+#pragma unroll
+                    for (int m = i; m < P; ++m) {
+                        const int nm = line_node<P>(dir, la, lb, m);
+                        float qm[7];
+#pragma unroll
+                        for (int k = 0; k < 7; ++k) qm[k] = Q[k * P3 + nm];
+                        const float cm[5] = {Cc[nm], Cc[P3 + nm], Cc[2 * P3 + nm], Cc[3 * P3 + nm], Cc[4 * P3 + nm]};
+                        float nv[3];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) nv[d] = 0.5f * (J[(dir * 3 + d) * P3 + ni] + J[(dir * 3 + d) * P3 + nm]);
+                        float nn = sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+                        const float dn[3] = {__fdividef(nv[0], nn), __fdividef(nv[1], nn), __fdividef(nv[2], nn)};
+                        float F[5];
+                        if (g.ivf == PLENS_IVF_KENNEDY_GRUBER) kennedy_gruber_vol(qi, qm, get_e(ci), get_e(cm), dn, gm, F);
+                        else ismail_roe_vol(ci, cm, dn, gm, F);
+                        const float di = opD2<float>(ops, i * P + m) * nn, dm = opD2<float>(ops, m * P + i) * nn;
+#pragma unroll
+                        for (int v = 0; v < 5; ++v) {
+                            acc[i][v] += di * F[v];
+                            if (m != i) acc[m][v] += dm * F[v];
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int ni = line_node<P>(dir, la, lb, i);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) Acc[(dir * 5 + v) * P3 + ni] = acc[i][v];
+            }
+        }
+    }
+    // face values, registers (and viscous inputs) staged; partial sums visible
+    if (!__syncthreads_and(mbar_wait0(&bars[1]) ? 1 : 0)) {
+        if (tid == 0) s->err = PLENS_GPU_E_TIMEOUT;
+        mbar_wait0(&bars[1]);
+        return;
+    }
+
+    // ---- phase B: HO inviscid = volume + surface, scaled by 1/(-detJ)
+    const int ti[3] = {node % P, (node / P) % P, node / P2};
+    const float detJ = valid ? f64_to_f32(stDet[bn]) : 1.0f;
+    const float* sfb = stSf + cl * 6 * P2;  // this cell's face slots; variable stride NF
+    float ho[5] = {0, 0, 0, 0, 0};
+    if (valid) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) ho[v] = Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node];
+        const float ci[5] = {Cc[node], Cc[P3 + node], Cc[2 * P3 + node], Cc[3 * P3 + node], Cc[4 * P3 + node]};
+#pragma unroll
+        for (int sd = 0; sd < 3; ++sd) {
+#pragma unroll
+            for (int lr = 0; lr < 2; ++lr) {
+                if (ti[sd] != (lr ? N : 0)) continue;
+                const int f = 2 * sd + lr;
+                const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
+                // (F* - F_in(n/|n|)) |n| = F* |n| - F_in(n): the physical flux is linear in n
+                const float jn[3] = {J[(sd * 3) * P3 + node], J[(sd * 3 + 1) * P3 + node], J[(sd * 3 + 2) * P3 + node]};
+                const float nn = sqrtf(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
+                float fin[5];
+                inv_flux(ci, jn, gm, fin);
+                const float ss = lr ? -1.0f : 1.0f;
+                const float rw = __fdividef(1.0f, opW<float>(ops, lr * N));
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    const float fs = -ss * sfb[v * NF + f * P2 + q];
+                    ho[v] += -ss * (fs * nn - fin[v]) * rw;
+                }
+            }
+        }
+        const float js = __fdividef(-1.0f, detJ);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) ho[v] *= js;
+    }
+
+    // ---- viscous HO residual: nodal viscous fluxes along each contravariant direction
+    float hd[5] = {0, 0, 0, 0, 0};
+    if (VISC) {
+        __syncthreads();  // Acc is reused
+        float av[9];
+#pragma unroll
+        for (int m = 0; m < 9; ++m) av[m] = valid ? stAv[m * NB + bn] : 0.0f;
+        if (valid) {
+            const float ci[5] = {Cc[node], Cc[P3 + node], Cc[2 * P3 + node], Cc[3 * P3 + node], Cc[4 * P3 + node]};
+#pragma unroll
+            for (int md = 0; md < 3; ++md) {
+                const float jn[3] = {J[(md * 3) * P3 + node], J[(md * 3 + 1) * P3 + node], J[(md * 3 + 2) * P3 + node]};
+                float F[5];
+                dif_flux(ci, av, jn, F);  // linear in the direction: F(n/|n|) |n| = F(n)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) Acc[(md * 5 + v) * P3 + node] = F[v];
+            }
+        }
+        __syncthreads();
+        if (valid) {
+            for (int m = 0; m < P; ++m) {
+#pragma unroll
+                for (int md = 0; md < 3; ++md) {
+                    const int lo = (md == 0) ? m + P * ti[1] + P2 * ti[2] : (md == 1) ? ti[0] + P * m + P2 * ti[2] : ti[0] + P * ti[1] + P2 * m;
+                    const float dvl = opD<float>(ops, ti[md] * P + m);
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) hd[v] += dvl * Acc[(md * 5 + v) * P3 + lo];
+                }
+            }
+            const float ci[5] = {Cc[node], Cc[P3 + node], Cc[2 * P3 + node], Cc[3 * P3 + node], Cc[4 * P3 + node]};
+            const float* sf3b = stSf3 + cl * 6 * P2;
+#pragma unroll
+            for (int sd = 0; sd < 3; ++sd) {
+#pragma unroll
+                for (int lr = 0; lr < 2; ++lr) {
+                    if (ti[sd] != (lr ? N : 0)) continue;
+                    const int f = 2 * sd + lr;
+                    const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
+                    const float jn[3] = {J[(sd * 3) * P3 + node], J[(sd * 3 + 1) * P3 + node], J[(sd * 3 + 2) * P3 + node]};
+                    const float nn = sqrtf(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
+                    float fin[5];
+                    dif_flux(ci, av, jn, fin);
+                    const float ss = lr ? -1.0f : 1.0f;
+                    const float rw = __fdividef(1.0f, opW<float>(ops, lr * N));
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        const float fs = -ss * sf3b[v * NF + f * P2 + q];
+                        hd[v] += -ss * (fs * nn - fin[v]) * rw;
+                    }
+                }
+            }
+            const float js = __fdividef(1.0f, detJ);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) hd[v] *= js;
+        }
+    }
+
+    // ---- phase C: first-order subcell residual, only where alpha > 0
+    float lo[5] = {0, 0, 0, 0, 0};
+    bool any_lo = false;
+#pragma unroll
+    for (int k = 0; k < CPB; ++k)
+        if (k < ncb && stored_gt0<float>(dv.alpha[cell0 + k])) any_lo = true;
+    if (any_lo) {
+        __syncthreads();
+        const bool do_lo = valid && stored_gt0<float>(alpha);
+        if (do_lo) {
+            const float fb = (alpha_t <= 0.0f) ? 0.0f : (alpha_t <= 1.0f ? alpha_t : 1.0f);
+            for (int task = node; task < 3 * P2; task += P3) {
+                const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
+                float acc[P][5];
+#pragma unroll
+                for (int i = 0; i < P; ++i)
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) acc[i][v] = 0.0f;
+                // running subcell normal n_(i-1,i) = Ja_0 + sum_{l<i} sum_m Q_lm Ja_m
+                // (metric_terms.cc:106-141)
+                const int n0 = line_node<P>(dir, la, lb, 0);
+                float sn[3] = {J[(dir * 3) * P3 + n0], J[(dir * 3 + 1) * P3 + n0], J[(dir * 3 + 2) * P3 + n0]};
+#pragma unroll
+                for (int id = 1; id < P; ++id) {
+#pragma unroll
+                    for (int m = 0; m < P; ++m) {
+                        const int nm = line_node<P>(dir, la, lb, m);
+                        const float qlm = opQ<float>(ops, (id - 1) * P + m);
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) sn[d] += qlm * J[(dir * 3 + d) * P3 + nm];
+                    }
+                    const int nl = line_node<P>(dir, la, lb, id - 1), nr = line_node<P>(dir, la, lb, id);
+                    const float nn = sqrtf(sn[0] * sn[0] + sn[1] * sn[1] + sn[2] * sn[2]);
+                    const float dn[3] = {__fdividef(sn[0], nn), __fdividef(sn[1], nn), __fdividef(sn[2], nn)};
+                    const float cL[5] = {Cc[nl], Cc[P3 + nl], Cc[2 * P3 + nl], Cc[3 * P3 + nl], Cc[4 * P3 + nl]};
+                    const float cR[5] = {Cc[nr], Cc[P3 + nr], Cc[2 * P3 + nr], Cc[3 * P3 + nr], Cc[4 * P3 + nr]};
+                    float F[5];
+                    inv_surf_flux(cL, cR, dn, gm, g.isf, fb, F);
+                    const float wl = __fdividef(nn, opW<float>(ops, id - 1)), wr = __fdividef(nn, opW<float>(ops, id));
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        acc[id - 1][v] += F[v] * wl;
+                        acc[id][v] -= F[v] * wr;
+                    }
+                }
+                // cell-face terms at both ends of the line
+#pragma unroll
+                for (int lr = 0; lr < 2; ++lr) {
+                    const int i = lr ? N : 0;
+                    const int ni = line_node<P>(dir, la, lb, i);
+                    const int f = 2 * dir + lr;
+                    const int q = la + P * lb;
+                    const float j0 = J[(dir * 3) * P3 + ni], j1 = J[(dir * 3 + 1) * P3 + ni], j2 = J[(dir * 3 + 2) * P3 + ni];
+                    const float nn = sqrtf(j0 * j0 + j1 * j1 + j2 * j2);
+                    const float sw = __fdividef(nn, opW<float>(ops, lr * N));  // contrib_sign * flux_sign = +1
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) acc[i][v] += sfb[v * NF + f * P2 + q] * sw;
+                }
+#pragma unroll
+                for (int i = 0; i < P; ++i) {
+                    const int ni = line_node<P>(dir, la, lb, i);
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) Acc[(dir * 5 + v) * P3 + ni] = acc[i][v];
+                }
+            }
+        }
+        __syncthreads();
+        if (do_lo) {
+            const float js = __fdividef(-1.0f, detJ);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) lo[v] = (Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node]) * js;
+        }
+    }
+    if (!valid) return;
+
+    // ---- phase D: blend and register combination in FP32 (the residual is an FP32 result);
+    // registers stored and the state accumulated in FP64
+    float R[5];
+    const float ad = VISC ? f64_to_f32(dv.alpha_d[cell]) : 0.0f;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        if (VISC) R[v] = (1.0f - ad) * hd[v] + alpha_t * lo[v] + (1.0f - alpha_t) * ho[v];
+        else R[v] = alpha_t * lo[v] + (1.0f - alpha_t) * ho[v];
+    }
+    if (g.plens_2d) R[3] = 0.0f;
+    if (sa.mode == 0) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) sa.Rout[v * dv.nd + dof] = f32_to_f64(R[v]);
+        return;
+    }
+    const float dtu = f64_to_f32(s->dt_update);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+        const float Rs = R[v] * dtu;
+        const int64_t k = v * dv.nd + dof;
+        const double u = stU[v * NB + bn];
+        if (sa.mode == 1) {
+            float inc;
+            if (sa.stage == 1) inc = sa.fc2 * Rs;
+            else if (sa.stage == 2) inc = sa.fc1 * f64_to_f32(stR1[v * NB + bn]) + sa.fc2 * Rs;
+            else inc = sa.fc0 * f64_to_f32(stR0[v * NB + bn]) + sa.fc1 * f64_to_f32(stR1[v * NB + bn]) + sa.fc2 * Rs;
+            sa.Rw[k] = f32_to_f64(Rs);
+            const double un = u + f32_to_f64(inc);
+            dv.U[k] = un;
+            dv.Uf[k] = f64_to_f32(un);
+        } else {
+            const double Rsd = f32_to_f64(Rs);
+            double un;
+            if (sa.stage == 1) un = u + Rsd;
+            else if (sa.stage == 2) un = 0.75 * dv.U0[k] + 0.25 * u + 0.25 * Rsd;
+            else un = 1.0 / 3 * dv.U0[k] + 2.0 / 3 * u + 2.0 / 3 * Rsd;
+            dv.U[k] = un;
+            dv.Uf[k] = f64_to_f32(un);
+        }
+    }
+}
+
+}  // namespace plens_gpu

@@ -1,0 +1,142 @@
+"""The mixed form (FP32 flux differencing, FP64 state, metrics and RK registers) against the FP64
+oracle, over the kernels it dispatches to: the TMA-staged volume kernel (even P: N = 1, 3, 5;
+inviscid and viscous), the generic one (odd P), every surface and volume flux scheme, RK3 and the
+positivity check.
+
+Tolerances: one RHS, max over equations of max|R_mixed - R_oracle| / max|R_oracle| <= 2e-4 (2e-3
+on the 1e-3-clustered curved O-mesh, where the wall-cell residual is a small difference of large
+fluxes); after 20 steps, relative L1 of rho, momentum and rho E <= 1e-4.
+"""
+import numpy as np
+import pytest
+
+from helpers import make, max_rel_err, rel_l1
+from oracle.pyoracle import Oracle
+from plens_gb300 import configs
+from plens_gb300.api import GpuSolver, PositivityError
+
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 2e-4
+STEPS_TOL = 1e-4
+
+
+def _state(case64, steps):
+    o = Oracle(case64)
+    o.set_state(case64.initial_state(), case64.start_time)
+    o.advance(steps)
+    U, t, _, _ = o.get_state()
+    return U, t
+
+
+def _rhs_err(spec64, specmx, steps=2):
+    c64, cmx = make(spec64), make(specmx)
+    U, t = _state(c64, steps)
+    o = Oracle(c64)
+    o.set_state(U, t)
+    Ro = o.rhs()[0]
+    g = GpuSolver(cmx)
+    g.set_state(U, t)
+    Rg = g.rhs()
+    return max_rel_err(Rg, Ro)
+
+
+def _steps_err(spec64, specmx, steps=20):
+    c64, cmx = make(spec64), make(specmx)
+    o = Oracle(c64)
+    o.set_state(c64.initial_state(), c64.start_time)
+    o.advance(steps)
+    g = GpuSolver(cmx)
+    g.set_state(cmx.initial_state(), cmx.start_time)
+    g.advance(steps)
+    return rel_l1(g.get_state(), o.get_state()[0])
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3, 4, 5])
+def test_mixed_dmr_degrees(degree):
+    e = _rhs_err(configs.dmr(nx=12, ny=4, degree=degree), configs.dmr(nx=12, ny=4, degree=degree, precision="mixed"))
+    print(f"N={degree} rhs err {e:.3e}")
+    assert e <= RHS_TOL
+    s = _steps_err(configs.dmr(nx=12, ny=4, degree=degree), configs.dmr(nx=12, ny=4, degree=degree, precision="mixed"))
+    print(f"N={degree} 20-step rel L1 {s}")
+    assert s.max() <= STEPS_TOL
+
+
+def test_mixed_sod():
+    e = _rhs_err(configs.sod(n=40), configs.sod(n=40, precision="mixed"), steps=10)
+    assert e <= RHS_TOL
+    assert _steps_err(configs.sod(n=40), configs.sod(n=40, precision="mixed"), 100).max() <= STEPS_TOL
+
+
+@pytest.mark.parametrize("scheme", ["Rusanov", "AUSM+-up", "Rusanov-HLLC", "Chandrashekhar"])
+def test_mixed_surface_schemes(scheme):
+    def spec(prec):
+        prm, files, deg = configs.dmr(nx=12, ny=4, precision=prec)
+        return prm.replace("set inviscid surface flux scheme = HLLC", f"set inviscid surface flux scheme = {scheme}"), files, deg
+    e = _rhs_err(spec("fp64"), spec("mixed"))
+    print(f"{scheme} rhs err {e:.3e}")
+    assert e <= RHS_TOL
+
+
+@pytest.mark.parametrize("scheme", ["KG", "IR"])
+def test_mixed_volume_schemes(scheme):
+    def spec(prec):
+        prm, files, deg = configs.dmr(nx=8, ny=4, precision=prec)
+        return prm.replace("set inviscid volume flux scheme = Chandrashekhar", f"set inviscid volume flux scheme = {scheme}"), files, deg
+    e = _rhs_err(spec("fp64"), spec("mixed"))
+    print(f"{scheme} rhs err {e:.3e}")
+    assert e <= RHS_TOL
+
+
+def test_mixed_viscous_cylinder():
+    c64 = make(configs.cylinder(n_radial=6, n_azimuthal=12))
+    cmx = make(configs.cylinder(n_radial=6, n_azimuthal=12, precision="mixed"))
+    U, t = _state(c64, 2)
+    o = Oracle(c64)
+    o.set_state(U, t)
+    Ro = o.rhs()[0]
+    g = GpuSolver(cmx)
+    g.set_state(U, t)
+    Rg = g.rhs()
+    e = max_rel_err(Rg, Ro)
+    d = np.abs(Rg - Ro)
+    worst = np.unravel_index(np.argmax(d / np.abs(Ro).max(axis=1, keepdims=True)), d.shape)
+    print(f"cylinder rhs err {e:.3e} (worst var {worst[0]} cell {worst[1] // 64}); per-var rel L1 "
+          f"{d.sum(axis=1) / np.abs(Ro).sum(axis=1)}")
+    assert e <= 2e-3
+    s = _steps_err(configs.cylinder(n_radial=6, n_azimuthal=12), configs.cylinder(n_radial=6, n_azimuthal=12, precision="mixed"))
+    print(f"cylinder 20-step rel L1 {s}")
+    assert s.max() <= STEPS_TOL
+
+
+def test_mixed_viscous_shock_vortex():
+    e = _rhs_err(configs.shock_vortex(n=3, modes=2), configs.shock_vortex(n=3, modes=2, precision="mixed"), steps=1)
+    print(f"shock-vortex rhs err {e:.3e}")
+    assert e <= RHS_TOL
+    s = _steps_err(configs.shock_vortex(n=3, modes=2), configs.shock_vortex(n=3, modes=2, precision="mixed"), 5)
+    assert s.max() <= STEPS_TOL
+
+
+def test_mixed_rk3():
+    def spec(prec):
+        prm, files, deg = configs.dmr(nx=12, ny=4, precision=prec)
+        return prm.replace("set RK order = 4", "set RK order = 3"), files, deg
+    assert _steps_err(spec("fp64"), spec("mixed")).max() <= STEPS_TOL
+
+
+def test_mixed_positivity_failure_reports_first_bad_dof():
+    """The mixed form's screened check decides rho > 0, e > 0 in FP64: a state with e < 0 by a
+    tiny margin at one dof (invisible to an FP32 test) and rho < 0 at a later one."""
+    case = make(configs.dmr(nx=12, ny=4, precision="mixed"))
+    U = case.initial_state()
+    k = 301
+    ke = 0.5 * (U[1, k] ** 2 + U[2, k] ** 2 + U[3, k] ** 2) / U[0, k]
+    U[4, k] = ke * (1 - 1e-12)
+    U[0, 777] = -1.0
+    g = GpuSolver(case)
+    g.set_state(U)
+    with pytest.raises(PositivityError) as ei:
+        g.rhs()
+    assert ei.value.dof == k
+    g.set_state(case.initial_state(), 0.0)
+    g.rhs()
