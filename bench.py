@@ -177,12 +177,12 @@ def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_in
     g.set_state(U0, 0.0)
     g.advance(warmup)
     stream = torch.cuda.ExternalStream(g.stream, device=torch.device("cuda", device_index))
-    g.set_kernel_timing(True)
     launches0 = g.kernel_launches
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
+    # timed region: the steps as the library runs them (each step a replayed CUDA graph)
     with ClockSampler(device_index) as cs:
         ev0.record(stream)
         g.advance_async(steps)
@@ -192,6 +192,11 @@ def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_in
     barrier()
     ms = ev0.elapsed_time(ev1)
     launches = g.kernel_launches - launches0
+    # the same number of steps again with the library's CUDA events around every volume-kernel
+    # launch (eager launches), for the kernel's own duration
+    g.set_kernel_timing(True)
+    g.advance_async(steps)
+    g.synchronize()
     vol_ms, vol_n = g.kernel_timing()
     g.set_kernel_timing(False)
     stats = g.sensor_stats() if sensor == "learned" else None
@@ -259,31 +264,49 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# per configuration: the accuracy window of the FP32 forms against the FP64 form (the config's own
+# run length where it fits in minutes, else a stated window), and the full-size window in which the
+# FP64 form is compared with the oracle
+WORKLOADS = {
+    "sod": {"acc_steps": 100, "acc_end": None, "oracle_steps": 100, "note": "config run length: 100 steps"},
+    # the config runs to t = 0.2, but every form (FP64 included, as the FP64 oracle) stops there
+    # on the positivity assertion first: the window is fixed, and `horizon` reports where the FP32
+    # form stops
+    "dmr": {"acc_steps": 1000, "acc_end": None, "oracle_steps": 100,
+            "note": "first 1000 steps (the config's t = 0.2 is not reached, see horizon)", "horizon": 0.2},
+    "cylinder": {"acc_steps": 1000, "acc_end": None, "oracle_steps": 10,
+                 "note": "first 1000 of the config's 20000 steps"},
+    "shock_vortex": {"acc_steps": 20, "acc_end": None, "oracle_steps": 1,
+                     "note": "first 20 of the config's 500 steps"},
+}
+
+
 def run_workload_report(args):
     """One JSON line per configuration: DOF-stage/s of the FP64 plain form, the FP32 form with
-    the modal and with the learned sensor, the oracle on the host cores, and the relative L1
-    errors of the FP32 forms against the FP64 form (itself equal to the oracle to 1e-10, see the
-    parity tests) after --accuracy-steps steps from the initial condition."""
+    the modal and with the learned sensor, and the oracle on the host cores; the relative L1
+    errors of the FP32 forms against the FP64 form over the configuration's accuracy window, and
+    of the FP64 form against the oracle over a full-size window."""
     import torch
 
+    from oracle.pyoracle import Oracle, max_threads
     from plens_gb300 import configs
     from plens_gb300.api import GpuSolver, PlensError
 
     torch.cuda.set_device(0)
+    wl = WORKLOADS[args.workload]
+    acc_steps = args.accuracy_steps or wl["acc_steps"]
+    end = wl["acc_end"] if wl["acc_end"] is not None else 1e300
     weights = _sensor_weights()
     forms = [("fp64_plain", "fp64", "modal"), ("fp32_modal", "mixed", "modal")]
     if weights is not None:
         forms.append(("fp32_learned", "mixed", "learned"))
-    out = {"workload": args.workload}
+    out = {"workload": args.workload, "accuracy_window": wl["note"] if not args.accuracy_steps else f"{acc_steps} steps"}
     states = {}
     for name, prec, sensor in forms:
         r = measure_form(prec, sensor, args.steps, args.warmup, 0, weights, workload=args.workload)
         nd = r["case"].n_dofs
         out[name] = {"dof_stage_per_s": nd * 5 * args.steps / (r["ms"] / 1e3), "ms_per_step": r["ms"] / args.steps,
-                     "volume_kernel_ms": r["vol_ms"] / max(r["vol_n"], 1), "n_dofs": nd}
-        if r["stats"]:
-            out[name]["sensor_stats"] = r["stats"]
-        # accuracy run from the initial condition
+                     "volume_kernel_ms": r["vol_ms"] / max(r["vol_n"], 1), "n_dofs": nd, "clocks": r["clocks"]}
         case = configs.make_case(_spec(args.workload, prec, sensor))
         g = GpuSolver(case)
         if sensor == "learned":
@@ -291,10 +314,10 @@ def run_workload_report(args):
         g.set_state(case.initial_state(), case.start_time)
         t0 = time.perf_counter()
         try:
-            g.advance(args.accuracy_steps)
+            g.advance(acc_steps, end)
             states[name] = g.get_state()
-            out[name]["accuracy_run"] = {"steps": args.accuracy_steps, "seconds": time.perf_counter() - t0,
-                                         "t_end": g.get_time()[0]}
+            t, n, _ = g.get_time()
+            out[name]["accuracy_run"] = {"steps": n, "seconds": time.perf_counter() - t0, "t_end": t}
         except PlensError as e:
             out[name]["accuracy_run"] = {"error": str(e)}
         if sensor == "learned":
@@ -305,19 +328,42 @@ def run_workload_report(args):
     for name in ("fp32_modal", "fp32_learned"):
         if name in states and "fp64_plain" in states:
             out[name]["rel_l1_vs_fp64"] = dict(zip(("rho", "momentum", "rhoE"), _rel_l1(states[name], states["fp64_plain"])))
-    if not args.no_cpu_baseline:
-        from oracle.pyoracle import Oracle, max_threads
-        case = configs.make_case(_spec(args.workload, "fp64", "modal"))
-        o = Oracle(case)
-        o.set_state(case.initial_state(), case.start_time)
+    if wl.get("horizon"):
+        # how far the FP32 modal form gets towards the configuration's end time
+        case = configs.make_case(_spec(args.workload, "mixed", "modal"))
+        g = GpuSolver(case)
+        g.set_state(case.initial_state(), case.start_time)
         t0 = time.perf_counter()
-        o.advance(1)
-        t1 = time.perf_counter() - t0
-        n = max(1, min(args.steps, int(20.0 / max(t1, 1e-3))))
-        t0 = time.perf_counter()
-        o.advance(n)
-        dt = time.perf_counter() - t0
-        out["cpu_oracle"] = {"dof_stage_per_s": case.n_dofs * 5 * n / dt, "cores": max_threads(), "steps": n}
+        h = {"end_time": wl["horizon"]}
+        try:
+            for _ in range(200):
+                g.advance(500, wl["horizon"])
+                t, n, dt = g.get_time()
+                if t >= wl["horizon"] or time.perf_counter() - t0 > 120:
+                    break
+            h["reached"] = True
+        except PlensError as e:
+            h["reached"] = False
+            h["error"] = str(e)
+        t, n, dt = g.get_time()
+        h.update({"t": t, "steps": n, "last_dt": dt, "seconds": time.perf_counter() - t0})
+        out["horizon_fp32_modal"] = h
+        g.close()
+    # the FP64 form against the oracle at full size
+    case = configs.make_case(_spec(args.workload, "fp64", "modal"))
+    o = Oracle(case)
+    o.set_state(case.initial_state(), case.start_time)
+    t0 = time.perf_counter()
+    o.advance(wl["oracle_steps"])
+    dt = time.perf_counter() - t0
+    g = GpuSolver(case)
+    g.set_state(case.initial_state(), case.start_time)
+    g.advance(wl["oracle_steps"])
+    out["fp64_vs_oracle"] = {"steps": wl["oracle_steps"],
+                             "rel_l1": dict(zip(("rho", "momentum", "rhoE"), _rel_l1(g.get_state(), o.get_state()[0])))}
+    g.close()
+    out["cpu_oracle"] = {"dof_stage_per_s": case.n_dofs * 5 * wl["oracle_steps"] / dt, "cores": max_threads(),
+                         "steps": wl["oracle_steps"], "seconds": dt}
     print(json.dumps(out), flush=True)
 
 
@@ -331,7 +377,7 @@ def main():
     ap.add_argument("--workload", default="", choices=["", "sod", "dmr", "cylinder", "shock_vortex"],
                     help="per-configuration report (throughput of every form, accuracy after --accuracy-steps) "
                          "instead of the benchmark line")
-    ap.add_argument("--accuracy-steps", type=int, default=100)
+    ap.add_argument("--accuracy-steps", type=int, default=0, help="override the accuracy window (steps)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -402,7 +448,7 @@ def main():
         "dtype": "f32 flux differencing + f64 state/registers",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": f"mixed FP32 + {fast_sensor} sensor",
-                   "l2": "working set per step > L2 (state, 3 registers, metrics, face buffers ~ 0.3 GB)",
+                   "l2": "working set per step > L2 (state, 3 registers, metrics, face buffers ~ 0.5 GB)",
                    "parallelism": f"replicas x{ws}"},
         "forms": {
             "fp64_plain": job["plain"],
@@ -412,9 +458,11 @@ def main():
         },
         "roofline": {
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_kind": peak_kind, "kernel": f"k_volume (mixed form, {fast_sensor} sensor)",
-            "traffic": _traffic_from_profile("k_volume_dmr.md"),
-            "note": "algorithmic 280 B per DOF-stage x 921600 DoFs per launch / live CUDA-event launch time",
+            "peak_kind": peak_kind, "kernel": f"k_volume_mx (mixed form, {fast_sensor} sensor)",
+            "traffic": _traffic_from_profile("k_volume_mx_dmr.md"),
+            "note": "achieved: algorithmic 280 B per DOF-stage x 921600 DoFs per launch / mean CUDA-event "
+                    "launch time of the kernel-timing pass; traffic: ncu DRAM bytes of a stage-1 launch "
+                    "(no RK register read yet), profiles/k_volume_mx_dmr.md",
         },
         "e2e": {"value": hd["e2e"], "unit": UNIT, "h2d_bytes_per_step": fast["bytes_state"],
                 "d2h_bytes_per_step": fast["bytes_state"]},

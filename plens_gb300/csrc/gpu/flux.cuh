@@ -23,7 +23,8 @@ template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrt
 template <class T> __device__ __forceinline__ T dlog(T x) { return log(x); }
 template <> __device__ __forceinline__ float dlog<float>(float x) { return logf(x); }
 template <class T> __device__ __forceinline__ T dpow(T x, T y) { return pow(x, y); }
-template <> __device__ __forceinline__ float dpow<float>(float x, float y) { return powf(x, y); }
+// FP32: the base is a positive pressure or speed ratio on every call of this path
+template <> __device__ __forceinline__ float dpow<float>(float x, float y) { return __powf(x, y); }
 template <class T> __device__ __forceinline__ T dabs(T x) { return fabs(x); }
 template <> __device__ __forceinline__ float dabs<float>(float x) { return fabsf(x); }
 
@@ -485,6 +486,77 @@ __device__ __forceinline__ void inv_surf_flux(const T o[5], const T nb[5], const
         for (int col = 0; col < 3; ++col) a += R[row][col] * fr[1 + col];
         f[1 + row] = a;
     }
+}
+
+// Mixed form, HLLC: the same flux as the rotation of inv_surf_flux + hllc_x, evaluated in the
+// original frame. With the frame's x axis e = n (or +-x when |x cross n| <= 1e-3, where the
+// reference keeps the identity, navier_stokes.cc:489-521) the rotated states' x velocity is v.e,
+// the physical x-flux rotated back is the flux along e, and the HLLC star state rotated back is
+// t (rho, rho (v + (s - v.e) e), E + (s - v.e)(rho s + p/(S - v.e))) (navier_stokes.cc:936-1033).
+// The wave-speed estimate keeps the reference's PVRS / TRRS / TSRS choice; the side and the
+// supersonic cases are selected without branches.
+__device__ __forceinline__ void hllc_n_f32(const float l[5], const float r[5], const float nin[3], float gma, float f[5])
+{
+    float e[3] = {nin[0], nin[1], nin[2]};
+    if (!(sqrtf(nin[1] * nin[1] + nin[2] * nin[2]) > 1e-3f)) {  // |x cross n|
+        e[0] = (nin[0] < 0.0f) ? -1.0f : 1.0f;
+        e[1] = 0.0f;
+        e[2] = 0.0f;
+    }
+    const float ril = __fdividef(1.0f, l[0]), rir = __fdividef(1.0f, r[0]);
+    const float ul = (l[1] * e[0] + l[2] * e[1] + l[3] * e[2]) * ril;
+    const float ur = (r[1] * e[0] + r[2] * e[1] + r[3] * e[2]) * rir;
+    const float pl = (gma - 1.0f) * (l[4] - 0.5f * (l[1] * l[1] + l[2] * l[2] + l[3] * l[3]) * ril);
+    const float pr = (gma - 1.0f) * (r[4] - 0.5f * (r[1] * r[1] + r[2] * r[2] + r[3] * r[3]) * rir);
+    const float pmin = fminf(pl, pr), pmax = fmaxf(pl, pr);
+    const float al = sqrtf(gma * pl * ril), ar = sqrtf(gma * pr * rir);
+    const float p_pvrs = 0.5f * (pl + pr) - 0.125f * (ur - ul) * (l[0] + r[0]) * (al + ar);
+    float ps;
+    if (__fdividef(pmax, pmin) < 2.0f && pmin <= p_pvrs && p_pvrs <= pmax) {
+        ps = p_pvrs;
+    } else if (p_pvrs < pmin) {
+        const float z = __fdividef(gma - 1.0f, 2.0f * gma);
+        ps = __powf(__fdividef((al + ar) - 0.5f * (gma - 1.0f) * (ur - ul), al * __powf(pl, -z) + ar * __powf(pr, -z)),
+                    __fdividef(1.0f, z));
+    } else {
+        const float p0 = fmaxf(p_pvrs, 0.0f), ga = __fdividef(2.0f, gma + 1.0f), gb = __fdividef(gma - 1.0f, gma + 1.0f);
+        const float gl = sqrtf(__fdividef(ga * ril, p0 + gb * pl)), gr = sqrtf(__fdividef(ga * rir, p0 + gb * pr));
+        ps = __fdividef(gl * pl + gr * pr - (ur - ul), gl + gr);
+    }
+    const float gq = __fdividef(gma + 1.0f, 2.0f * gma);
+    const float ql = (ps <= pl) ? 1.0f : sqrtf(1.0f + gq * (__fdividef(ps, pl) - 1.0f));
+    const float qr = (ps <= pr) ? 1.0f : sqrtf(1.0f + gq * (__fdividef(ps, pr) - 1.0f));
+    const float sl = ul - al * ql, sr = ur + ar * qr;
+    const float ml = l[0] * (sl - ul), mr = r[0] * (sr - ur);
+    const float s = __fdividef(pr - pl + ml * ul - mr * ur, ml - mr);
+    // side: the left state when sl > 0 or s > 0; supersonic when the side's wave has the sign
+    const bool left = (sl > 0.0f) || (s > 0.0f);
+    const bool super = left ? (sl > 0.0f) : !(sr > 0.0f);
+    const float* K = left ? l : r;
+    const float uK = left ? ul : ur, pK = left ? pl : pr, SK = left ? sl : sr;
+    float FK[5];
+    FK[0] = K[0] * uK;
+    FK[1] = uK * K[1] + pK * e[0];
+    FK[2] = uK * K[2] + pK * e[1];
+    FK[3] = uK * K[3] + pK * e[2];
+    FK[4] = (K[4] + pK) * uK;
+    const float t = __fdividef(SK - uK, SK - s), ds = s - uK;
+    float Us[5];
+    Us[0] = t * K[0];
+    Us[1] = t * (K[1] + K[0] * ds * e[0]);
+    Us[2] = t * (K[2] + K[0] * ds * e[1]);
+    Us[3] = t * (K[3] + K[0] * ds * e[2]);
+    Us[4] = t * (K[4] + ds * (K[0] * s + __fdividef(pK, SK - uK)));
+#pragma unroll
+    for (int v = 0; v < 5; ++v) f[v] = super ? FK[v] : FK[v] + SK * (Us[v] - K[v]);
+}
+
+// mixed-form surface flux: HLLC in the original frame, the other schemes through the rotation
+__device__ __forceinline__ void inv_surf_flux_mx(const float o[5], const float nb[5], const float n[3], float gma, int isf,
+                                                 float fb, float f[5])
+{
+    if (isf == PLENS_ISF_HLLC) hllc_n_f32(o, nb, n, gma, f);
+    else inv_surf_flux(o, nb, n, gma, isf, fb, f);
 }
 
 // viscous flux along a unit direction from the symmetric stress tensor and heat flux stored as

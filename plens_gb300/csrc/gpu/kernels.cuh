@@ -565,7 +565,7 @@ __device__ __forceinline__ void bc_ghost(int stage, const Dev& dv, const GasP& g
 // face task. Interior faces are computed once and written to both sides (neighbour sign +1 in
 // stage 1, -1 in stages 2 and 3); boundary faces (periodic included) once per side.
 template <int P, class T, int STAGE>
-__global__ void __launch_bounds__(128) k_surface(Dev dv, GasP g, double* out)
+__global__ void __launch_bounds__(128, (sizeof(T) == 4 ? 10 : 1)) k_surface(Dev dv, GasP g, double* out)
 {
     constexpr int P2 = P * P;
     Scalars* s = dv.sc;
@@ -592,7 +592,9 @@ __global__ void __launch_bounds__(128) k_surface(Dev dv, GasP g, double* out)
 #pragma unroll
     for (int d = 0; d < 3; ++d) n[d] = to_real<T>(dv.ft_normal[idx * 3 + d]);
     T fb = T(0);
-    if (STAGE == 2) {
+    // the flux blender enters the Chandrashekhar and Rusanov-blended schemes only
+    if (STAGE == 2 && (g.isf == PLENS_ISF_CHANDRASHEKHAR || g.isf == PLENS_ISF_RUSANOV_HLLC ||
+                       g.isf == PLENS_ISF_RUSANOV_AUSM_PLUS_UP)) {
         const int64_t c = dv.ft_cell[ti];
         if constexpr (sizeof(T) == 8) {
             double a = (bc >= 0) ? dv.alpha[c] : 0.5 * (dv.alpha[c] + dv.alpha[dv.ft_nbr_cell[ti]]);
@@ -615,7 +617,8 @@ __global__ void __launch_bounds__(128) k_surface(Dev dv, GasP g, double* out)
 #pragma unroll
         for (int v = 0; v < 5; ++v) fl[v] = T(0.5) * (cs[v] + c2[v]);
     } else if (STAGE == 2) {
-        inv_surf_flux(cs, c2, n, gm, g.isf, fb, fl);
+        if constexpr (sizeof(T) == 4) inv_surf_flux_mx(cs, c2, n, gm, g.isf, fb, fl);
+        else inv_surf_flux(cs, c2, n, gm, g.isf, fb, fl);
     } else {
         T f1[5], f2[5];
         dif_flux(cs, av, n, f1);
@@ -1128,7 +1131,8 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                     const T cL[5] = {Cc[nl], Cc[P3 + nl], Cc[2 * P3 + nl], Cc[3 * P3 + nl], Cc[4 * P3 + nl]};
                     const T cR[5] = {Cc[nr], Cc[P3 + nr], Cc[2 * P3 + nr], Cc[3 * P3 + nr], Cc[4 * P3 + nr]};
                     T F[5];
-                    inv_surf_flux(cL, cR, dn, gm, g.isf, fb, F);
+                    if constexpr (sizeof(T) == 4) inv_surf_flux_mx(cL, cR, dn, gm, g.isf, fb, F);
+                    else inv_surf_flux(cL, cR, dn, gm, g.isf, fb, F);
                     const T wl = opW<T>(ops, id - 1), wr = opW<T>(ops, id);
 #pragma unroll
                     for (int v = 0; v < 5; ++v) {

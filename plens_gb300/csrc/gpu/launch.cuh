@@ -3,6 +3,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "surface_mx.cuh"
 #include "volume_mx.cuh"
 
 namespace plens_gpu {
@@ -34,6 +35,12 @@ struct Launch {
     {
         const int64_t n = dv.ntask * P * P;
         const int grid = (int)((n + 127) / 128);
+        if constexpr (sizeof(T) == 4) {
+            if (stage == 2) {  // two face dofs per thread
+                k_surface_inv_mx<P><<<(int)((n + 255) / 256), 128, 0, st>>>(dv, g, out);
+                return 1;
+            }
+        }
         if (stage == 1) k_surface<P, T, 1><<<grid, 128, 0, st>>>(dv, g, out);
         else if (stage == 2) k_surface<P, T, 2><<<grid, 128, 0, st>>>(dv, g, out);
         else k_surface<P, T, 3><<<grid, 128, 0, st>>>(dv, g, out);

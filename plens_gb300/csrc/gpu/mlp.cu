@@ -67,13 +67,13 @@ __device__ __forceinline__ float gelu_d(float x)
 
 // rho*p at the P^3 nodes (vs) -> interpolated to the 4^3 GLL nodes, divided by its mean, minus 1
 // (xs); one warp.
-template <int P>
+template <int P, int XS = 1>
 __device__ void interp_normalise(const Interp& ip, float* vs, float* ts, float* xs)
 {
     constexpr int P2 = P * P;
     const int lane = threadIdx.x & 31;
     if (P == 4) {
-        for (int n = lane; n < 64; n += 32) xs[n] = vs[n];
+        for (int n = lane; n < 64; n += 32) xs[n * XS] = vs[n];
     } else {
         // x: [a][j][k] (a < 4), then y, then z
         for (int n = lane; n < 4 * P2; n += 32) {
@@ -94,17 +94,17 @@ __device__ void interp_normalise(const Interp& ip, float* vs, float* ts, float* 
             const int a = n % 4, b = (n / 4) % 4, cc = n / 16;
             float s = 0;
             for (int k = 0; k < P; ++k) s += ip.I[cc * kMaxP + k] * vs[a + 4 * b + 16 * k];
-            xs[n] = s;
+            xs[n * XS] = s;
         }
     }
     __syncwarp();
-    float m = xs[lane] + xs[lane + 32];
+    float m = xs[lane * XS] + xs[(lane + 32) * XS];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) m += __shfl_xor_sync(0xffffffffu, m, off);
     m *= (1.0f / 64.0f);
     const float inv = 1.0f / m;
-    xs[lane] = xs[lane] * inv - 1.0f;
-    xs[lane + 32] = xs[lane + 32] * inv - 1.0f;
+    xs[lane * XS] = xs[lane * XS] * inv - 1.0f;
+    xs[(lane + 32) * XS] = xs[(lane + 32) * XS] * inv - 1.0f;
     __syncwarp();
 }
 
@@ -145,11 +145,14 @@ __device__ void cell_features(const Dev& dv, double gamma, const Interp& ip, int
     interp_normalise<P>(ip, vs, ts, xs);
 }
 
-// MLP forward of one sample held in xs (shared) by one warp; returns alpha_max*sigmoid(z).
-// W is the parameter vector with W1 and W2 stored transposed ([in][out]) so that the 32 lanes,
-// each computing one output, read consecutive shared-memory words.
-__device__ float mlp_forward_warp(const float* W, const float* xs, float* hs, float amax)
+// MLP forward (W1 and W2 stored transposed, [in][out], so the 32 lanes -- each computing two
+// outputs -- read consecutive shared-memory words) for G cells at once by one warp: the inputs are stored [k][g] so one
+// 16-byte broadcast load feeds the G cells, and each weight read from shared memory serves G
+// multiply-adds (the per-cell form reads one weight per multiply-add).
+template <int G>
+__device__ void mlp_forward_group(const float* W, const float* xs, float* hs, float amax, float out[G])
 {
+    static_assert(G == 4, "inputs are read as float4");
     const int lane = threadIdx.x & 31;
     const float* W1t = W;
     const float* b1 = W1t + kMlpHid * kMlpIn;
@@ -157,31 +160,50 @@ __device__ float mlp_forward_warp(const float* W, const float* xs, float* hs, fl
     const float* b2 = W2t + kMlpHid * kMlpHid;
     const float* w3 = b2 + kMlpHid;
     const float b3 = w3[kMlpHid];
-    float h0 = b1[lane], h1 = b1[lane + 32];
-    for (int k = 0; k < kMlpIn; ++k) {
-        const float xk = xs[k];
-        h0 += W1t[k * kMlpHid + lane] * xk;
-        h1 += W1t[k * kMlpHid + lane + 32] * xk;
-    }
-    __syncwarp();
-    hs[lane] = gelu(h0);
-    hs[lane + 32] = gelu(h1);
-    __syncwarp();
-    float a0 = b2[lane], a1 = b2[lane + 32];
-    for (int k = 0; k < kMlpHid; ++k) {
-        const float hk = hs[k];
-        a0 += W2t[k * kMlpHid + lane] * hk;
-        a1 += W2t[k * kMlpHid + lane + 32] * hk;
-    }
-    float z = w3[lane] * gelu(a0) + w3[lane + 32] * gelu(a1);
+    float h0[G], h1[G];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) z += __shfl_xor_sync(0xffffffffu, z, off);
-    z += b3;
+    for (int g = 0; g < G; ++g) {
+        h0[g] = b1[lane];
+        h1[g] = b1[lane + 32];
+    }
+#pragma unroll 8
+    for (int k = 0; k < kMlpIn; ++k) {
+        const float4 x = *reinterpret_cast<const float4*>(xs + k * G);
+        const float w0 = W1t[k * kMlpHid + lane], w1 = W1t[k * kMlpHid + lane + 32];
+        h0[0] += w0 * x.x; h0[1] += w0 * x.y; h0[2] += w0 * x.z; h0[3] += w0 * x.w;
+        h1[0] += w1 * x.x; h1[1] += w1 * x.y; h1[2] += w1 * x.z; h1[3] += w1 * x.w;
+    }
     __syncwarp();
-    return amax / (1.0f + expf(-z));
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        hs[lane * G + g] = gelu(h0[g]);
+        hs[(lane + 32) * G + g] = gelu(h1[g]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        h0[g] = b2[lane];
+        h1[g] = b2[lane + 32];
+    }
+#pragma unroll 8
+    for (int k = 0; k < kMlpHid; ++k) {
+        const float4 x = *reinterpret_cast<const float4*>(hs + k * G);
+        const float w0 = W2t[k * kMlpHid + lane], w1 = W2t[k * kMlpHid + lane + 32];
+        h0[0] += w0 * x.x; h0[1] += w0 * x.y; h0[2] += w0 * x.z; h0[3] += w0 * x.w;
+        h1[0] += w1 * x.x; h1[1] += w1 * x.y; h1[2] += w1 * x.z; h1[3] += w1 * x.w;
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        float z = w3[lane] * gelu(h0[g]) + w3[lane + 32] * gelu(h1[g]);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) z += __shfl_xor_sync(0xffffffffu, z, off);
+        out[g] = amax / (1.0f + expf(-(z + b3)));
+    }
+    __syncwarp();
 }
 
 constexpr int kWarpsPerBlock = 8;
+constexpr int kGroup = 4;  // cells per warp in one network evaluation
 
 // Learned values below this are set to 0 (the modal indicator's own cut is alpha_min = 1e-3): the
 // network's sigmoid never returns exact zeros, and without a cut the subcell residual would run
@@ -190,7 +212,13 @@ constexpr float kLearnedCut = 0.01f;
 
 // Per-warp shared scratch of the inference kernel (floats): nodal values, interpolation / modal
 // transform buffer, network input, hidden layer.
-constexpr int kScratchV = kMaxP * kMaxP * kMaxP, kScratch = 2 * kScratchV + 64 + 64;
+template <int P>
+struct InferScratch {
+    // nodal values / y-pass output / modal transform buffers, then the group's inputs and hidden layer
+    static constexpr int V0 = P * P * P, V1 = 16 * P, V2 = 4 * P * P;
+    static constexpr int V = ((V0 > V1 ? (V0 > V2 ? V0 : V2) : (V1 > V2 ? V1 : V2)) + 3) / 4 * 4;
+    static constexpr int per_warp = 2 * V + 2 * 64 * kGroup;
+};
 constexpr int kParamsPad = (kMlpParams + 3) / 4 * 4;  // float4 copies
 
 // This cell's FP32 state, the nodes lane, lane + 32, ... of the warp (NPL per lane).
@@ -276,7 +304,7 @@ __device__ float modal_alpha_warp(const Ops& ops, const BlendP& bp, float gm, co
 
 // Network input of one cell from its FP32 state (rho*p at the nodes, interpolated to 4^3 GLL
 // nodes, normalised by the mean), with the positivity assertion of the RHS.
-template <int P, int NPL>
+template <int P, int NPL, int XS = 1>
 __device__ void features_from_state(const Dev& dv, int64_t cell, float gm, const Interp& ip, const float u[NPL][5],
                                     float* vs, float* ts, float* xs)
 {
@@ -295,7 +323,7 @@ __device__ void features_from_state(const Dev& dv, int64_t cell, float gm, const
         }
     }
     __syncwarp();
-    interp_normalise<P>(ip, vs, ts, xs);
+    interp_normalise<P, XS>(ip, vs, ts, xs);
 }
 
 // Fused inference of the modal indicator's value (the blender before neighbour smoothing):
@@ -303,18 +331,18 @@ __device__ void features_from_state(const Dev& dv, int64_t cell, float gm, const
 // plain indicator instead, computed by the same warp. Persistent grid: each warp walks cells
 // with a stride and holds the next cell's state in registers while it evaluates the current one.
 template <int P>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_sensor_infer(Dev dv, const float* __restrict__ Wt, GasP g,
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, (P <= 4 ? 3 : 1)) k_sensor_infer(Dev dv, const float* __restrict__ Wt, GasP g,
                                                                        BlendP bp, Ops ops, Interp ip, double* out,
                                                                        int gated, const uint8_t* mask)
 {
-    constexpr int P3 = P * P * P, NPL = (P3 + 31) / 32;
+    constexpr int P3 = P * P * P, NPL = (P3 + 31) / 32, G = kGroup;
+    using SC = InferScratch<P>;
     extern __shared__ __align__(16) float smem_f[];
     float* sW = smem_f;                                   // [kParamsPad], W1 and W2 transposed
-    float* scr = sW + kParamsPad + (threadIdx.x >> 5) * kScratch;
-    float* sv = scr;
-    float* st = sv + kScratchV;
-    float* sx = st + kScratchV;
-    float* sh = sx + 64;
+    float* sv = sW + kParamsPad + (threadIdx.x >> 5) * SC::per_warp;
+    float* st = sv + SC::V;
+    float* sx = st + SC::V;   // [64][G]
+    float* sh = sx + 64 * G;  // [64][G]
     Scalars* s = dv.sc;
     if (!s->active) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) *dv.lo_count = 0;  // this stage's troubled-cell list
@@ -332,31 +360,50 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_sensor_infer(Dev dv, co
     int64_t cell = (int64_t)blockIdx.x * kWarpsPerBlock + warp;
     float u[NPL][5];
     if (cell < dv.nc) load_cell_f32<P, NPL>(dv, cell, lane, u);
-    for (; cell < dv.nc; cell += stride) {
-        float un[NPL][5];  // next cell's state, in flight during this cell's work
-        if (cell + stride < dv.nc) load_cell_f32<P, NPL>(dv, cell + stride, lane, un);
-        float at;
-        if (mask && mask[cell]) {
-            features_from_state<P, NPL>(dv, cell, gm, ip, u, sv, st, sx);  // positivity check
-            at = modal_alpha_warp<P, NPL>(ops, bp, gm, u, sv, st);
-        } else {
-            features_from_state<P, NPL>(dv, cell, gm, ip, u, sv, st, sx);
-            at = mlp_forward_warp(sW, sx, sh, amax);
-            if (at < cut) at = 0.0f;
-        }
-        if (lane == 0) {
-            double a = f32_to_f64(at);
-            if (dv.cell_wall[cell]) {
-                const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
-                a = (wl > a) ? wl : a;
+    while (cell < dv.nc) {
+        // G cells of this warp's sequence: inputs (and the plain indicator of handed-back cells)
+        int64_t cg[G];
+        float am[G];
+        bool mk[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            cg[g] = cell;
+            mk[g] = false;
+            am[g] = 0.0f;
+            if (cell < dv.nc) {
+                float un[NPL][5];  // next cell's state, in flight during this cell's work
+                if (cell + stride < dv.nc) load_cell_f32<P, NPL>(dv, cell + stride, lane, un);
+                features_from_state<P, NPL, G>(dv, cell, gm, ip, u, sv, st, sx + g);
+                if (mask && mask[cell]) {
+                    mk[g] = true;
+                    am[g] = modal_alpha_warp<P, NPL>(ops, bp, gm, u, sv, st);
+                }
+#pragma unroll
+                for (int j = 0; j < NPL; ++j)
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) u[j][v] = un[j][v];
+            } else {
+                sx[lane * G + g] = 0.0f;
+                sx[(lane + 32) * G + g] = 0.0f;
+                __syncwarp();
             }
-            out[cell] = a;
+            cell += stride;
+        }
+        float at[G];
+        mlp_forward_group<G>(sW, sx, sh, amax, at);
+        if (lane == 0) {
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                if (cg[g] >= dv.nc) continue;
+                double a = mk[g] ? f32_to_f64(am[g]) : ((at[g] < cut) ? 0.0 : f32_to_f64(at[g]));
+                if (dv.cell_wall[cg[g]]) {
+                    const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
+                    a = (wl > a) ? wl : a;
+                }
+                out[cg[g]] = a;
+            }
         }
         __syncwarp();
-#pragma unroll
-        for (int j = 0; j < NPL; ++j)
-#pragma unroll
-            for (int v = 0; v < 5; ++v) u[j][v] = un[j][v];
     }
 }
 
@@ -424,7 +471,7 @@ int launch_infer(const Dev& dv, const float* Wt, const GasP& g, const BlendP& bp
                  int gated, const uint8_t* mask, cudaStream_t st)
 {
     const Interp ip = make_interp(P);
-    const size_t bytes = sizeof(float) * (kParamsPad + kWarpsPerBlock * kScratch);
+    const size_t bytes = sizeof(float) * (kParamsPad + kWarpsPerBlock * InferScratch<P>::per_warp);
     static int per_sm = 0;
     if (!per_sm) {
         cudaFuncSetAttribute(k_sensor_infer<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);

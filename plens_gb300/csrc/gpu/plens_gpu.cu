@@ -164,6 +164,12 @@ struct plens_ctx {
     size_t ev_used = 0;
     double vol_ms = 0;
     int64_t vol_n = 0;
+    // one RK step captured as a CUDA graph and replayed (two variants with the learned sensor:
+    // without and with the judge); rebuilt when the end time changes
+    cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+    int64_t step_graph_launches[2] = {0, 0};
+    double step_graph_end = 0;
+    bool use_graphs = true;
 };
 
 namespace {
@@ -550,6 +556,8 @@ int plens_gpu_destroy(plens_ctx* c)
         cudaEventDestroy(pr.first);
         cudaEventDestroy(pr.second);
     }
+    for (auto& gx : c->step_graph)
+        if (gx) cudaGraphExecDestroy(gx);
     for (void* p : c->allocs) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -632,12 +640,65 @@ int plens_gpu_time_step(plens_ctx* c, double* dt_out)
     return 0;
 }
 
+namespace {
+
+// One step through its CUDA graph: the launch sequence of a step is the same every step (the
+// kernels read time, dt and the sensor state from device scalars), so it is captured once per
+// variant and replayed; the host-side judge schedule of the learned sensor picks the variant.
+int graph_step(plens_ctx* c, double end_time)
+{
+    if (c->step_graph_end != end_time) {
+        for (auto& gx : c->step_graph)
+            if (gx) {
+                cudaGraphExecDestroy(gx);
+                gx = nullptr;
+            }
+        c->step_graph_end = end_time;
+    }
+    bool judged = false;
+    if (c->learned) {
+        mlp_step_begin(c->mlp, c->dv, c->prm.judge_every, c->stream);
+        judged = c->mlp.judge_this_step;
+    }
+    const int v = judged ? 1 : 0;
+    if (!c->step_graph[v]) {
+        cudaGraph_t g = nullptr;
+        const int64_t l0 = c->launches;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+        const int r = launch_step(c, end_time, false);
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (r) {
+            if (g) cudaGraphDestroy(g);
+            return r;
+        }
+        if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+        const cudaError_t e2 = cudaGraphInstantiate(&c->step_graph[v], g, 0);
+        cudaGraphDestroy(g);
+        if (e2 != cudaSuccess) return cuda_fail(c, e2, "cudaGraphInstantiate");
+        c->step_graph_launches[v] = c->launches - l0;
+        c->launches = l0;
+    }
+    if (c->learned) c->mlp.judge_this_step = false;
+    CK(cudaGraphLaunch(c->step_graph[v], c->stream));
+    c->launches += c->step_graph_launches[v];
+    return 0;
+}
+
+int run_step(plens_ctx* c, double end_time)
+{
+    // graphs need the launch sequence to be fixed: not while volume-kernel events are recorded
+    if (c->use_graphs && !c->timing) return graph_step(c, end_time);
+    return launch_step(c, end_time);
+}
+
+}  // namespace
+
 int plens_gpu_advance_async(plens_ctx* c, int64_t n_steps, double end_time)
 {
     if (!c || !c->dv.U || n_steps < 0) return PLENS_GPU_E_INVALID;
     if (c->learned && !c->mlp.weights_set) return fail(c, PLENS_GPU_E_INVALID, "learned sensor: weights not set");
     for (int64_t s = 0; s < n_steps; ++s)
-        if (int r = launch_step(c, end_time)) return r;
+        if (int r = run_step(c, end_time)) return r;
     return 0;
 }
 
@@ -666,7 +727,7 @@ int plens_gpu_advance(plens_ctx* c, int64_t n_steps, double end_time)
             const int64_t nb = std::min<int64_t>(kBatch, n_steps - done);
             const int counter0 = c->mlp.step_counter;
             for (int64_t k = 0; k < nb; ++k)
-                if (int r = launch_step(c, end_time)) return r;
+                if (int r = run_step(c, end_time)) return r;
             const int r = sync_and_check(c);
             if (r != PLENS_GPU_E_POSITIVITY) {
                 if (r) return r;

@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                     const float cL[5] = {Cc[nl], Cc[P3 + nl], Cc[2 * P3 + nl], Cc[3 * P3 + nl], Cc[4 * P3 + nl]};
                     const float cR[5] = {Cc[nr], Cc[P3 + nr], Cc[2 * P3 + nr], Cc[3 * P3 + nr], Cc[4 * P3 + nr]};
                     float F[5];
-                    inv_surf_flux(cL, cR, dn, gm, g.isf, fb, F);
+                    inv_surf_flux_mx(cL, cR, dn, gm, g.isf, fb, F);
                     const float wl = __fdividef(nn, opW<float>(ops, id - 1)), wr = __fdividef(nn, opW<float>(ops, id));
 #pragma unroll
                     for (int v = 0; v < 5; ++v) {
