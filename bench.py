@@ -162,14 +162,27 @@ def _spec(workload: str, precision: str, sensor: str):
     raise ValueError(workload)
 
 
+def _form_case(workload: str, precision: str, sensor: str, cache: dict | None = None):
+    """The workload's Case with the form's precision and sensor. With a cache, the mesh, metric
+    terms and initial state are built once per workload and only the two parameters change."""
+    from plens_gb300 import configs
+    if cache is None:
+        return configs.make_case(_spec(workload, precision, sensor))
+    if workload not in cache:
+        cache[workload] = configs.make_case(_spec(workload, "fp64", "modal"))
+    case = cache[workload]
+    case.params.precision = 1 if precision == "mixed" else 0
+    case.params.sensor = 1 if sensor == "learned" else 0
+    return case
+
+
 def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_index: int, weights=None,
-                 workload: str = "dmr"):
+                 workload: str = "dmr", cache: dict | None = None):
     import torch
 
-    from plens_gb300 import configs
     from plens_gb300.api import GpuSolver
 
-    case = configs.make_case(_spec(workload, precision, sensor))
+    case = _form_case(workload, precision, sensor, cache)
     U0 = case.initial_state()
     g = GpuSolver(case)
     if sensor == "learned":
@@ -272,8 +285,9 @@ WORKLOADS = {
     # the config runs to t = 0.2, but every form (FP64 included, as the FP64 oracle) stops there
     # on the positivity assertion first: the window is fixed, and `horizon` reports where the FP32
     # form stops
-    "dmr": {"acc_steps": 1000, "acc_end": None, "oracle_steps": 100,
-            "note": "first 1000 steps (the config's t = 0.2 is not reached, see horizon)", "horizon": 0.2},
+    "dmr": {"acc_steps": 1000, "acc_end": None, "oracle_steps": 100, "windows": [100, 300, 1000],
+            "note": "first 100, 300 and 1000 steps (the config's t = 0.2 is not reached, see horizon)",
+            "horizon": 0.2},
     "cylinder": {"acc_steps": 1000, "acc_end": None, "oracle_steps": 10,
                  "note": "first 1000 of the config's 20000 steps"},
     "shock_vortex": {"acc_steps": 20, "acc_end": None, "oracle_steps": 1,
@@ -302,35 +316,52 @@ def run_workload_report(args):
         forms.append(("fp32_learned", "mixed", "learned"))
     out = {"workload": args.workload, "accuracy_window": wl["note"] if not args.accuracy_steps else f"{acc_steps} steps"}
     states = {}
+    windows = [acc_steps] if args.accuracy_steps else wl.get("windows", [acc_steps])
+    cache = {}
     for name, prec, sensor in forms:
-        r = measure_form(prec, sensor, args.steps, args.warmup, 0, weights, workload=args.workload)
+        r = measure_form(prec, sensor, args.steps, args.warmup, 0, weights, workload=args.workload, cache=cache)
         nd = r["case"].n_dofs
         out[name] = {"dof_stage_per_s": nd * 5 * args.steps / (r["ms"] / 1e3), "ms_per_step": r["ms"] / args.steps,
                      "volume_kernel_ms": r["vol_ms"] / max(r["vol_n"], 1), "n_dofs": nd, "clocks": r["clocks"]}
-        case = configs.make_case(_spec(args.workload, prec, sensor))
+    # accuracy: every form from the initial condition, states kept at each window; the FP64 form
+    # once more from an initial density perturbed by 1e-12 (relative) measures how fast the flow
+    # itself amplifies a perturbation over the same windows
+    runs = [(n, p_, s_, False) for n, p_, s_ in forms] + [("fp64_perturbed_1e-12", "fp64", "modal", True)]
+    for name, prec, sensor, perturb in runs:
+        case = _form_case(args.workload, prec, sensor, cache)
         g = GpuSolver(case)
         if sensor == "learned":
             g.set_sensor_weights(weights)
-        g.set_state(case.initial_state(), case.start_time)
+        U0 = case.initial_state()
+        if perturb:
+            rng = np.random.default_rng(7)
+            U0[0] *= 1 + 1e-12 * rng.uniform(-1, 1, U0.shape[1])
+        g.set_state(U0, case.start_time)
         t0 = time.perf_counter()
+        rec = out.setdefault(name, {})
         try:
-            g.advance(acc_steps, end)
-            states[name] = g.get_state()
+            done = 0
+            for w in windows:
+                g.advance(w - done, end)
+                done = w
+                states[(name, w)] = g.get_state()
             t, n, _ = g.get_time()
-            out[name]["accuracy_run"] = {"steps": n, "seconds": time.perf_counter() - t0, "t_end": t}
+            rec["accuracy_run"] = {"steps": n, "seconds": time.perf_counter() - t0, "t_end": t}
         except PlensError as e:
-            out[name]["accuracy_run"] = {"error": str(e)}
+            rec["accuracy_run"] = {"error": str(e)}
         if sensor == "learned":
             st = g.sensor_stats()
             st["fallback_rate"] = st["fallbacks"] / max(st["judged"] * case.n_cells, 1)
-            out[name]["accuracy_run"]["sensor_stats"] = st
+            rec["accuracy_run"]["sensor_stats"] = st
         g.close()
-    for name in ("fp32_modal", "fp32_learned"):
-        if name in states and "fp64_plain" in states:
-            out[name]["rel_l1_vs_fp64"] = dict(zip(("rho", "momentum", "rhoE"), _rel_l1(states[name], states["fp64_plain"])))
+    for name in ("fp32_modal", "fp32_learned", "fp64_perturbed_1e-12"):
+        for w in windows:
+            if (name, w) in states and ("fp64_plain", w) in states:
+                out[name].setdefault("rel_l1_vs_fp64", {})[f"{w}_steps"] = dict(
+                    zip(("rho", "momentum", "rhoE"), _rel_l1(states[(name, w)], states[("fp64_plain", w)])))
     if wl.get("horizon"):
         # how far the FP32 modal form gets towards the configuration's end time
-        case = configs.make_case(_spec(args.workload, "mixed", "modal"))
+        case = _form_case(args.workload, "mixed", "modal", cache)
         g = GpuSolver(case)
         g.set_state(case.initial_state(), case.start_time)
         t0 = time.perf_counter()
@@ -350,7 +381,7 @@ def run_workload_report(args):
         out["horizon_fp32_modal"] = h
         g.close()
     # the FP64 form against the oracle at full size
-    case = configs.make_case(_spec(args.workload, "fp64", "modal"))
+    case = _form_case(args.workload, "fp64", "modal", cache)
     o = Oracle(case)
     o.set_state(case.initial_state(), case.start_time)
     t0 = time.perf_counter()
@@ -405,9 +436,11 @@ def main():
         barrier()
 
     weights = _sensor_weights()
-    plain = measure_form("fp64", "modal", args.steps, args.warmup, device.index)
-    modal = measure_form("mixed", "modal", args.steps, args.warmup, device.index)
-    learned = measure_form("mixed", "learned", args.steps, args.warmup, device.index, weights) if weights is not None else None
+    cache = {}
+    plain = measure_form("fp64", "modal", args.steps, args.warmup, device.index, cache=cache)
+    modal = measure_form("mixed", "modal", args.steps, args.warmup, device.index, cache=cache)
+    learned = (measure_form("mixed", "learned", args.steps, args.warmup, device.index, weights, cache=cache)
+               if weights is not None else None)
     fast = learned if learned is not None else modal
     fast_sensor = "learned" if learned is not None else "modal"
 

@@ -234,6 +234,15 @@ int plens_gpu_synchronize(plens_ctx* ctx);
 int plens_gpu_get_cell_scalars(plens_ctx* ctx, double* alpha, double* alpha_d, double* dt_cell);
 /* Auxiliary variables of the last viscous RHS ([9][ndof]): PLENS::gcrk_avars. */
 int plens_gpu_get_avars(plens_ctx* ctx, double* avars);
+/* Asynchronous snapshot for data output (replaces the host reads of PLENS::write,
+ * dgsem/plens.cc:4170-4322): _begin copies U, alpha, alpha_d, the auxiliary variables (viscous)
+ * and the clock on the context's stream into a device buffer, then to library-owned pinned host
+ * memory on a second stream, and returns at once -- steps launched after it overlap the copy.
+ * _end waits for that copy and hands the snapshot out (any pointer may be NULL; avars [9][ndof]).
+ * One snapshot may be pending at a time. */
+int plens_gpu_snapshot_begin(plens_ctx* ctx);
+int plens_gpu_snapshot_end(plens_ctx* ctx, double* U, double* alpha, double* alpha_d, double* avars,
+                           double* time, int64_t* n_steps, double* dt);
 /* First dof that failed the positivity check of the last failing call (-1 if none). */
 int plens_gpu_first_bad_dof(const plens_ctx* ctx, int64_t* dof);
 /* Self-test of the mixed form's integer-pipe FP64 <-> FP32 conversions (no reference

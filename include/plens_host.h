@@ -43,6 +43,24 @@ double plens_case_eval_expr(const plens_case* c, int32_t idx, double x, double y
 /* All parameters with their values (ParameterHandler::print_parameters); valid until destroy. */
 const char* plens_case_prm_echo(const plens_case* c);
 
+/* Data output of PLENS::write (dgsem/plens.cc:4170-4322) with post_process (3950-3963): a VTK XML
+ * unstructured grid of the case's mesh (each cell's GLL nodes as points, N^3 linear sub-hexahedra)
+ * with txx..qz (if avars is not NULL), rho, p, T, u, v, w as point data and subdomain, alpha,
+ * alpha_d, loc_dt, global_active_cell_index as cell data. U: [5][ndof]; avars: [9][ndof] or NULL;
+ * alpha, alpha_d: [n_cells] or NULL. Returns 0, or 1 with plens_case_last_error set. */
+int plens_write_vtu(const plens_case* c, const char* path, const double* U, const double* avars,
+                    const double* alpha, const double* alpha_d, double loc_dt);
+/* ParaView collection record (DataOutBase::write_pvd_record) of n (time, file) pairs. */
+int plens_write_pvd(const char* path, int64_t n, const double* times, const char* const* files);
+/* Restart archive of the state (replaces the SolutionTransfer archives that the reference's
+ * "from archive restart" initial condition reads, IBCs/from_archive_restart.cc:23-73): this
+ * build's own format -- a header (magic, degree, cells, dofs, steps, output counter, time) and
+ * U [5][ndof] in FP64. The "from archive restart" IC type of input.prm reads it back. */
+int plens_write_archive(const plens_case* c, const char* path, const double* U, double time, int64_t n_steps,
+                        int64_t output_counter);
+int plens_read_archive(const plens_case* c, const char* path, double* U, double* time, int64_t* n_steps,
+                       int64_t* output_counter);
+
 /* Stand-alone helpers for the known-answer tests. */
 int plens_expr_eval_string(const char* src, double x, double y, double z, double t, double* out);
 int plens_gll_1d(int n_points, double* nodes, double* weights);

@@ -124,6 +124,10 @@ def host_lib() -> C.CDLL:
         L.plens_case_prm_echo.restype = C.c_char_p
         L.plens_expr_eval_string.argtypes = [C.c_char_p, dbl, dbl, dbl, dbl, C.POINTER(dbl)]
         L.plens_gll_1d.argtypes = [C.c_int, vp, vp]
+        L.plens_write_vtu.argtypes = [vp, C.c_char_p, vp, vp, vp, vp, dbl]
+        L.plens_write_pvd.argtypes = [C.c_char_p, i64, vp, C.POINTER(C.c_char_p)]
+        L.plens_write_archive.argtypes = [vp, C.c_char_p, vp, dbl, i64, i64]
+        L.plens_read_archive.argtypes = [vp, C.c_char_p, vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(i64)]
         _host = L
     return _host
 
@@ -161,6 +165,8 @@ def gpu_lib() -> C.CDLL:
         L.plens_gpu_mlp_loss_grad.argtypes = [vp, vp, i64, vp, C.c_float, C.POINTER(C.c_float), vp]
         L.plens_gpu_mlp_infer.argtypes = [vp, i64, vp, C.c_float, vp]
         L.plens_gpu_selftest_conversions.argtypes = [i64, C.c_uint64, C.POINTER(i64)]
+        L.plens_gpu_snapshot_begin.argtypes = [vp]
+        L.plens_gpu_snapshot_end.argtypes = [vp, vp, vp, vp, vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(dbl)]
         L.plens_gpu_set_kernel_timing.argtypes = [vp, C.c_int]
         L.plens_gpu_kernel_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(i64)]
         _gpu = L
@@ -248,6 +254,36 @@ class Case:
 
     def prm_echo(self) -> str:
         return self._L.plens_case_prm_echo(self._h).decode()
+
+    def _hcheck(self, rc: int):
+        if rc != 0:
+            raise PlensError(self._L.plens_case_last_error().decode())
+
+    def write_vtu(self, path, U, avars=None, alpha=None, alpha_d=None, loc_dt=0.0):
+        """PLENS::write of one snapshot: a .vtu of the GLL nodes with rho, p, T, u, v, w (and the
+        auxiliary variables), alpha, alpha_d and loc_dt as cell data."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None for a in (U, avars, alpha, alpha_d)]
+        ptrs = [_ptr(a) if a is not None else None for a in arrs]
+        self._hcheck(self._L.plens_write_vtu(self._h, str(path).encode(), ptrs[0], ptrs[1], ptrs[2], ptrs[3], loc_dt))
+
+    def write_archive(self, path, U, time: float, n_steps: int = 0, output_counter: int = 0):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        self._hcheck(self._L.plens_write_archive(self._h, str(path).encode(), _ptr(U), time, n_steps, output_counter))
+
+    def read_archive(self, path):
+        U = np.empty((5, self.n_dofs), dtype=np.float64)
+        t, n, k = C.c_double(), C.c_int64(), C.c_int64()
+        self._hcheck(self._L.plens_read_archive(self._h, str(path).encode(), _ptr(U), C.byref(t), C.byref(n), C.byref(k)))
+        return U, t.value, n.value, k.value
+
+
+def write_pvd(path, entries):
+    """ParaView collection record of (time, file name) pairs."""
+    L = host_lib()
+    times = np.array([e[0] for e in entries], dtype=np.float64)
+    names = (C.c_char_p * max(len(entries), 1))(*[str(e[1]).encode() for e in entries])
+    if L.plens_write_pvd(str(path).encode(), len(entries), _ptr(times), names) != 0:
+        raise PlensError(L.plens_case_last_error().decode())
 
 
 def eval_expression(src: str, x=0.0, y=0.0, z=0.0, t=0.0) -> float:
@@ -373,6 +409,20 @@ class GpuSolver:
         e = C.c_double()
         self._check(self.L.plens_gpu_sensor_stats(self.h, C.byref(j), C.byref(f), C.byref(e), C.byref(lo)), "sensor_stats")
         return {"judged": j.value, "fallbacks": f.value, "max_alpha_err": e.value, "lo_cells_last": lo.value}
+
+    def snapshot_begin(self):
+        """Start an asynchronous snapshot (state, alpha, alpha_d, auxiliary variables, clock)."""
+        self._check(self.L.plens_gpu_snapshot_begin(self.h), "snapshot_begin")
+
+    def snapshot_end(self) -> dict:
+        U = np.empty((5, self.n_dofs))
+        a = np.empty(self.n_cells)
+        ad = np.empty(self.n_cells)
+        av = np.empty((9, self.n_dofs))
+        t, n, dt = C.c_double(), C.c_int64(), C.c_double()
+        self._check(self.L.plens_gpu_snapshot_end(self.h, _ptr(U), _ptr(a), _ptr(ad), _ptr(av), C.byref(t),
+                                                  C.byref(n), C.byref(dt)), "snapshot_end")
+        return {"U": U, "alpha": a, "alpha_d": ad, "avars": av, "time": t.value, "n_steps": n.value, "dt": dt.value}
 
     def sensor_pairs(self):
         x = np.empty((self.n_cells, 64), dtype=np.float32)

@@ -26,9 +26,9 @@ BUILD = PKG / "_build"
 INCLUDE = ROOT / "include"
 
 GENCODE = "arch=compute_103a,code=sm_103a"
-CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
+CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall", "-Wno-unused-function"]
 
-HOST_SRCS = ["host/expr_compile.cpp", "host/prm.cpp", "host/setup.cpp", "host/capi.cpp"]
+HOST_SRCS = ["host/expr_compile.cpp", "host/prm.cpp", "host/setup.cpp", "host/output.cpp", "host/capi.cpp"]
 GPU_SRCS = ["gpu/plens_gpu.cu", "gpu/mlp.cu", "gpu/noalloc.cu"]
 # kernels_inst.cu is compiled once per (P, precision)
 GPU_INST = [(P, prec) for P in (2, 3, 4, 5, 6) for prec in ("fp64", "mixed")]
@@ -89,7 +89,7 @@ def build_host() -> Path:
         "host",
     )
     if _newer(out, objs):
-        _run(["g++", "-shared", "-o", str(out), *map(str, objs)])
+        _run(["g++", "-shared", "-fopenmp", "-o", str(out), *map(str, objs)])
     return out
 
 
@@ -142,7 +142,7 @@ def build_driver() -> Path:
     )
     libs = [LIB / "libplens_host.so", LIB / "libplens_gpu.so"]
     if _newer(out, objs + libs):
-        _run(["g++", "-o", str(out), *map(str, objs), f"-L{LIB}", "-lplens_host", "-lplens_gpu",
+        _run(["g++", "-fopenmp", "-o", str(out), *map(str, objs), f"-L{LIB}", "-lplens_host", "-lplens_gpu",
               f"-Wl,-rpath,{LIB}"])
     return out
 

@@ -356,6 +356,23 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_blender(Dev dv, Ops o
     }
 }
 
+// the rest of the smoothing of one cell after the neighbour max: TV filter, alpha, alpha_d and the
+// troubled-cell list
+__device__ __forceinline__ void smooth_finish(const Dev& dv, const BlendP& bp, Scalars* s, int64_t c, double& a)
+{
+    if (bp.do_filter && !(a > bp.amin)) {
+        const double asum = dv.tvstat[c], ub = dv.tvstat[dv.nc + c], tl = dv.tvstat[2 * dv.nc + c];
+        if (!(ub < 1e-2 * asum)) a = a + (bp.amax - a) * (1 - tl / ub);
+    }
+    dv.alpha[c] = a;
+    const double* x = dv.center + 3 * c;
+    dv.alpha_d[c] = (eval_expr(dv, bp.expr_vis, x[0], x[1], x[2], s->time) > 0) ? ((1.0 < a / bp.amax) ? 1.0 : a / bp.amax) : 0.0;
+    if (dv.lo_list && a > 0) {  // compacted troubled-cell list (learned-sensor contexts)
+        const int k = atomicAdd(dv.lo_count, 1);
+        dv.lo_list[k] = (int32_t)c;
+    }
+}
+
 // neighbour smoothing over interior faces against the pre-smoothing values, optional TV filter
 // and alpha_d (dgsem/plens.cc:2926-2961, blender_calculator.cc:196-259)
 static __global__ void k_alpha_smooth(Dev dv, BlendP bp)
@@ -373,17 +390,7 @@ static __global__ void k_alpha_smooth(Dev dv, BlendP bp)
         const double h = 0.5 * dv.alpha_raw[nb];
         a = (h > a) ? h : a;
     }
-    if (bp.do_filter && !(a > bp.amin)) {
-        const double asum = dv.tvstat[c], ub = dv.tvstat[dv.nc + c], tl = dv.tvstat[2 * dv.nc + c];
-        if (!(ub < 1e-2 * asum)) a = a + (bp.amax - a) * (1 - tl / ub);
-    }
-    dv.alpha[c] = a;
-    const double* x = dv.center + 3 * c;
-    dv.alpha_d[c] = (eval_expr(dv, bp.expr_vis, x[0], x[1], x[2], s->time) > 0) ? ((1.0 < a / bp.amax) ? 1.0 : a / bp.amax) : 0.0;
-    if (dv.lo_list && a > 0) {  // compacted troubled-cell list (learned-sensor contexts)
-        const int k = atomicAdd(dv.lo_count, 1);
-        dv.lo_list[k] = (int32_t)c;
-    }
+    smooth_finish(dv, bp, s, c, a);
 }
 
 // --------------------------------------------------------------------------- BC ghosts

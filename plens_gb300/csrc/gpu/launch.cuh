@@ -36,8 +36,17 @@ struct Launch {
         const int64_t n = dv.ntask * P * P;
         const int grid = (int)((n + 127) / 128);
         if constexpr (sizeof(T) == 4) {
-            if (stage == 2) {  // two face dofs per thread
-                k_surface_inv_mx<P><<<(int)((n + 255) / 256), 128, 0, st>>>(dv, g, out);
+            if (stage == 2) {  // persistent, software-pipelined
+                static int blocks = 0;
+                if (!blocks) {
+                    int dev = 0, nsm = 0, occ = 0;
+                    cudaGetDevice(&dev);
+                    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_surface_inv_mx<P>, 128, 0);
+                    blocks = (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
+                }
+                const int64_t need = (n + 127) / 128;
+                k_surface_inv_mx<P><<<(int)(need < blocks ? need : blocks), 128, 0, st>>>(dv, g, out);
                 return 1;
             }
         }

@@ -579,7 +579,8 @@ int mlp_set_weights(MlpDevice& m, const float* host_params, cudaStream_t st)
     return 0;
 }
 
-int mlp_sensor_launch(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, int P, cudaStream_t st)
+int mlp_sensor_launch(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, int P,
+                      cudaStream_t st)
 {
     switch (P) {
     case 2: return sensor_stage<2>(m, dv, ops, g, bp, st);

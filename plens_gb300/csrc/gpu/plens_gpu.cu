@@ -170,6 +170,14 @@ struct plens_ctx {
     int64_t step_graph_launches[2] = {0, 0};
     double step_graph_end = 0;
     bool use_graphs = true;
+    // asynchronous snapshot: device copy on the compute stream, device -> pinned host copy on a
+    // second stream while later steps run
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
+    unsigned char* snap_dev = nullptr;
+    unsigned char* snap_host = nullptr;
+    size_t snap_bytes = 0;
+    bool snap_pending = false;
 };
 
 namespace {
@@ -558,6 +566,12 @@ int plens_gpu_destroy(plens_ctx* c)
     }
     for (auto& gx : c->step_graph)
         if (gx) cudaGraphExecDestroy(gx);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    if (c->snap_host) cudaFreeHost(c->snap_host);
+    if (c->snap_dev) cudaFree(c->snap_dev);
+    if (c->snap_ready) cudaEventDestroy(c->snap_ready);
+    if (c->snap_done) cudaEventDestroy(c->snap_done);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     for (void* p : c->allocs) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -836,6 +850,73 @@ int plens_gpu_selftest_conversions(int64_t n, uint64_t seed, int64_t* mismatches
     cudaFree(d);
     if (e != cudaSuccess) return PLENS_GPU_E_CUDA;
     *mismatches = (int64_t)h;
+    return 0;
+}
+
+namespace {
+// snapshot layout: U [5][nd] f64 | alpha [nc] f64 | alpha_d [nc] f64 | avars (viscous: [9][nd] in
+// the form's storage type) | Scalars
+size_t snap_off_avars(const plens_ctx* c) { return sizeof(double) * (5 * c->nd + 2 * c->nc); }
+size_t snap_avars_bytes(const plens_ctx* c)
+{
+    return c->viscous ? (c->mixed ? sizeof(float) : sizeof(double)) * 9 * c->nd : 0;
+}
+size_t snap_off_scalars(const plens_ctx* c) { return (snap_off_avars(c) + snap_avars_bytes(c) + 15) / 16 * 16; }
+}  // namespace
+
+int plens_gpu_snapshot_begin(plens_ctx* c)
+{
+    if (!c || !c->dv.U) return PLENS_GPU_E_INVALID;
+    if (c->snap_pending) return fail(c, PLENS_GPU_E_INVALID, "a snapshot is already pending");
+    if (!c->snap_dev) {
+        c->snap_bytes = snap_off_scalars(c) + sizeof(Scalars);
+        CK(cudaMalloc(&c->snap_dev, c->snap_bytes));
+        CK(cudaMallocHost(&c->snap_host, c->snap_bytes));
+        CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->snap_ready, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->snap_done, cudaEventDisableTiming));
+    }
+    cudaStream_t st = c->stream;
+    unsigned char* d = c->snap_dev;
+    CK(cudaMemcpyAsync(d, c->dv.U, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(d + sizeof(double) * 5 * c->nd, c->dv.alpha, sizeof(double) * c->nc, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(d + sizeof(double) * (5 * c->nd + c->nc), c->dv.alpha_d, sizeof(double) * c->nc,
+                       cudaMemcpyDeviceToDevice, st));
+    if (c->viscous)
+        CK(cudaMemcpyAsync(d + snap_off_avars(c), c->dv.avars, snap_avars_bytes(c), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(d + snap_off_scalars(c), c->sc, sizeof(Scalars), cudaMemcpyDeviceToDevice, st));
+    CK(cudaEventRecord(c->snap_ready, st));
+    CK(cudaStreamWaitEvent(c->copy_stream, c->snap_ready, 0));
+    CK(cudaMemcpyAsync(c->snap_host, c->snap_dev, c->snap_bytes, cudaMemcpyDeviceToHost, c->copy_stream));
+    CK(cudaEventRecord(c->snap_done, c->copy_stream));
+    c->snap_pending = true;
+    return 0;
+}
+
+int plens_gpu_snapshot_end(plens_ctx* c, double* U, double* alpha, double* alpha_d, double* avars, double* time,
+                           int64_t* n_steps, double* dt)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    if (!c->snap_pending) return fail(c, PLENS_GPU_E_INVALID, "no snapshot pending");
+    c->snap_pending = false;
+    CK(cudaEventSynchronize(c->snap_done));
+    const unsigned char* h = c->snap_host;
+    if (U) std::memcpy(U, h, sizeof(double) * 5 * c->nd);
+    if (alpha) std::memcpy(alpha, h + sizeof(double) * 5 * c->nd, sizeof(double) * c->nc);
+    if (alpha_d) std::memcpy(alpha_d, h + sizeof(double) * (5 * c->nd + c->nc), sizeof(double) * c->nc);
+    if (avars && c->viscous) {
+        if (c->mixed) {
+            const float* f = reinterpret_cast<const float*>(h + snap_off_avars(c));
+            for (int64_t i = 0; i < 9 * c->nd; ++i) avars[i] = f[i];
+        } else {
+            std::memcpy(avars, h + snap_off_avars(c), sizeof(double) * 9 * c->nd);
+        }
+    }
+    Scalars sc;
+    std::memcpy(&sc, h + snap_off_scalars(c), sizeof(sc));
+    if (time) *time = sc.time;
+    if (n_steps) *n_steps = sc.n_steps;
+    if (dt) *dt = sc.dt;
     return 0;
 }
 

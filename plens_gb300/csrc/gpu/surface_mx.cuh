@@ -1,75 +1,101 @@
 // surface_mx.cuh -- the mixed form's inviscid face-flux kernel (calc_surf_flux stage 2,
-// dgsem/plens.cc:1717-1913): k_surface<P, float, 2> with two face dofs per thread. The kernel is
-// bound by the latency of its gathers (the two states of a face dof are found through the
-// precomputed dof tables), so each thread first issues the loads of both of its face dofs and
-// then evaluates both fluxes.
+// dgsem/plens.cc:1717-1913): the work of k_surface<P, float, 2> as a persistent, software-
+// pipelined loop. The kernel is bound by the latency of its gathers: a face dof's two states are
+// found through the precomputed dof tables (a dependent load), so each thread keeps two face dofs
+// in flight -- the tables of the face dof after next and the states of the next one are loading
+// while it evaluates the current one.
 #pragma once
 
 #include "kernels.cuh"
 
 namespace plens_gpu {
 
-template <int P>
-__global__ void __launch_bounds__(128, 6) k_surface_inv_mx(Dev dv, GasP g, double* out)
+// per face dof: what the loop carries between iterations
+struct FaceItem {
+    int64_t idx;     // face dof of the task list (-1: none)
+    int32_t gd, gdn; // own dof, other dof (interior or periodic partner; -1 for other BCs)
+    int32_t bc;
+    int32_t slot, slot_nb;  // face slots of both sides (-1: no neighbour slot)
+    float n[3];
+};
+
+__device__ __forceinline__ FaceItem face_item(const Dev& dv, int64_t idx, int64_t total, int P2)
 {
-    constexpr int P2 = P * P, K = 2;
+    FaceItem it;
+    it.idx = (idx < total) ? idx : -1;
+    if (it.idx >= 0) {
+        it.gd = dv.fd_own[idx];
+        it.gdn = dv.fd_nbr[idx];
+        it.bc = dv.ft_bc[idx / P2];
+        it.slot = dv.fs_own[idx];
+        it.slot_nb = dv.fs_nbr[idx];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) it.n[d] = f64_to_f32(dv.ft_normal[idx * 3 + d]);
+    }
+    return it;
+}
+
+__device__ __forceinline__ void face_states(const Dev& dv, const FaceItem& it, float cs[5], float c2[5])
+{
+    if (it.idx < 0) return;
+    load_state<float>(dv, it.gd, cs);
+    if (it.gdn >= 0) load_state<float>(dv, it.gdn, c2);
+}
+
+template <int P>
+__global__ void __launch_bounds__(128, 4) k_surface_inv_mx(Dev dv, GasP g, double* out)
+{
+    constexpr int P2 = P * P;
     Scalars* s = dv.sc;
     if (!s->active) return;
     const int64_t total = dv.ntask * P2;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const float gm = f64_to_f32(g.gamma);
     const bool blended = g.isf == PLENS_ISF_CHANDRASHEKHAR || g.isf == PLENS_ISF_RUSANOV_HLLC ||
                          g.isf == PLENS_ISF_RUSANOV_AUSM_PLUS_UP;
-    int64_t idx[K], gd[K], gdn[K];
-    int bc[K];
-    bool ok[K];
-    float cs[K][5], c2[K][5], n[K][3];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        idx[k] = i0 + k * stride;
-        ok[k] = idx[k] < total;
-        if (ok[k]) {
-            bc[k] = dv.ft_bc[idx[k] / P2];
-            gd[k] = dv.fd_own[idx[k]];
-            gdn[k] = dv.fd_nbr[idx[k]];
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        if (!ok[k]) continue;
-        load_state<float>(dv, gd[k], cs[k]);
-        if (gdn[k] >= 0) load_state<float>(dv, gdn[k], c2[k]);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) n[k][d] = f64_to_f32(dv.ft_normal[idx[k] * 3 + d]);
-    }
     float* o = as_real<float>(out);
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        if (!ok[k]) continue;
-        const int64_t ti = idx[k] / P2;
+    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    FaceItem cur = face_item(dv, i0, total, P2);
+    FaceItem nxt = face_item(dv, i0 + stride, total, P2);
+    float cs[5], c2[5];
+    face_states(dv, cur, cs, c2);
+    while (cur.idx >= 0) {
+        // in flight during this face dof's flux: the next one's states, the one after's tables
+        float ns[5], n2[5];
+        face_states(dv, nxt, ns, n2);
+        const FaceItem aft = face_item(dv, cur.idx + 2 * stride, total, P2);
+
+        const int64_t ti = cur.idx / P2;
         float fb = 0.0f;
         if (blended) {
             const int64_t c = dv.ft_cell[ti];
             float a = f64_to_f32(dv.alpha[c]);
-            if (bc[k] < 0) a = 0.5f * (a + f64_to_f32(dv.alpha[dv.ft_nbr_cell[ti]]));
+            if (cur.bc < 0) a = 0.5f * (a + f64_to_f32(dv.alpha[dv.ft_nbr_cell[ti]]));
             fb = (a <= 0.0f) ? 0.0f : (a <= 1.0f ? a : 1.0f);
         }
-        if (bc[k] >= 0) {
-            const plens_bc_desc& b = dv.bcs[bc[k]];
+        if (cur.bc >= 0) {
+            const plens_bc_desc& b = dv.bcs[cur.bc];
             if (b.type != PLENS_BC_PERIODIC) {  // periodic: the partner's state is the ghost
                 float av[9] = {}, ag[9];
-                bc_ghost<float>(2, dv, g, b, cs[k], av, n[k], dv.ft_xyz + idx[k] * 3, s->time, -1, c2[k], ag);
+                bc_ghost<float>(2, dv, g, b, cs, av, cur.n, dv.ft_xyz + cur.idx * 3, s->time, -1, c2, ag);
             }
         }
         float fl[5];
-        inv_surf_flux_mx(cs[k], c2[k], n[k], gm, g.isf, fb, fl);
-        const int64_t slot = dv.fs_own[idx[k]], slot_nb = dv.fs_nbr[idx[k]];
+        inv_surf_flux_mx(cs, c2, cur.n, gm, g.isf, fb, fl);
+        const int64_t slot = cur.slot, slot_nb = cur.slot_nb;
 #pragma unroll
         for (int v = 0; v < 5; ++v) o[v * dv.nslot + slot] = fl[v];
         if (slot_nb >= 0)
 #pragma unroll
             for (int v = 0; v < 5; ++v) o[v * dv.nslot + slot_nb] = -fl[v];
+
+        cur = nxt;
+        nxt = aft;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            cs[v] = ns[v];
+            c2[v] = n2[v];
+        }
     }
 }
 

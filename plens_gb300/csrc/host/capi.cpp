@@ -2,8 +2,10 @@
 #include <cstring>
 #include <exception>
 #include <string>
+#include <vector>
 
 #include "plens_host.h"
+#include "output.h"
 #include "setup.h"
 
 struct plens_case {
@@ -50,6 +52,77 @@ int plens_case_initial_state(const plens_case* c, double* U)
 {
     std::memcpy(U, c->c->U0.data(), sizeof(double) * c->c->U0.size());
     return 0;
+}
+
+int plens_write_vtu(const plens_case* c, const char* path, const double* U, const double* avars,
+                    const double* alpha, const double* alpha_d, double loc_dt)
+{
+    if (!c || !path || !U) {
+        g_last_error = "null argument";
+        return 1;
+    }
+    try {
+        plens::Snapshot s;
+        s.U = U;
+        s.avars = avars;
+        s.alpha = alpha;
+        s.alpha_d = alpha_d;
+        s.loc_dt = loc_dt;
+        plens::write_vtu(path, *c->c, s);
+        return 0;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return 1;
+    }
+}
+
+int plens_write_pvd(const char* path, int64_t n, const double* times, const char* const* files)
+{
+    if (!path || n < 0 || (n > 0 && (!times || !files))) {
+        g_last_error = "null argument";
+        return 1;
+    }
+    try {
+        std::vector<std::pair<double, std::string>> e;
+        for (int64_t i = 0; i < n; ++i) e.emplace_back(times[i], files[i]);
+        plens::write_pvd(path, e);
+        return 0;
+    } catch (const std::exception& ex) {
+        g_last_error = ex.what();
+        return 1;
+    }
+}
+
+int plens_write_archive(const plens_case* c, const char* path, const double* U, double time, int64_t n_steps,
+                        int64_t output_counter)
+{
+    if (!c || !path || !U) {
+        g_last_error = "null argument";
+        return 1;
+    }
+    try {
+        plens::write_archive(path, *c->c, U, time, n_steps, output_counter);
+        return 0;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return 1;
+    }
+}
+
+int plens_read_archive(const plens_case* c, const char* path, double* U, double* time, int64_t* n_steps,
+                       int64_t* output_counter)
+{
+    if (!c || !path || !U) {
+        g_last_error = "null argument";
+        return 1;
+    }
+    try {
+        plens::read_archive(path, c->c->degree, c->c->n_cells, c->c->n_dofs, U, time, n_steps, output_counter);
+        return 0;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return 1;
+    }
 }
 
 int plens_case_dof_xyz(const plens_case* c, double* xyz)

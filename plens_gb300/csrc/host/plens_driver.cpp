@@ -1,6 +1,8 @@
 // plens_driver.cpp -- see plens_driver.h.
 #include "plens_driver.h"
 
+#include "output.h"
+
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -70,6 +72,21 @@ void PLENS::set_blender()
 }
 void PLENS::read_time_settings() { build_if_needed(); }
 
+namespace {
+std::string counter_name(const std::string& base, int64_t counter)
+{
+    char buf[32];
+    std::snprintf(buf, sizeof(buf), "_%06lld", (long long)counter);
+    return base + buf;
+}
+}  // namespace
+
+// PLENS::run + write (dgsem/plens.cc:1509-1550, 4170-4322): the state is written at every
+// `write frequency`-th step and at the end -- a .vtu file per output (one process: no .pvtu), the
+// .pvd collection, the .times log (counter, time, wall time) and a restart archive (.ar, read
+// back by the "from archive restart" initial condition). Each output is an asynchronous device
+// snapshot: the next `write frequency` steps are already running on the GPU while the host
+// writes the files of the previous output.
 void PLENS::run()
 {
     set_sol_vecs();
@@ -78,23 +95,64 @@ void PLENS::run()
     {
         std::ofstream f(dir + "/simulation_parameters.prm");
         f << case_->prm_echo << "\n# FE degree " << degree_ << "\n# Mapping degree " << case_->mapping_degree
-          << "\n# Processors 1 (GPU)\n# DoFs per variable " << case_->n_dofs << "\n";
+          << "\n# Processors 1 (GPU)\n# DoFs per variable " << case_->n_dofs << "\n# Indicator: Hennemenn"
+          << "\n# Lifting: entropy variables\n";
     }
-    std::ofstream times(dir + "/" + case_->base_file_name + ".times");
+    const std::string base = case_->base_file_name;
+    std::ofstream times(dir + "/" + base + ".times", std::ios::app);
     const auto t0 = std::chrono::steady_clock::now();
+    auto wall = [&] { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
+    const bool viscous = !(case_->params.mu0 < 1e-16);
+    const bool learned = case_->params.sensor == PLENS_SENSOR_LEARNED;
+    const int64_t nd = case_->n_dofs, nc = case_->n_cells;
+    std::vector<double> U(5 * nd), alpha(nc), alpha_d(nc), avars(viscous ? 9 * nd : 0);
+    std::vector<std::pair<double, std::string>> pvd;
+    int64_t counter = case_->starting_output_counter;
+
+    auto write_snapshot = [&]() {
+        double t = 0, dt = 0;
+        int64_t n = 0;
+        check(plens_gpu_snapshot_end(ctx_, U.data(), alpha.data(), alpha_d.data(), viscous ? avars.data() : nullptr,
+                                     &t, &n, &dt),
+              ctx_, "snapshot_end");
+        const std::string name = counter_name(base, counter);
+        Snapshot s;
+        s.U = U.data();
+        s.avars = viscous ? avars.data() : nullptr;
+        s.alpha = alpha.data();
+        s.alpha_d = alpha_d.data();
+        s.loc_dt = dt;
+        write_vtu(dir + "/" + name + ".vtu", *case_, s);
+        pvd.emplace_back(t, name + ".vtu");
+        write_pvd(dir + "/" + base + ".pvd", pvd);
+        write_archive(dir + "/" + name + ".ar", *case_, U.data(), t, n, counter);
+        times << counter << " " << t << " " << wall() << "\n";
+        times.flush();
+        ++counter;
+    };
+
     double t = case_->start_time, dt = 0;
     int64_t n = 0;
     check(plens_gpu_get_time(ctx_, &t, &n, &dt), ctx_, "get_time");
+    check(plens_gpu_snapshot_begin(ctx_), ctx_, "snapshot_begin");
     while (t < case_->end_time) {
-        check(plens_gpu_advance(ctx_, case_->write_freq, case_->end_time), ctx_, "advance");
+        if (learned) {
+            // the learned sensor's positivity fallback redoes steps from the host
+            write_snapshot();
+            check(plens_gpu_advance(ctx_, case_->write_freq, case_->end_time), ctx_, "advance");
+        } else {
+            check(plens_gpu_advance_async(ctx_, case_->write_freq, case_->end_time), ctx_, "advance_async");
+            write_snapshot();  // overlaps the steps just launched
+            check(plens_gpu_synchronize(ctx_), ctx_, "advance");
+        }
         check(plens_gpu_get_time(ctx_, &t, &n, &dt), ctx_, "get_time");
-        const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        std::printf("Current time: %.9g, dt: %.6g, time steps: %lld, elapsed wall time: %.3f\n", t, dt, (long long)n, wall);
-        times << n << " " << t << " " << wall << "\n";
+        std::printf("Current time: %.9g, dt: %.6g, time steps: %lld, elapsed wall time: %.3f\n", t, dt, (long long)n,
+                    wall());
+        check(plens_gpu_snapshot_begin(ctx_), ctx_, "snapshot_begin");
     }
-    std::vector<double> U(5 * case_->n_dofs);
+    write_snapshot();
     check(plens_gpu_get_state(ctx_, U.data()), ctx_, "get_state");
-    std::ofstream out(dir + "/" + case_->base_file_name + ".state", std::ios::binary);
+    std::ofstream out(dir + "/" + base + ".state", std::ios::binary);
     out.write(reinterpret_cast<const char*>(U.data()), sizeof(double) * U.size());
 }
 

@@ -27,8 +27,9 @@ public:
     void set_BC();
     void set_blender();
     void read_time_settings();
-    // while (cur_time < end_time) update(); with a progress line every `write frequency` steps
-    // and the final state written to <directory>/<base file name>.state (raw FP64 [5][ndof]).
+    // while (cur_time < end_time) update(); writing the state (.vtu, .pvd, .times, restart .ar)
+    // every `write frequency` steps and at the end, and the final state to
+    // <directory>/<base file name>.state (raw FP64 [5][ndof]).
     void run();
 
 private:

@@ -1,5 +1,6 @@
 // setup.cpp -- see setup.h. Each block names the reference routine it restates.
 #include "setup.h"
+#include "output.h"
 
 #include <algorithm>
 #include <cmath>
@@ -404,7 +405,7 @@ void declare_parameters(ParameterHandler& prm)
     }
     // IC (dgsem/plens.cc:322-380) + the seeded perturbations of this build's configs
     prm.declare_entry("IC/type", "piecewise function",
-                      "piecewise function|double mach reflection|uniform|shock vortex");
+                      "piecewise function|double mach reflection|uniform|shock vortex|from archive restart");
     prm.declare_entry("IC/file name", "ic.dat");
     prm.declare_entry("IC/archive mesh file name", "mesh.msh");
     prm.declare_entry("IC/archive mesh format", "msh");
@@ -1132,15 +1133,19 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
                         modes.push_back(md);
                     }
             std::vector<double> u(3 * nd, 0.0);
-            double usq = 0;
+            // the dofs are independent (threads over dofs; each dof sums its modes in order), the
+            // rms is summed serially so the field does not depend on the thread count
+#pragma omp parallel for schedule(static)
             for (int64_t dof = 0; dof < nd; ++dof) {
                 const double x[3] = {C.dof_xyz[dof], C.dof_xyz[nd + dof], C.dof_xyz[2 * nd + dof]};
                 for (const auto& md : modes) {
                     const double s = std::cos(md.k[0] * x[0] + md.k[1] * x[1] + md.k[2] * x[2] + md.ph);
                     for (int d = 0; d < 3; ++d) u[d * nd + dof] += md.a[d] * s;
                 }
-                for (int d = 0; d < 3; ++d) usq += u[d * nd + dof] * u[d * nd + dof];
             }
+            double usq = 0;
+            for (int64_t dof = 0; dof < nd; ++dof)
+                for (int d = 0; d < 3; ++d) usq += u[d * nd + dof] * u[d * nd + dof];
             const double urms = std::sqrt(usq / nd);
             const double g = pr.gamma, rho1 = 1.0, p1 = 1.0 / g, a1 = 1.0;  // a = 1 upstream
             const double scale = (urms > 0) ? Mt * a1 / urms : 0;
@@ -1156,6 +1161,11 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
                 prim_to_cons(g, behind ? rho2 : rho1, vel, behind ? p2 : p1, s);
                 setU(dof, s);
             }
+        } else if (ic == "from archive restart") {
+            // ICs::FromArchiveRestart (IBCs/from_archive_restart.cc:23-73): the state of an archive
+            // written for this mesh and degree (this build's own archive format, output.h); the
+            // start time and output counter come from the time integration settings, as there
+            read_archive(path(prm.get("IC/file name")), C.degree, C.n_cells, nd, C.U0.data(), nullptr, nullptr, nullptr);
         } else {
             throw std::runtime_error("Invalid IC type '" + ic + "'");
         }
