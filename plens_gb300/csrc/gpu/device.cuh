@@ -98,6 +98,12 @@ struct Dev {
     // and periodic partners; -1 otherwise), the owner's face slot and the neighbour's face slot
     // (interior faces; -1 otherwise)
     const int32_t *fd_own, *fd_nbr, *fs_own, *fs_nbr;
+    // the mixed form's inviscid face list: the face dofs above with each periodic pair of face
+    // tasks computed once (the partner's slot receives -F, as an interior face's neighbour does)
+    // when the scheme does not read alpha; per entry the task face dof, both dofs and slots, and
+    // the boundary condition to apply (-1: none)
+    int64_t n_mx;
+    const int32_t *mx_fd, *mx_own, *mx_nbr, *mx_sown, *mx_snbr, *mx_bc;
     const plens_bc_desc* bcs;
     int n_bc;
     const plens_expr_insn* expr_code;
@@ -119,7 +125,10 @@ struct Dev {
 __device__ __forceinline__ double eval_expr(const Dev& dv, int idx, double x, double y, double z, double t)
 {
     if (idx < 0 || idx >= dv.n_expr) return 0.0 / 0.0;
-    return plens::expr_eval(dv.expr_code + dv.expr_off[idx], dv.expr_len[idx], x, y, z, t);
+    const plens_expr_insn* code = dv.expr_code + dv.expr_off[idx];
+    const int len = dv.expr_len[idx];
+    if (len == 1 && code[0].op == plens::EOP_CONST) return code[0].val;  // a constant: no VM stack
+    return plens::expr_eval(code, len, x, y, z, t);
 }
 
 // FP64 <-> FP32 conversions by integer arithmetic on the IEEE-754 encodings, with the results of

@@ -45,7 +45,7 @@ struct Launch {
                     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_surface_inv_mx<P>, 128, 0);
                     blocks = (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
                 }
-                const int64_t need = (n + 127) / 128;
+                const int64_t need = (dv.n_mx + 127) / 128;
                 k_surface_inv_mx<P><<<(int)(need < blocks ? need : blocks), 128, 0, st>>>(dv, g, out);
                 return 1;
             }

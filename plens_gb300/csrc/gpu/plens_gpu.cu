@@ -489,6 +489,43 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         if ((r = dupload(c, &d.fd_own, own.data(), nfd)) || (r = dupload(c, &d.fd_nbr, nbr.data(), nfd)) ||
             (r = dupload(c, &d.fs_own, sown.data(), nfd)) || (r = dupload(c, &d.fs_nbr, snbr.data(), nfd)))
             return r;
+        if (c->mixed) {
+            // periodic pairs merged (owner: the smaller cell*6+face key) unless the scheme blends
+            // with alpha (the reference's own-alpha rule for periodic faces then applies per side)
+            const int isf = prm->inv_surf_flux;
+            const bool merge = isf != PLENS_ISF_CHANDRASHEKHAR && isf != PLENS_ISF_RUSANOV_HLLC &&
+                               isf != PLENS_ISF_RUSANOV_AUSM_PLUS_UP;
+            std::vector<int32_t> mfd, mown, mnbr, msown, msnbr, mbc;
+            for (int64_t t = 0; t < nt; ++t) {
+                const int bc = mesh->ft_bc[t];
+                const bool periodic = bc >= 0 && bc < prm->n_bc && prm->bcs[bc].type == PLENS_BC_PERIODIC;
+                const int64_t key = (int64_t)mesh->ft_cell[t] * 6 + mesh->ft_face[t];
+                const int64_t pkey = periodic ? (int64_t)mesh->ft_nbr_cell[t] * 6 + mesh->ft_nbr_face[t] : -1;
+                if (periodic && merge && pkey < key) continue;  // the partner's task computes it
+                for (int q = 0; q < P2; ++q) {
+                    const int64_t k = t * P2 + q;
+                    mfd.push_back((int32_t)k);
+                    mown.push_back(own[k]);
+                    mnbr.push_back(nbr[k]);
+                    msown.push_back(sown[k]);
+                    if (periodic && merge) {
+                        const int64_t nb = mesh->ft_nbr_cell[t];
+                        const int fn = mesh->ft_nbr_face[t], qn = mesh->ft_nbr_fdof[k];
+                        msnbr.push_back((int32_t)((nb * 6 + fn) * P2 + qn));
+                        mbc.push_back(-1);
+                    } else {
+                        msnbr.push_back(snbr[k]);
+                        mbc.push_back(bc);
+                    }
+                }
+            }
+            d.n_mx = (int64_t)mfd.size();
+            if ((r = dupload(c, &d.mx_fd, mfd.data(), mfd.size())) || (r = dupload(c, &d.mx_own, mown.data(), mown.size())) ||
+                (r = dupload(c, &d.mx_nbr, mnbr.data(), mnbr.size())) ||
+                (r = dupload(c, &d.mx_sown, msown.data(), msown.size())) ||
+                (r = dupload(c, &d.mx_snbr, msnbr.data(), msnbr.size())) || (r = dupload(c, &d.mx_bc, mbc.data(), mbc.size())))
+                return r;
+        }
     }
     // wall cells: a boundary face of type uniform temp wall or insulated wall
     // (dgsem/plens.cc:2909-2920)

@@ -19,18 +19,20 @@ struct FaceItem {
     float n[3];
 };
 
-__device__ __forceinline__ FaceItem face_item(const Dev& dv, int64_t idx, int64_t total, int P2)
+// entry i of the mixed face list; idx = the task face dof (normal, location, task)
+__device__ __forceinline__ FaceItem face_item(const Dev& dv, int64_t i, int64_t total)
 {
     FaceItem it;
-    it.idx = (idx < total) ? idx : -1;
-    if (it.idx >= 0) {
-        it.gd = dv.fd_own[idx];
-        it.gdn = dv.fd_nbr[idx];
-        it.bc = dv.ft_bc[idx / P2];
-        it.slot = dv.fs_own[idx];
-        it.slot_nb = dv.fs_nbr[idx];
+    it.idx = -1;
+    if (i < total) {
+        it.idx = dv.mx_fd[i];
+        it.gd = dv.mx_own[i];
+        it.gdn = dv.mx_nbr[i];
+        it.bc = dv.mx_bc[i];
+        it.slot = dv.mx_sown[i];
+        it.slot_nb = dv.mx_snbr[i];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) it.n[d] = f64_to_f32(dv.ft_normal[idx * 3 + d]);
+        for (int d = 0; d < 3; ++d) it.n[d] = f64_to_f32(dv.ft_normal[it.idx * 3 + d]);
     }
     return it;
 }
@@ -48,22 +50,23 @@ __global__ void __launch_bounds__(128, 4) k_surface_inv_mx(Dev dv, GasP g, doubl
     constexpr int P2 = P * P;
     Scalars* s = dv.sc;
     if (!s->active) return;
-    const int64_t total = dv.ntask * P2;
+    const int64_t total = dv.n_mx;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const float gm = f64_to_f32(g.gamma);
     const bool blended = g.isf == PLENS_ISF_CHANDRASHEKHAR || g.isf == PLENS_ISF_RUSANOV_HLLC ||
                          g.isf == PLENS_ISF_RUSANOV_AUSM_PLUS_UP;
     float* o = as_real<float>(out);
-    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    FaceItem cur = face_item(dv, i0, total, P2);
-    FaceItem nxt = face_item(dv, i0 + stride, total, P2);
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    FaceItem cur = face_item(dv, i, total);
+    FaceItem nxt = face_item(dv, i + stride, total);
     float cs[5], c2[5];
     face_states(dv, cur, cs, c2);
     while (cur.idx >= 0) {
         // in flight during this face dof's flux: the next one's states, the one after's tables
         float ns[5], n2[5];
         face_states(dv, nxt, ns, n2);
-        const FaceItem aft = face_item(dv, cur.idx + 2 * stride, total, P2);
+        const FaceItem aft = face_item(dv, i + 2 * stride, total);
+        i += stride;
 
         const int64_t ti = cur.idx / P2;
         float fb = 0.0f;
