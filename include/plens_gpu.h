@@ -234,6 +234,10 @@ int plens_gpu_synchronize(plens_ctx* ctx);
 int plens_gpu_get_cell_scalars(plens_ctx* ctx, double* alpha, double* alpha_d, double* dt_cell);
 /* Auxiliary variables of the last viscous RHS ([9][ndof]): PLENS::gcrk_avars. */
 int plens_gpu_get_avars(plens_ctx* ctx, double* avars);
+/* Learned sensor: evaluate the network's two hidden layers on the tensor cores (tcgen05, 3xTF32)
+ * or on the CUDA cores (enable = 0, the default: faster on the measured workloads). No reference
+ * counterpart. */
+int plens_gpu_set_sensor_tensor_cores(plens_ctx* ctx, int enable);
 /* Asynchronous snapshot for data output (replaces the host reads of PLENS::write,
  * dgsem/plens.cc:4170-4322): _begin copies U, alpha, alpha_d, the auxiliary variables (viscous)
  * and the clock on the context's stream into a device buffer, then to library-owned pinned host

@@ -166,6 +166,7 @@ def gpu_lib() -> C.CDLL:
         L.plens_gpu_mlp_infer.argtypes = [vp, i64, vp, C.c_float, vp]
         L.plens_gpu_selftest_conversions.argtypes = [i64, C.c_uint64, C.POINTER(i64)]
         L.plens_gpu_snapshot_begin.argtypes = [vp]
+        L.plens_gpu_set_sensor_tensor_cores.argtypes = [vp, C.c_int]
         L.plens_gpu_snapshot_end.argtypes = [vp, vp, vp, vp, vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(dbl)]
         L.plens_gpu_set_kernel_timing.argtypes = [vp, C.c_int]
         L.plens_gpu_kernel_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(i64)]
@@ -409,6 +410,10 @@ class GpuSolver:
         e = C.c_double()
         self._check(self.L.plens_gpu_sensor_stats(self.h, C.byref(j), C.byref(f), C.byref(e), C.byref(lo)), "sensor_stats")
         return {"judged": j.value, "fallbacks": f.value, "max_alpha_err": e.value, "lo_cells_last": lo.value}
+
+    def set_sensor_tensor_cores(self, enable: bool):
+        """Learned sensor: hidden layers on the tensor cores or the CUDA cores (the default)."""
+        self._check(self.L.plens_gpu_set_sensor_tensor_cores(self.h, 1 if enable else 0), "set_sensor_tensor_cores")
 
     def snapshot_begin(self):
         """Start an asynchronous snapshot (state, alpha, alpha_d, auxiliary variables, clock)."""

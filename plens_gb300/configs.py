@@ -128,7 +128,31 @@ end
 
 
 def dmr(nx: int = 240, ny: int = 60, precision="fp64", sensor="modal", end_time=0.2, noise=1e-6,
-        degree=3):
+        degree=3, z_bc="periodic"):
+    """Double Mach reflection. z_bc: "periodic" (the benchmark configuration) or "symmetry" (the
+    z boundaries of the reference's own input, study1/dmr/scripts/base_input.prm:43-48)."""
+    if z_bc == "periodic":
+        z_bcs = """    subsection bid5
+        set type = periodic
+        set periodic direction = 2
+        set periodic orientation = left
+        set other surface boundary id = 6
+    end
+    subsection bid6
+        set type = periodic
+        set periodic direction = 2
+        set periodic orientation = right
+        set other surface boundary id = 5
+    end"""
+    elif z_bc == "symmetry":
+        z_bcs = """    subsection bid5
+        set type = symmetry
+    end
+    subsection bid6
+        set type = symmetry
+    end"""
+    else:
+        raise ValueError(z_bc)
     prm = f"""
 subsection mesh
     set type = straight
@@ -181,18 +205,7 @@ subsection BCs
     subsection bid4
         set type = uniform temp wall
     end
-    subsection bid5
-        set type = periodic
-        set periodic direction = 2
-        set periodic orientation = left
-        set other surface boundary id = 6
-    end
-    subsection bid6
-        set type = periodic
-        set periodic direction = 2
-        set periodic orientation = right
-        set other surface boundary id = 5
-    end
+{z_bcs}
 end
 subsection blender parameters
     set variable = pxrho

@@ -80,57 +80,72 @@ static __global__ void k_clock(Dev dv)
 // plain form evaluates it in FP64 with the reference's expressions; the mixed form in FP32 (the
 // step size is a CFL bound, not an accumulated quantity), from FP64 state and metrics converted on
 // the integer pipes.
+// the stable step of one dof (T: arithmetic type)
+template <int P, class T>
+__device__ __forceinline__ T dof_stable_step(const Dev& dv, const GasP& g, double N15, int N, int64_t dof, T Co)
+{
+    constexpr int P3 = P * P * P;
+    const int64_t c = dof / P3;
+    const T gm = to_real<T>(g.gamma);
+    T cs[5];
+    load_state<T>(dv, dof, cs);
+    T a, vel[3];
+    if constexpr (sizeof(T) == 8) {
+        a = sqrt(gm * get_p(cs, gm) / cs[0]);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) vel[d] = cs[1 + d] / cs[0];
+    } else {
+        a = sqrtf(__fdividef(gm * get_p(cs, gm), cs[0]));
+        const T ri = __fdividef(1.0f, cs[0]);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) vel[d] = cs[1 + d] * ri;
+    }
+    T adv[3];
+#pragma unroll
+    for (int row = 0; row < 3; ++row) {
+        T acc = T(0);
+#pragma unroll
+        for (int col = 0; col < 3; ++col) acc += to_real<T>(dv.Jinv[(col * 3 + row) * dv.nd + dof]) * vel[col];
+        adv[row] = acc;
+    }
+    T madv = adv[0];
+    if (adv[1] > madv) madv = adv[1];
+    if (adv[2] > madv) madv = adv[2];
+    T mu = T(0);
+    if (!g.inviscid) {
+        if constexpr (sizeof(T) == 8) {
+            const double Tk = get_e(cs) / (g.R / (g.gamma - 1));
+            mu = g.const_visc ? g.mu0 : g.mu0 * pow(Tk / g.T0, 1.5) * (g.T0 + g.S) / (Tk + g.S);
+        } else {
+            const float Tk = __fdividef(get_e(cs) * to_real<T>(g.gamma - 1), to_real<T>(g.R));
+            const float T0 = to_real<T>(g.T0), S = to_real<T>(g.S), x = __fdividef(Tk, T0);
+            mu = g.const_visc ? to_real<T>(g.mu0) : to_real<T>(g.mu0) * x * sqrtf(x) * __fdividef(T0 + S, Tk + S);
+        }
+    }
+    const T h = to_real<T>(dv.h_min[c]);
+    return Co / (to_real<T>(N15) * (madv + a / h + (T)(N * N) * mu / (h * h * cs[0])));
+}
+
+// dofs per thread of the time-step kernel: two in the mixed form (their loads overlap)
+template <class T> constexpr int kStepItems = (sizeof(T) == 4) ? 2 : 1;
+
 template <int P, class T>
 __global__ void __launch_bounds__(256) k_time_step(Dev dv, GasP g, double N15, int N)
 {
     Scalars* s = dv.sc;
     if (!s->active) return;
-    constexpr int P3 = P * P * P;
+    constexpr int K = kStepItems<T>;
     __shared__ T s_red[8];
     T local = T(1e6);
-    const int64_t dof = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (dof < dv.nd) {
-        const int64_t c = dof / P3;
-        const T gm = to_real<T>(g.gamma);
-        T cs[5];
-        load_state<T>(dv, dof, cs);
-        T a, vel[3];
-        if constexpr (sizeof(T) == 8) {
-            a = sqrt(gm * get_p(cs, gm) / cs[0]);
+    const T Co = to_real<T>(s->courant);
+    const int64_t base = blockIdx.x * (int64_t)blockDim.x * K + threadIdx.x;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) vel[d] = cs[1 + d] / cs[0];
-        } else {
-            a = sqrtf(__fdividef(gm * get_p(cs, gm), cs[0]));
-            const T ri = __fdividef(1.0f, cs[0]);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) vel[d] = cs[1 + d] * ri;
+    for (int k = 0; k < K; ++k) {
+        const int64_t dof = base + (int64_t)k * blockDim.x;
+        if (dof < dv.nd) {
+            const T cur = dof_stable_step<P, T>(dv, g, N15, N, dof, Co);
+            if (cur < local) local = cur;
         }
-        T adv[3];
-#pragma unroll
-        for (int row = 0; row < 3; ++row) {
-            T acc = T(0);
-#pragma unroll
-            for (int col = 0; col < 3; ++col) acc += to_real<T>(dv.Jinv[(col * 3 + row) * dv.nd + dof]) * vel[col];
-            adv[row] = acc;
-        }
-        T madv = adv[0];
-        if (adv[1] > madv) madv = adv[1];
-        if (adv[2] > madv) madv = adv[2];
-        T mu = T(0);
-        if (!g.inviscid) {
-            if constexpr (sizeof(T) == 8) {
-                const double Tk = get_e(cs) / (g.R / (g.gamma - 1));
-                mu = g.const_visc ? g.mu0 : g.mu0 * pow(Tk / g.T0, 1.5) * (g.T0 + g.S) / (Tk + g.S);
-            } else {
-                const float Tk = __fdividef(get_e(cs) * to_real<T>(g.gamma - 1), to_real<T>(g.R));
-                const float T0 = to_real<T>(g.T0), S = to_real<T>(g.S), x = __fdividef(Tk, T0);
-                mu = g.const_visc ? to_real<T>(g.mu0) : to_real<T>(g.mu0) * x * sqrtf(x) * __fdividef(T0 + S, Tk + S);
-            }
-        }
-        const T h = to_real<T>(dv.h_min[c]);
-        const T Co = to_real<T>(s->courant);
-        const T cur = Co / (to_real<T>(N15) * (madv + a / h + (T)(N * N) * mu / (h * h * cs[0])));
-        if (cur < local) local = cur;
     }
     // warp-shuffle min, then block min, then one atomic per block
 #pragma unroll

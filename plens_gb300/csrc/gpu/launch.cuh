@@ -107,7 +107,8 @@ struct Launch {
     }
     static int time_step(const Dev& dv, const GasP& g, double N15, int N, cudaStream_t st)
     {
-        const int grid = (int)((dv.nd + 255) / 256);
+        const int64_t per_block = 256 * kStepItems<T>;
+        const int grid = (int)((dv.nd + per_block - 1) / per_block);
         k_time_step<P, T><<<grid, 256, 0, st>>>(dv, g, N15, N);
         return 1;
     }

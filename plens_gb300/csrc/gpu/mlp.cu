@@ -10,6 +10,7 @@
 
 #include "kernels.cuh"
 #include "mlp.cuh"
+#include "mlp_tc.cuh"
 
 namespace plens_gpu {
 
@@ -407,6 +408,175 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, (P <= 4 ? 3 : 1)) k_senso
     }
 }
 
+// The same inference with the two hidden layers on the tensor cores (mlp_tc.cuh): tiles of 128
+// cells per block; the eight warps compute the inputs of 16 cells each (as above), one thread
+// issues each layer's 24 tcgen05.mma, and every thread applies bias and GELU to its row's 32
+// accumulator columns. One block per SM (137 KB of shared memory).
+constexpr int kTcParams = 4 * tc::kK * tc::kN + 3 * tc::kN + 4;  // W1 hi/lo, W2 hi/lo, b1, b2, w3, b3 (+pad)
+
+template <int P>
+struct TcSmem {
+    static constexpr int SV = InferScratch<P>::V, per_warp = 2 * SV + 64;
+    static constexpr size_t oB = 0;                                       // 4 x [64][64] operand layout
+    static constexpr size_t oBias = oB + 4 * tc::kK * tc::kN;            // b1, b2, w3, b3
+    static constexpr size_t oAhi = oBias + 256;
+    static constexpr size_t oAlo = oAhi + tc::kRows * tc::kK;
+    static constexpr size_t oRed = oAlo + tc::kRows * tc::kK;             // [128][2]
+    static constexpr size_t oMod = oRed + 2 * tc::kRows;                  // [128]
+    static constexpr size_t oScr = oMod + tc::kRows;
+    static constexpr size_t floats = oScr + 8 * per_warp;
+    static constexpr size_t bytes = floats * sizeof(float);
+};
+
+template <int P>
+__global__ void __launch_bounds__(256, 1) k_sensor_infer_tc(Dev dv, const float* __restrict__ Wtc, GasP g, BlendP bp,
+                                                             Ops ops, Interp ip, double* out, int gated,
+                                                             const uint8_t* mask)
+{
+    constexpr int P3 = P * P * P, NPL = (P3 + 31) / 32;
+    using L = TcSmem<P>;
+    extern __shared__ __align__(128) float smem_tc[];
+    float* smem_f = smem_tc;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    float* sB = smem_f + L::oB;
+    const float* W1hi = sB;
+    const float* W1lo = sB + tc::kK * tc::kN;
+    const float* W2hi = sB + 2 * tc::kK * tc::kN;
+    const float* W2lo = sB + 3 * tc::kK * tc::kN;
+    const float* b1 = smem_f + L::oBias;
+    const float* b2 = b1 + 64;
+    const float* w3 = b2 + 64;
+    float* sAhi = smem_f + L::oAhi;
+    float* sAlo = smem_f + L::oAlo;
+    float* sRed = smem_f + L::oRed;
+    float* sMod = smem_f + L::oMod;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    float* sv = smem_f + L::oScr + warp * L::per_warp;
+    float* st = sv + L::SV;
+    float* sx = st + L::SV;
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    if (blockIdx.x == 0 && tid == 0) *dv.lo_count = 0;  // this stage's troubled-cell list
+    if (gated && s->sensor_fallback) return;
+    {
+        const float4* src = reinterpret_cast<const float4*>(Wtc);
+        float4* dst = reinterpret_cast<float4*>(smem_f);
+        for (int i = tid; i < kTcParams / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    if (warp == 0) tc::tmem_alloc(&tmem_base);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_base;
+    const float cut = fmaxf(f64_to_f32(bp.amin), kLearnedCut), amax = f64_to_f32(bp.amax), b3 = w3[64];
+    const float gm = f64_to_f32(g.gamma);
+    const int q = warp & 3, h = warp >> 2, row_e = 32 * q + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * h);
+    const int64_t ntiles = (dv.nc + tc::kRows - 1) / tc::kRows;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        // inputs: warp w fills rows 16w .. 16w+15
+        float u[NPL][5];
+        const int64_t c0 = tile * tc::kRows + 16 * warp;
+        if (c0 < dv.nc) load_cell_f32<P, NPL>(dv, c0, lane, u);
+        for (int r = 0; r < 16; ++r) {
+            const int row = 16 * warp + r;
+            const int64_t cell = c0 + r;
+            if (cell < dv.nc) {
+                float un[NPL][5];
+                if (r < 15 && cell + 1 < dv.nc) load_cell_f32<P, NPL>(dv, cell + 1, lane, un);
+                features_from_state<P, NPL, 1>(dv, cell, gm, ip, u, sv, st, sx);
+                float am = -1.0f;
+                if (mask && mask[cell]) am = modal_alpha_warp<P, NPL>(ops, bp, gm, u, sv, st);
+                if (lane == 0) sMod[row] = am;
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const int k = lane + 32 * j;
+                    const float x = sx[k], hi = tc::tf32_hi(x);
+                    sAhi[tc::core_off(row, k)] = hi;
+                    sAlo[tc::core_off(row, k)] = x - hi;
+                }
+                __syncwarp();
+#pragma unroll
+                for (int j = 0; j < NPL; ++j)
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) u[j][v] = un[j][v];
+            } else {
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    sAhi[tc::core_off(row, lane + 32 * j)] = 0.0f;
+                    sAlo[tc::core_off(row, lane + 32 * j)] = 0.0f;
+                }
+                if (lane == 0) sMod[row] = -1.0f;
+            }
+        }
+        float v[32];
+        for (int layer = 0; layer < 2; ++layer) {
+            tc::fence_smem_async();
+            tc::fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after();
+                if (layer == 0) tc::layer_mma(tmem, sAhi, sAlo, W1hi, W1lo);
+                else tc::layer_mma(tmem, sAhi, sAlo, W2hi, W2lo);
+                tc::mma_commit(&bar);
+            }
+            bool done = false;
+            for (int it = 0; it < (1 << 22) && !done; ++it) done = mbar_try_wait(&bar, phase);
+            ok = __syncthreads_and(done ? 1 : 0) != 0;
+            if (!ok) break;
+            phase ^= 1;
+            tc::fence_after();
+            tc::tmem_ld32(taddr, v);
+            if (layer == 0) {
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const int col = 32 * h + i;
+                    const float x = gelu(v[i] + b1[col]), hi = tc::tf32_hi(x);
+                    sAhi[tc::core_off(row_e, col)] = hi;
+                    sAlo[tc::core_off(row_e, col)] = x - hi;
+                }
+            } else {
+                float z = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) z += w3[32 * h + i] * gelu(v[i] + b2[32 * h + i]);
+                sRed[2 * row_e + h] = z;
+            }
+        }
+        if (!ok) break;
+        tc::fence_before();
+        __syncthreads();
+        if (h == 0) {
+            const int64_t cell = tile * tc::kRows + row_e;
+            if (cell < dv.nc) {
+                const float z = sRed[2 * row_e] + sRed[2 * row_e + 1] + b3;
+                const float at = amax / (1.0f + expf(-z)), am = sMod[row_e];
+                double a = (am >= 0.0f) ? f32_to_f64(am) : ((at < cut) ? 0.0 : f32_to_f64(at));
+                if (dv.cell_wall[cell]) {
+                    const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
+                    a = (wl > a) ? wl : a;
+                }
+                out[cell] = a;
+            }
+        }
+        __syncthreads();  // the operand and reduction buffers are reused by the next tile
+    }
+    if (!ok) {
+        if (tid == 0) s->err = PLENS_GPU_E_TIMEOUT;
+        for (int it = 0; it < (1 << 22); ++it)  // the MMAs in flight complete before the TMEM goes
+            if (mbar_try_wait(&bar, phase)) break;
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem);
+}
+
 // judge (per cell, before smoothing): where |alpha_mlp - alpha_plain| exceeds the tolerance the
 // plain value is kept and the cell is marked, so the plain indicator keeps computing it until the
 // next judged step; elsewhere the MLP value is used. The smoothing max(a, a_nbr/2) is 1-Lipschitz
@@ -467,6 +637,27 @@ __global__ void k_features(Dev dv, GasP g, Interp ip, float* x)
 }
 
 template <int P>
+int launch_infer_tc(const Dev& dv, const float* Wtc, const GasP& g, const BlendP& bp, const Ops& ops, double* out,
+                    int gated, const uint8_t* mask, cudaStream_t st)
+{
+    const Interp ip = make_interp(P);
+    const size_t bytes = TcSmem<P>::bytes;
+    static int nsm = 0;
+    if (!nsm) {
+        cudaFuncSetAttribute(k_sensor_infer_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm < 1) nsm = 1;
+    }
+    const int64_t tiles = (dv.nc + tc::kRows - 1) / tc::kRows;
+    if (tiles < 1) return 0;
+    const int64_t blocks = std::min<int64_t>(tiles, nsm);
+    k_sensor_infer_tc<P><<<(unsigned)blocks, 256, bytes, st>>>(dv, Wtc, g, bp, ops, ip, out, gated, mask);
+    return 1;
+}
+
+template <int P>
 int launch_infer(const Dev& dv, const float* Wt, const GasP& g, const BlendP& bp, const Ops& ops, double* out,
                  int gated, const uint8_t* mask, cudaStream_t st)
 {
@@ -512,7 +703,8 @@ int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, con
     b0.gate = 0;
     b0.mask = nullptr;
     if (m.judge_this_step) {
-        n += launch_infer<P>(dv, m.params_t, g, bp, ops, m.alpha_plain, 0, nullptr, st);
+        n += m.use_tc ? launch_infer_tc<P>(dv, m.params_tc, g, bp, ops, m.alpha_plain, 0, nullptr, st)
+                      : launch_infer<P>(dv, m.params_t, g, bp, ops, m.alpha_plain, 0, nullptr, st);
         n += launch_blender<P>(dv, ops, g, b0, st);
         const unsigned grid = (unsigned)((dv.nc + 127) / 128);
         k_judge_cells<<<grid, 128, 0, st>>>(dv, m.alpha_plain, m.mask, m.tol, m.maxerr, m.nbad);
@@ -522,11 +714,12 @@ int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, con
     } else {
         // the cells the judge handed back get the plain indicator inside the inference kernel;
         // the plain blender itself runs only in whole-domain fallback
-        n += launch_infer<P>(dv, m.params_t, g, bp, ops, dv.alpha_raw, 1, m.mask, st);
+        n += m.use_tc ? launch_infer_tc<P>(dv, m.params_tc, g, bp, ops, dv.alpha_raw, 1, m.mask, st)
+                      : launch_infer<P>(dv, m.params_t, g, bp, ops, dv.alpha_raw, 1, m.mask, st);
         BlendP b1 = bp;
         b1.gate = 1;
         b1.mask = nullptr;
-        n += launch_blender<P>(dv, ops, g, b1, st, 152 * 8);
+        n += launch_blender<P>(dv, ops, g, b1, st, 152 * 2);
     }
     k_alpha_smooth<<<(unsigned)((dv.nc + 127) / 128), 128, 0, st>>>(dv, b0);
     return n + 1;
@@ -541,6 +734,8 @@ int mlp_create(MlpDevice& m, int64_t nc, std::vector<void*>& allocs)
     allocs.push_back(m.params);
     if (cudaMalloc(&m.params_t, sizeof(float) * kParamsPad) != cudaSuccess) return 1;
     allocs.push_back(m.params_t);
+    if (cudaMalloc(&m.params_tc, sizeof(float) * kTcParams) != cudaSuccess) return 1;
+    allocs.push_back(m.params_tc);
     if (cudaMalloc(&m.alpha_plain, sizeof(double) * (nc + 1)) != cudaSuccess) return 1;
     allocs.push_back(m.alpha_plain);
     if (cudaMalloc(&m.maxerr, sizeof(unsigned long long)) != cudaSuccess) return 1;
@@ -572,6 +767,35 @@ int mlp_set_weights(MlpDevice& m, const float* host_params, cudaStream_t st)
         }
         t[dst] = host_params[i];
     }
+    // the tensor-core copy: W1 and W2 ([out][in], i.e. the B operands N x K) split into TF32 hi
+    // and lo parts in the canonical operand layout, then b1, b2, w3, b3
+    std::vector<float> w(kTcParams, 0.0f);
+    {
+        const float* W1 = host_params;
+        const float* B1 = W1 + kMlpHid * kMlpIn;
+        const float* W2 = B1 + kMlpHid;
+        const float* B2 = W2 + kMlpHid * kMlpHid;
+        const float* W3 = B2 + kMlpHid;
+        const int mat = tc::kK * tc::kN;
+        for (int o = 0; o < kMlpHid; ++o)
+            for (int k = 0; k < kMlpIn; ++k) {
+                const int off = tc::core_off(o, k);
+                const float a = W1[o * kMlpIn + k], b = W2[o * kMlpHid + k];
+                const float ah = tc::tf32_hi(a), bh = tc::tf32_hi(b);
+                w[off] = ah;
+                w[mat + off] = a - ah;
+                w[2 * mat + off] = bh;
+                w[3 * mat + off] = b - bh;
+            }
+        for (int i = 0; i < kMlpHid; ++i) {
+            w[4 * mat + i] = B1[i];
+            w[4 * mat + 64 + i] = B2[i];
+            w[4 * mat + 128 + i] = W3[i];
+        }
+        w[4 * mat + 192] = W3[kMlpHid];
+    }
+    if (cudaMemcpyAsync(m.params_tc, w.data(), sizeof(float) * kTcParams, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return 1;
     if (cudaMemcpyAsync(m.params, host_params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, st) != cudaSuccess) return 1;
     if (cudaMemcpyAsync(m.params_t, t.data(), sizeof(float) * kParamsPad, cudaMemcpyHostToDevice, st) != cudaSuccess) return 1;
     if (cudaStreamSynchronize(st) != cudaSuccess) return 1;

@@ -901,6 +901,20 @@ size_t snap_avars_bytes(const plens_ctx* c)
 size_t snap_off_scalars(const plens_ctx* c) { return (snap_off_avars(c) + snap_avars_bytes(c) + 15) / 16 * 16; }
 }  // namespace
 
+int plens_gpu_set_sensor_tensor_cores(plens_ctx* c, int enable)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    if (!c->learned) return fail(c, PLENS_GPU_E_INVALID, "context was created without the learned sensor");
+    if (int r = sync_and_check(c)) return r;
+    c->mlp.use_tc = enable != 0;
+    for (auto& gx : c->step_graph)  // the step's launch sequence changed
+        if (gx) {
+            cudaGraphExecDestroy(gx);
+            gx = nullptr;
+        }
+    return 0;
+}
+
 int plens_gpu_snapshot_begin(plens_ctx* c)
 {
     if (!c || !c->dv.U) return PLENS_GPU_E_INVALID;

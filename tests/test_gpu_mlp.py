@@ -83,3 +83,33 @@ def test_learned_sensor_in_the_rhs():
     ref.advance(30)
     err = rel_l1(gl.get_state(), ref.get_state()[0])
     assert err[0] <= 1e-4, (err, st)
+
+
+def test_sensor_tensor_cores_match_cuda_cores():
+    """The inference kernel with the hidden layers on the tensor cores (tcgen05, 3xTF32) gives the
+    CUDA-core kernel's alpha: to 1e-5 everywhere but at the 0.01 cut, where a value may land on
+    either side."""
+    from pathlib import Path
+
+    w = np.fromfile(Path(__file__).resolve().parents[1] / "plens_gb300" / "sensor_weights.bin", dtype=np.float32)
+    base = make(configs.dmr(nx=48, ny=12))
+    o = Oracle(base)
+    o.set_state(base.initial_state(), 0.0)
+    o.advance(40)
+    U, t, _, _ = o.get_state()
+    case = make(configs.dmr(nx=48, ny=12, precision="mixed", sensor="learned"))
+    out = []
+    for tc_on in (True, False):
+        g = GpuSolver(case)
+        g.set_sensor_weights(w)
+        g.set_sensor_tensor_cores(tc_on)
+        g.set_state(U, t)
+        R = g.rhs()
+        a, _, _ = g.cell_scalars()
+        out.append((a, R))
+    (a1, R1), (a2, R2) = out
+    d = np.abs(a1 - a2)
+    assert (a1 > 0).any()
+    off = d > 1e-5
+    assert off.mean() <= 2e-3, d.max()
+    assert np.all(np.minimum(a1[off], a2[off]) < 0.011), (a1[off], a2[off])
