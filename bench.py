@@ -177,7 +177,7 @@ def _form_case(workload: str, precision: str, sensor: str, cache: dict | None = 
 
 
 def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_index: int, weights=None,
-                 workload: str = "dmr", cache: dict | None = None):
+                 workload: str = "dmr", cache: dict | None = None, tensor_cores: bool = False):
     import torch
 
     from plens_gb300.api import GpuSolver
@@ -187,6 +187,7 @@ def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_in
     g = GpuSolver(case)
     if sensor == "learned":
         g.set_sensor_weights(weights)
+        g.set_sensor_tensor_cores(tensor_cores)
     g.set_state(U0, 0.0)
     g.advance(warmup)
     stream = torch.cuda.ExternalStream(g.stream, device=torch.device("cuda", device_index))
@@ -409,6 +410,8 @@ def main():
                     help="per-configuration report (throughput of every form, accuracy after --accuracy-steps) "
                          "instead of the benchmark line")
     ap.add_argument("--accuracy-steps", type=int, default=0, help="override the accuracy window (steps)")
+    ap.add_argument("--sensor-tensor-cores", action="store_true",
+                    help="the learned sensor's hidden layers on the tensor cores (tcgen05, 3xTF32)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -439,7 +442,8 @@ def main():
     cache = {}
     plain = measure_form("fp64", "modal", args.steps, args.warmup, device.index, cache=cache)
     modal = measure_form("mixed", "modal", args.steps, args.warmup, device.index, cache=cache)
-    learned = (measure_form("mixed", "learned", args.steps, args.warmup, device.index, weights, cache=cache)
+    learned = (measure_form("mixed", "learned", args.steps, args.warmup, device.index, weights, cache=cache,
+                            tensor_cores=args.sensor_tensor_cores)
                if weights is not None else None)
     fast = learned if learned is not None else modal
     fast_sensor = "learned" if learned is not None else "modal"
@@ -480,7 +484,8 @@ def main():
         "vs_baseline": None,
         "dtype": "f32 flux differencing + f64 state/registers",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": f"mixed FP32 + {fast_sensor} sensor",
+        "config": {"workload": WORKLOAD, "form": f"mixed FP32 + {fast_sensor} sensor"
+                   + (" (network on tensor cores)" if args.sensor_tensor_cores and learned is not None else ""),
                    "l2": "working set per step > L2 (state, 3 registers, metrics, face buffers ~ 0.5 GB)",
                    "parallelism": f"replicas x{ws}"},
         "forms": {

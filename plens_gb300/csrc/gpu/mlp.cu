@@ -408,169 +408,182 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, (P <= 4 ? 3 : 1)) k_senso
     }
 }
 
-// The same inference with the two hidden layers on the tensor cores (mlp_tc.cuh): tiles of 128
-// cells per block; the eight warps compute the inputs of 16 cells each (as above), one thread
-// issues each layer's 24 tcgen05.mma, and every thread applies bias and GELU to its row's 32
-// accumulator columns. One block per SM (137 KB of shared memory).
+// The same inference with the two hidden layers on the tensor cores (mlp_tc.cuh), in two kernels:
+// k_sensor_inputs computes every cell's network input at full occupancy and writes it, already
+// split into TF32 hi/lo parts, in the shared-memory image of its 128-cell tile (the canonical
+// operand layout: a tile is one contiguous 64 KB block); k_sensor_mlp_tc then moves a tile with
+// one TMA bulk copy, runs each hidden layer as 24 tcgen05.mma, and every thread finishes its own
+// row (bias, GELU, the output layer) from the accumulator in tensor memory.
 constexpr int kTcParams = 4 * tc::kK * tc::kN + 3 * tc::kN + 4;  // W1 hi/lo, W2 hi/lo, b1, b2, w3, b3 (+pad)
+constexpr int kTileFloats = 2 * tc::kRows * tc::kK;              // A hi + A lo of one tile
 
 template <int P>
-struct TcSmem {
-    static constexpr int SV = InferScratch<P>::V, per_warp = 2 * SV + 64;
-    static constexpr size_t oB = 0;                                       // 4 x [64][64] operand layout
-    static constexpr size_t oBias = oB + 4 * tc::kK * tc::kN;            // b1, b2, w3, b3
-    static constexpr size_t oAhi = oBias + 256;
-    static constexpr size_t oAlo = oAhi + tc::kRows * tc::kK;
-    static constexpr size_t oRed = oAlo + tc::kRows * tc::kK;             // [128][2]
-    static constexpr size_t oMod = oRed + 2 * tc::kRows;                  // [128]
-    static constexpr size_t oScr = oMod + tc::kRows;
-    static constexpr size_t floats = oScr + 8 * per_warp;
-    static constexpr size_t bytes = floats * sizeof(float);
-};
-
-template <int P>
-__global__ void __launch_bounds__(256, 1) k_sensor_infer_tc(Dev dv, const float* __restrict__ Wtc, GasP g, BlendP bp,
-                                                             Ops ops, Interp ip, double* out, int gated,
-                                                             const uint8_t* mask)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, (P <= 4 ? 3 : 1))
+    k_sensor_inputs(Dev dv, GasP g, BlendP bp, Ops ops, Interp ip, float* __restrict__ tiles, float* __restrict__ mod,
+                    int gated, const uint8_t* mask)
 {
     constexpr int P3 = P * P * P, NPL = (P3 + 31) / 32;
-    using L = TcSmem<P>;
-    extern __shared__ __align__(128) float smem_tc[];
-    float* smem_f = smem_tc;
-    __shared__ __align__(8) uint64_t bar;
+    using SC = InferScratch<P>;
+    extern __shared__ __align__(16) float smem_in[];
+    float* sv = smem_in + (threadIdx.x >> 5) * (2 * SC::V + 64);
+    float* st = sv + SC::V;
+    float* sx = st + SC::V;
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *dv.lo_count = 0;  // this stage's troubled-cell list
+    if (gated && s->sensor_fallback) return;
+    const float gm = f64_to_f32(g.gamma);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * kWarpsPerBlock;
+    int64_t cell = (int64_t)blockIdx.x * kWarpsPerBlock + warp;
+    float u[NPL][5];
+    if (cell < dv.nc) load_cell_f32<P, NPL>(dv, cell, lane, u);
+    for (; cell < dv.nc; cell += stride) {
+        float un[NPL][5];  // next cell's state, in flight during this cell's work
+        if (cell + stride < dv.nc) load_cell_f32<P, NPL>(dv, cell + stride, lane, un);
+        features_from_state<P, NPL, 1>(dv, cell, gm, ip, u, sv, st, sx);
+        float am = -1.0f;
+        if (mask && mask[cell]) am = modal_alpha_warp<P, NPL>(ops, bp, gm, u, sv, st);
+        float* t = tiles + (cell / tc::kRows) * kTileFloats;
+        const int row = (int)(cell % tc::kRows);
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int k = lane + 32 * j;
+            const float x = sx[k], hi = tc::tf32_hi(x);
+            t[tc::core_off(row, k)] = hi;
+            t[tc::kRows * tc::kK + tc::core_off(row, k)] = x - hi;
+        }
+        if (lane == 0) mod[cell] = am;
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < NPL; ++j)
+#pragma unroll
+            for (int v = 0; v < 5; ++v) u[j][v] = un[j][v];
+    }
+}
+
+struct TcMlpSmem {
+    static constexpr size_t oB = 0;                                  // W1 hi/lo, W2 hi/lo, biases
+    static constexpr size_t oA = (kTcParams + 31) / 32 * 32;        // tile: A hi, A lo
+    static constexpr size_t bytes = (oA + kTileFloats) * sizeof(float);
+};
+
+__global__ void __launch_bounds__(128, 1) k_sensor_mlp_tc(Dev dv, const float* __restrict__ Wtc,
+                                                          const float* __restrict__ tiles,
+                                                          const float* __restrict__ mod, BlendP bp, double* out,
+                                                          int gated)
+{
+    extern __shared__ __align__(128) float smem_mlp[];
+    __shared__ __align__(8) uint64_t bar_ld, bar_mma;
     __shared__ uint32_t tmem_base;
-    float* sB = smem_f + L::oB;
+    float* sB = smem_mlp + TcMlpSmem::oB;
+    float* sAhi = smem_mlp + TcMlpSmem::oA;
+    float* sAlo = sAhi + tc::kRows * tc::kK;
     const float* W1hi = sB;
     const float* W1lo = sB + tc::kK * tc::kN;
     const float* W2hi = sB + 2 * tc::kK * tc::kN;
     const float* W2lo = sB + 3 * tc::kK * tc::kN;
-    const float* b1 = smem_f + L::oBias;
+    const float* b1 = sB + 4 * tc::kK * tc::kN;
     const float* b2 = b1 + 64;
     const float* w3 = b2 + 64;
-    float* sAhi = smem_f + L::oAhi;
-    float* sAlo = smem_f + L::oAlo;
-    float* sRed = smem_f + L::oRed;
-    float* sMod = smem_f + L::oMod;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    float* sv = smem_f + L::oScr + warp * L::per_warp;
-    float* st = sv + L::SV;
-    float* sx = st + L::SV;
     Scalars* s = dv.sc;
     if (!s->active) return;
-    if (blockIdx.x == 0 && tid == 0) *dv.lo_count = 0;  // this stage's troubled-cell list
     if (gated && s->sensor_fallback) return;
-    {
-        const float4* src = reinterpret_cast<const float4*>(Wtc);
-        float4* dst = reinterpret_cast<float4*>(smem_f);
-        for (int i = tid; i < kTcParams / 4; i += blockDim.x) dst[i] = src[i];
-    }
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t ntiles = (dv.nc + tc::kRows - 1) / tc::kRows;
     if (warp == 0) tc::tmem_alloc(&tmem_base);
     if (tid == 0) {
-        mbar_init(&bar, 1);
+        mbar_init(&bar_ld, 1);
+        mbar_init(&bar_mma, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        int64_t t0 = blockIdx.x;
+        mbar_arrive_expect_tx(&bar_ld, (uint32_t)(kTcParams * 4 + kTileFloats * 4));
+        tma_load_1d(sB, Wtc, (uint32_t)(kTcParams * 4), &bar_ld);
+        tma_load_1d(sAhi, tiles + t0 * kTileFloats, (uint32_t)(kTileFloats * 4), &bar_ld);
     }
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = tmem_base;
-    const float cut = fmaxf(f64_to_f32(bp.amin), kLearnedCut), amax = f64_to_f32(bp.amax), b3 = w3[64];
-    const float gm = f64_to_f32(g.gamma);
-    const int q = warp & 3, h = warp >> 2, row_e = 32 * q + lane;
-    const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * h);
-    const int64_t ntiles = (dv.nc + tc::kRows - 1) / tc::kRows;
-    uint32_t phase = 0;
+    const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+    const int row = 32 * warp + lane;
+    const float cut = fmaxf(f64_to_f32(bp.amin), kLearnedCut), amax = f64_to_f32(bp.amax);
+    uint32_t ph_ld = 0, ph_mma = 0;
     bool ok = true;
-    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        // inputs: warp w fills rows 16w .. 16w+15
-        float u[NPL][5];
-        const int64_t c0 = tile * tc::kRows + 16 * warp;
-        if (c0 < dv.nc) load_cell_f32<P, NPL>(dv, c0, lane, u);
-        for (int r = 0; r < 16; ++r) {
-            const int row = 16 * warp + r;
-            const int64_t cell = c0 + r;
-            if (cell < dv.nc) {
-                float un[NPL][5];
-                if (r < 15 && cell + 1 < dv.nc) load_cell_f32<P, NPL>(dv, cell + 1, lane, un);
-                features_from_state<P, NPL, 1>(dv, cell, gm, ip, u, sv, st, sx);
-                float am = -1.0f;
-                if (mask && mask[cell]) am = modal_alpha_warp<P, NPL>(ops, bp, gm, u, sv, st);
-                if (lane == 0) sMod[row] = am;
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    const int k = lane + 32 * j;
-                    const float x = sx[k], hi = tc::tf32_hi(x);
-                    sAhi[tc::core_off(row, k)] = hi;
-                    sAlo[tc::core_off(row, k)] = x - hi;
-                }
-                __syncwarp();
-#pragma unroll
-                for (int j = 0; j < NPL; ++j)
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) u[j][v] = un[j][v];
-            } else {
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    sAhi[tc::core_off(row, lane + 32 * j)] = 0.0f;
-                    sAlo[tc::core_off(row, lane + 32 * j)] = 0.0f;
-                }
-                if (lane == 0) sMod[row] = -1.0f;
-            }
-        }
-        float v[32];
-        for (int layer = 0; layer < 2; ++layer) {
-            tc::fence_smem_async();
-            tc::fence_before();
-            __syncthreads();
-            if (tid == 0) {
-                tc::fence_after();
-                if (layer == 0) tc::layer_mma(tmem, sAhi, sAlo, W1hi, W1lo);
-                else tc::layer_mma(tmem, sAhi, sAlo, W2hi, W2lo);
-                tc::mma_commit(&bar);
-            }
-            bool done = false;
-            for (int it = 0; it < (1 << 22) && !done; ++it) done = mbar_try_wait(&bar, phase);
-            ok = __syncthreads_and(done ? 1 : 0) != 0;
-            if (!ok) break;
-            phase ^= 1;
-            tc::fence_after();
-            tc::tmem_ld32(taddr, v);
-            if (layer == 0) {
-#pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const int col = 32 * h + i;
-                    const float x = gelu(v[i] + b1[col]), hi = tc::tf32_hi(x);
-                    sAhi[tc::core_off(row_e, col)] = hi;
-                    sAlo[tc::core_off(row_e, col)] = x - hi;
-                }
-            } else {
-                float z = 0.0f;
-#pragma unroll
-                for (int i = 0; i < 32; ++i) z += w3[32 * h + i] * gelu(v[i] + b2[32 * h + i]);
-                sRed[2 * row_e + h] = z;
-            }
-        }
+    auto wait = [&](uint64_t* bar, uint32_t& ph) {
+        bool done = false;
+        for (int it = 0; it < (1 << 22) && !done; ++it) done = mbar_try_wait(bar, ph);
+        ok = __syncthreads_and(done ? 1 : 0) != 0;
+        if (ok) ph ^= 1;
+    };
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        wait(&bar_ld, ph_ld);  // this tile's inputs (and, first, the weights) are in shared memory
         if (!ok) break;
+        float v[2][32];
+        // hidden layer 1: the accumulator, plus bias and GELU, becomes hidden layer 2's input
+        if (tid == 0) {
+            tc::fence_after();
+            tc::layer_mma(tmem, sAhi, sAlo, W1hi, W1lo);
+            tc::mma_commit(&bar_mma);
+        }
+        wait(&bar_mma, ph_mma);
+        if (!ok) break;
+        tc::fence_after();
+        tc::tmem_ld32(taddr, v[0]);
+        tc::tmem_ld32(taddr + 32, v[1]);
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                const int col = 32 * hh + i;
+                const float x = gelu(v[hh][i] + b1[col]), hi = tc::tf32_hi(x);
+                sAhi[tc::core_off(row, col)] = hi;
+                sAlo[tc::core_off(row, col)] = x - hi;
+            }
+        tc::fence_smem_async();
         tc::fence_before();
         __syncthreads();
-        if (h == 0) {
-            const int64_t cell = tile * tc::kRows + row_e;
-            if (cell < dv.nc) {
-                const float z = sRed[2 * row_e] + sRed[2 * row_e + 1] + b3;
-                const float at = amax / (1.0f + expf(-z)), am = sMod[row_e];
-                double a = (am >= 0.0f) ? f32_to_f64(am) : ((at < cut) ? 0.0 : f32_to_f64(at));
-                if (dv.cell_wall[cell]) {
-                    const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
-                    a = (wl > a) ? wl : a;
-                }
-                out[cell] = a;
-            }
+        // hidden layer 2
+        if (tid == 0) {
+            tc::fence_after();
+            tc::layer_mma(tmem, sAhi, sAlo, W2hi, W2lo);
+            tc::mma_commit(&bar_mma);
         }
-        __syncthreads();  // the operand and reduction buffers are reused by the next tile
+        wait(&bar_mma, ph_mma);
+        if (!ok) break;
+        tc::fence_after();
+        tc::tmem_ld32(taddr, v[0]);
+        tc::tmem_ld32(taddr + 32, v[1]);
+        float z = w3[64];  // b3 (the weights arrived with the first tile)
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+            for (int i = 0; i < 32; ++i) z += w3[32 * hh + i] * gelu(v[hh][i] + b2[32 * hh + i]);
+        const int64_t cell = tile * tc::kRows + row;
+        if (cell < dv.nc) {
+            const float at = amax / (1.0f + expf(-z)), am = mod[cell];
+            double a = (am >= 0.0f) ? f32_to_f64(am) : ((at < cut) ? 0.0 : f32_to_f64(at));
+            if (dv.cell_wall[cell]) {
+                const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
+                a = (wl > a) ? wl : a;
+            }
+            out[cell] = a;
+        }
+        tc::fence_before();
+        __syncthreads();  // every row has read the accumulator and the tile buffer is free
+        const int64_t next = tile + gridDim.x;
+        if (tid == 0 && next < ntiles) {
+            tc::fence_after();
+            mbar_arrive_expect_tx(&bar_ld, (uint32_t)(kTileFloats * 4));
+            tma_load_1d(sAhi, tiles + next * kTileFloats, (uint32_t)(kTileFloats * 4), &bar_ld);
+        }
     }
     if (!ok) {
         if (tid == 0) s->err = PLENS_GPU_E_TIMEOUT;
-        for (int it = 0; it < (1 << 22); ++it)  // the MMAs in flight complete before the TMEM goes
-            if (mbar_try_wait(&bar, phase)) break;
+        for (int it = 0; it < (1 << 22); ++it)  // copies and MMAs in flight complete first
+            if (mbar_try_wait(&bar_ld, ph_ld)) break;
+        for (int it = 0; it < (1 << 22); ++it)
+            if (mbar_try_wait(&bar_mma, ph_mma)) break;
     }
     tc::fence_before();
     __syncthreads();
@@ -637,24 +650,30 @@ __global__ void k_features(Dev dv, GasP g, Interp ip, float* x)
 }
 
 template <int P>
-int launch_infer_tc(const Dev& dv, const float* Wtc, const GasP& g, const BlendP& bp, const Ops& ops, double* out,
+int launch_infer_tc(MlpDevice& m, const Dev& dv, const GasP& g, const BlendP& bp, const Ops& ops, double* out,
                     int gated, const uint8_t* mask, cudaStream_t st)
 {
     const Interp ip = make_interp(P);
-    const size_t bytes = TcSmem<P>::bytes;
-    static int nsm = 0;
-    if (!nsm) {
-        cudaFuncSetAttribute(k_sensor_infer_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        int dev = 0;
+    const size_t in_bytes = sizeof(float) * kWarpsPerBlock * (2 * InferScratch<P>::V + 64);
+    static int in_blocks = 0, nsm = 0;
+    if (!in_blocks) {
+        cudaFuncSetAttribute(k_sensor_inputs<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)in_bytes);
+        int dev = 0, occ = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        if (nsm < 1) nsm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sensor_inputs<P>, 32 * kWarpsPerBlock, in_bytes);
+        nsm = std::max(1, nsm);
+        in_blocks = std::max(1, occ) * nsm;
+        cudaFuncSetAttribute(k_sensor_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TcMlpSmem::bytes);
     }
     const int64_t tiles = (dv.nc + tc::kRows - 1) / tc::kRows;
     if (tiles < 1) return 0;
-    const int64_t blocks = std::min<int64_t>(tiles, nsm);
-    k_sensor_infer_tc<P><<<(unsigned)blocks, 256, bytes, st>>>(dv, Wtc, g, bp, ops, ip, out, gated, mask);
-    return 1;
+    const int64_t blocks = std::min<int64_t>((dv.nc + kWarpsPerBlock - 1) / kWarpsPerBlock, in_blocks);
+    k_sensor_inputs<P><<<(unsigned)blocks, 32 * kWarpsPerBlock, in_bytes, st>>>(dv, g, bp, ops, ip, m.tiles, m.mod,
+                                                                             gated, mask);
+    k_sensor_mlp_tc<<<(unsigned)std::min<int64_t>(tiles, nsm), 128, TcMlpSmem::bytes, st>>>(dv, m.params_tc, m.tiles,
+                                                                                         m.mod, bp, out, gated);
+    return 2;
 }
 
 template <int P>
@@ -703,7 +722,7 @@ int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, con
     b0.gate = 0;
     b0.mask = nullptr;
     if (m.judge_this_step) {
-        n += m.use_tc ? launch_infer_tc<P>(dv, m.params_tc, g, bp, ops, m.alpha_plain, 0, nullptr, st)
+        n += m.use_tc ? launch_infer_tc<P>(m, dv, g, bp, ops, m.alpha_plain, 0, nullptr, st)
                       : launch_infer<P>(dv, m.params_t, g, bp, ops, m.alpha_plain, 0, nullptr, st);
         n += launch_blender<P>(dv, ops, g, b0, st);
         const unsigned grid = (unsigned)((dv.nc + 127) / 128);
@@ -714,7 +733,7 @@ int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, con
     } else {
         // the cells the judge handed back get the plain indicator inside the inference kernel;
         // the plain blender itself runs only in whole-domain fallback
-        n += m.use_tc ? launch_infer_tc<P>(dv, m.params_tc, g, bp, ops, dv.alpha_raw, 1, m.mask, st)
+        n += m.use_tc ? launch_infer_tc<P>(m, dv, g, bp, ops, dv.alpha_raw, 1, m.mask, st)
                       : launch_infer<P>(dv, m.params_t, g, bp, ops, dv.alpha_raw, 1, m.mask, st);
         BlendP b1 = bp;
         b1.gate = 1;
@@ -736,6 +755,17 @@ int mlp_create(MlpDevice& m, int64_t nc, std::vector<void*>& allocs)
     allocs.push_back(m.params_t);
     if (cudaMalloc(&m.params_tc, sizeof(float) * kTcParams) != cudaSuccess) return 1;
     allocs.push_back(m.params_tc);
+    {
+        // network inputs in tile images (rows past the last cell stay zero) and the plain
+        // indicator of handed-back cells
+        const int64_t ntiles = (nc + tc::kRows - 1) / tc::kRows;
+        if (cudaMalloc(&m.tiles, sizeof(float) * kTileFloats * ntiles) != cudaSuccess ||
+            cudaMemset(m.tiles, 0, sizeof(float) * kTileFloats * ntiles) != cudaSuccess)
+            return 1;
+        allocs.push_back(m.tiles);
+        if (cudaMalloc(&m.mod, sizeof(float) * nc) != cudaSuccess) return 1;
+        allocs.push_back(m.mod);
+    }
     if (cudaMalloc(&m.alpha_plain, sizeof(double) * (nc + 1)) != cudaSuccess) return 1;
     allocs.push_back(m.alpha_plain);
     if (cudaMalloc(&m.maxerr, sizeof(unsigned long long)) != cudaSuccess) return 1;

@@ -19,7 +19,9 @@ struct MlpDevice {
     float* params = nullptr;        // [kMlpParams] W1 b1 W2 b2 w3 b3
     float* params_t = nullptr;      // the same with W1, W2 transposed (CUDA-core inference kernel)
     float* params_tc = nullptr;     // W1, W2 as TF32 hi/lo tensor-core operands, then the biases
-    bool use_tc = false;            // the inference kernel with the hidden layers on the tensor cores
+    float* tiles = nullptr;         // tensor-core form: network inputs, one 64 KB operand image per 128 cells
+    float* mod = nullptr;           // tensor-core form: plain-indicator alpha of handed-back cells (-1: none)
+    bool use_tc = false;            // the inference kernels with the hidden layers on the tensor cores
     double* alpha_plain = nullptr;  // [nc] judge: MLP alpha of the judged stage
     unsigned long long* maxerr = nullptr;  // order-preserving max per-cell alpha error
     uint8_t* mask = nullptr;        // [nc] cells handed back to the plain indicator by the judge
