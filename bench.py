@@ -60,8 +60,43 @@ def _traffic_from_profile(name: str):
     return None
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes (the library the driver installs): SM clock, its
+    maximum and the active clock-event (throttle) reasons of one GPU."""
+
+    SW_POWER_CAP, HW_SLOWDOWN, SW_THERMAL, HW_THERMAL = 0x4, 0x8, 0x20, 0x40
+
+    def __init__(self, index: int):
+        import ctypes
+        self.C = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sm_clock(self) -> int:
+        v = self.C.c_uint()
+        self.lib.nvmlDeviceGetClockInfo(self.h, 1, self.C.byref(v))  # NVML_CLOCK_SM
+        return v.value
+
+    def sm_max(self) -> int:
+        v = self.C.c_uint()
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, self.C.byref(v))
+        return v.value
+
+    def reasons(self) -> int:
+        v = self.C.c_ulonglong()
+        self.reasons_fn(self.h, self.C.byref(v))
+        return v.value
+
+
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """Clock / throttle sampling during the timed region: NVML polled every 2 ms from a thread
+    (the timed regions are tens of milliseconds), else nvidia-smi at its 200 ms period."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -70,9 +105,31 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.idx = gpu_index
         self.proc = None
-        self.path = Path(tempfile.mkstemp(prefix="clocks_", suffix=".csv")[1])
+        self.thread = None
+        self.samples = []
+        self.nvml = None
+        try:
+            self.nvml = _Nvml(gpu_index)
+            self.max_mhz = self.nvml.sm_max()
+        except Exception:
+            self.nvml = None
+        self.path = None if self.nvml else Path(tempfile.mkstemp(prefix="clocks_", suffix=".csv")[1])
+
+    def _poll(self):
+        while not self.stop.is_set():
+            try:
+                self.samples.append((self.nvml.sm_clock(), self.nvml.reasons()))
+            except Exception:
+                pass
+            self.stop.wait(0.002)
 
     def __enter__(self):
+        if self.nvml is not None:
+            import threading
+            self.stop = threading.Event()
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
@@ -82,6 +139,9 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
+        if self.thread is not None:
+            self.stop.set()
+            self.thread.join(timeout=5)
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -90,6 +150,14 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            if not self.samples:
+                return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["unsampled"], "source": "nvml"}
+            names = ((_Nvml.HW_SLOWDOWN, "hw_slowdown"), (_Nvml.HW_THERMAL, "hw_thermal_slowdown"),
+                     (_Nvml.SW_THERMAL, "sw_thermal_slowdown"), (_Nvml.SW_POWER_CAP, "sw_power_cap"))
+            reasons = sorted({n for _, r in self.samples for bit, n in names if r & bit})
+            return {"sm_mhz": statistics.median(c for c, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                    "reasons": reasons, "samples": len(self.samples), "source": "nvml, 2 ms"}
         try:
             rows = [r.split(",") for r in self.path.read_text().strip().splitlines() if r.strip()]
         except Exception:
