@@ -115,6 +115,12 @@ typedef struct plens_params {
     int32_t do_filtering;              /* TV filter (blender_calculator.cc:196-259) */
     /* time integration */
     int32_t rk_order;          /* 4: RK4(3)5[3R+]N; 3: SSP-RK3 */
+    /* local time stepping (calc_time_step, dgsem/plens.cc:3880-3911) */
+    int32_t local_stepping;        /* "request local stepping" */
+    int32_t limit_local_step;      /* "limit local time step" */
+    double local_start_time;       /* per-cell steps only while t > this ("local stepping start time") */
+    double local_nbr_factor;       /* dt_c <= factor * unlimited dt of each interior-face neighbour */
+    double local_global_factor;    /* dt_c <= factor * global dt */
     /* precision / learned sensor (new; no counterpart in the reference) */
     int32_t precision;         /* enum plens_precision */
     int32_t sensor;            /* enum plens_sensor */

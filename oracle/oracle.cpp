@@ -1085,11 +1085,17 @@ struct Oracle {
     }
 
     // -------------------------------------------------------- calc_time_step (plens.cc:3810-3912)
+    // Returns the global step; loc_dt receives what multiplies each cell's RHS: the per-cell
+    // stable step, limited by the neighbours' unlimited steps and the global one, while local
+    // stepping is requested and t > its start time, else the global step (plens.cc:3876-3911).
+    std::vector<double> cell_dt, loc_dt;
     double calc_time_step()
     {
         double Co = ev(Pm.expr_courant, 0, 0, 0, time);
         if (Co >= 1) Co = 0.9;
         double proc = 1e6;
+        cell_dt.assign(nc, 0.0);
+        loc_dt.assign(nc, 0.0);
 #pragma omp parallel for reduction(min : proc)
         for (int64_t c = 0; c < nc; ++c) {
             double cell_step = 1e6;
@@ -1106,7 +1112,25 @@ struct Oracle {
                 const double cur = Co / (std::pow(N, 1.5) * (madv + a / h + N * N * mu[dof] / (h * h * cs[0])));
                 if (cur < cell_step) cell_step = cur;
             }
+            cell_dt[c] = cell_step;
             if (cell_step < proc) proc = cell_step;
+        }
+        const bool local = Pm.local_stepping && time > Pm.local_start_time;
+#pragma omp parallel for
+        for (int64_t c = 0; c < nc; ++c) {
+            double m = proc;
+            if (local) {
+                m = cell_dt[c];
+                if (Pm.limit_local_step) {
+                    // interior faces only: a periodic face is a boundary face (cell_nbr = -1)
+                    for (int f = 0; f < 6; ++f) {
+                        const int32_t nb = cell_nbr[6 * c + f];
+                        if (nb >= 0) m = std::min(m, Pm.local_nbr_factor * cell_dt[nb]);
+                    }
+                    m = std::min(m, Pm.local_global_factor * proc);
+                }
+            }
+            loc_dt[c] = m;
         }
         return proc;
     }
@@ -1124,14 +1148,14 @@ struct Oracle {
                               582400652113.0 / 7078426004906, b_[3]};
         int st = calc_rhs();
         if (st) return st;
-        // loc_time_steps holds the unclipped global step and multiplies the RHS; only the clock
-        // uses the step clipped to end_time (dgsem/plens.cc:3903-3911, 4339-4341, 3925-3940)
+        // loc_time_steps (unclipped; per cell under local stepping) multiplies the RHS; only the
+        // clock uses the global step clipped to end_time (dgsem/plens.cc:3903-3911, 4339-4341,
+        // 3925-3940)
         dt = calc_time_step();
-        const double dt_update = dt;
         if (dt > (end_time - time)) dt = end_time - time;
         auto mult = [&]() {
 #pragma omp parallel for
-            for (int64_t i = 0; i < 5 * nd; ++i) R[i] = R[i] * dt_update;
+            for (int64_t i = 0; i < 5 * nd; ++i) R[i] = R[i] * loc_dt[(i % nd) / P3];
         };
         mult();
         if (Pm.rk_order == 4) {
@@ -1275,6 +1299,16 @@ int oracle_rhs(void* h, double* R, double* alpha, double* alpha_d, double* avars
     if (alpha_d) std::memcpy(alpha_d, o->alpha_d.data(), sizeof(double) * o->nc);
     if (avars) std::memcpy(avars, o->avars.data(), sizeof(double) * 9 * o->nd);
     return 0;
+}
+
+// what multiplies each cell's RHS in the last calc_time_step (loc_time_steps)
+int oracle_loc_time_steps(void* h, double* out)
+{
+    auto* o = static_cast<Oracle*>(h);
+    if (!o || !out) return PLENS_GPU_E_INVALID;
+    if ((int64_t)o->loc_dt.size() != o->nc) return PLENS_GPU_E_INVALID;
+    for (int64_t c = 0; c < o->nc; ++c) out[c] = o->loc_dt[c];
+    return PLENS_GPU_OK;
 }
 
 int oracle_time_step(void* h, double* dt)

@@ -36,6 +36,7 @@ def lib() -> C.CDLL:
         L.oracle_get_state.argtypes = [vp, vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(dbl)]
         L.oracle_rhs.argtypes = [vp, vp, vp, vp, vp]
         L.oracle_time_step.argtypes = [vp, C.POINTER(dbl)]
+        L.oracle_loc_time_steps.argtypes = [vp, vp]
         L.oracle_advance.argtypes = [vp, i64, dbl]
         L.oracle_first_bad_dof.argtypes = [vp]
         L.oracle_first_bad_dof.restype = i64
@@ -106,6 +107,12 @@ class Oracle:
         dt = C.c_double()
         self.L.oracle_time_step(self.h, C.byref(dt))
         return dt.value
+
+    def loc_time_steps(self):
+        """Per-cell factor of the RHS from the last time-step calculation (loc_time_steps)."""
+        out = np.empty(self.n_cells)
+        self._status(self.L.oracle_loc_time_steps(self.h, _p(out)), "loc_time_steps")
+        return out
 
     def advance(self, n_steps, end_time=1e300):
         self._status(self.L.oracle_advance(self.h, n_steps, end_time), "advance")

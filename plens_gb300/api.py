@@ -59,6 +59,8 @@ class Params(C.Structure):
         ("sharpness_factor", C.c_double), ("alpha_min", C.c_double), ("alpha_max", C.c_double),
         ("expr_wall_blender_limit", C.c_int32), ("expr_vis_blending_region", C.c_int32),
         ("expr_courant", C.c_int32), ("do_filtering", C.c_int32), ("rk_order", C.c_int32),
+        ("local_stepping", C.c_int32), ("limit_local_step", C.c_int32), ("local_start_time", C.c_double),
+        ("local_nbr_factor", C.c_double), ("local_global_factor", C.c_double),
         ("precision", C.c_int32), ("sensor", C.c_int32), ("judge_every", C.c_int32),
         ("judge_alpha_tol", C.c_double),
         ("n_bc", C.c_int32), ("bcs", C.POINTER(BCDesc)),

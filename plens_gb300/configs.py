@@ -223,8 +223,20 @@ end
     return prm, {}, degree
 
 
+def _local_stepping(local: dict | None) -> str:
+    """The "time integration" lines of local time stepping: ``local`` = dict(start=t0,
+    limit=bool, neighbor=factor, global_=factor); None keeps global stepping."""
+    if not local:
+        return ""
+    return (f"    set request local stepping = true\n"
+            f"    set local stepping start time = {local.get('start', 0.0)!r}\n"
+            f"    set limit local time step = {'true' if local.get('limit', False) else 'false'}\n"
+            f"    set local step neighbor factor = {local.get('neighbor', 1.05)!r}\n"
+            f"    set local step global factor = {local.get('global_', 1000.0)!r}\n")
+
+
 def cylinder(n_radial: int = 160, n_azimuthal: int = 128, precision="fp64", sensor="modal",
-             end_time=1e9, courant=0.3, mapping_degree_note=True):
+             end_time=1e9, courant=0.3, mapping_degree_note=True, local: dict | None = None):
     gamma, Rgas, Tinf, Mach, Re, D = 1.4, 287.0, 200.0, 8.0, 1e5, 2.0
     pinf = 100.0
     rho = pinf / (Rgas * Tinf)
@@ -315,7 +327,7 @@ subsection time integration
     set RK order = 4
     set Courant number = {courant}
     set end time = {end_time}
-end
+{_local_stepping(local)}end
 subsection data output
     set write frequency = 1000000
 end

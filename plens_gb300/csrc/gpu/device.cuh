@@ -119,8 +119,17 @@ struct Dev {
     double* avars;     // [9][nd]
     int32_t* lo_list;  // compacted troubled-cell list
     int32_t* lo_count;
+    // local time stepping (null unless requested): per-cell stable step, and what multiplies
+    // each cell's RHS (loc_time_steps)
+    double *dt_cell, *dt_loc;
     Scalars* sc;
 };
+
+// the factor of a cell's RHS: its local step, or the unclipped global step
+__device__ __forceinline__ double rhs_step(const Dev& dv, int64_t cell)
+{
+    return dv.dt_loc ? dv.dt_loc[cell] : dv.sc->dt_update;
+}
 
 __device__ __forceinline__ double eval_expr(const Dev& dv, int idx, double x, double y, double z, double t)
 {

@@ -163,6 +163,68 @@ __global__ void __launch_bounds__(256) k_time_step(Dev dv, GasP g, double N15, i
     }
 }
 
+// Local time stepping: the same per-dof bound, reduced per cell (one warp per cell) into
+// dt_cell and over all cells into the global minimum (calc_time_step, dgsem/plens.cc:3836-3872).
+template <int P, class T>
+__global__ void __launch_bounds__(256) k_time_step_cells(Dev dv, GasP g, double N15, int N)
+{
+    constexpr int P3 = P * P * P;
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    __shared__ double s_red[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t cell = blockIdx.x * 8ll + warp;
+    const T Co = to_real<T>(s->courant);
+    T local = T(1e6);
+    if (cell < dv.nc)
+        for (int l = lane; l < P3; l += 32) {
+            const T cur = dof_stable_step<P, T>(dv, g, N15, N, cell * P3 + l, Co);
+            if (cur < local) local = cur;
+        }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const T o = __shfl_xor_sync(0xffffffffu, local, off);
+        if (o < local) local = o;
+    }
+    const double cd = to_f64<T>(local);
+    if (lane == 0) {
+        if (cell < dv.nc) dv.dt_cell[cell] = cd;
+        s_red[warp] = cd;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = s_red[0];
+        for (int w = 1; w < 8; ++w)
+            if (s_red[w] < m) m = s_red[w];
+        atomicMin(&s->dtmin, ord_double(m));
+    }
+}
+
+// loc_time_steps after the global reduction (dgsem/plens.cc:3880-3911): while local stepping is
+// on (t > start), each cell's own step, optionally limited by factor x the unlimited steps of its
+// interior-face neighbours (a periodic face is a boundary face: cell_nbr = -1) and by factor x
+// the global step; otherwise the global step. All from the unclipped global step.
+static __global__ void k_local_dt(Dev dv, int limit, double start_time, double nbr_factor, double global_factor)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= dv.nc) return;
+    const double dtg = s->dt_update;
+    double m = dtg;
+    if (s->time > start_time) {
+        m = dv.dt_cell[c];
+        if (limit) {
+            for (int f = 0; f < 6; ++f) {
+                const int32_t nb = dv.cell_nbr[6 * c + f];
+                if (nb >= 0) m = fmin(m, nbr_factor * dv.dt_cell[nb]);
+            }
+            m = fmin(m, global_factor * dtg);
+        }
+    }
+    dv.dt_loc[c] = m;
+}
+
 // Courant number of the step from its expression of t (capped to 0.9 when >= 1,
 // dgsem/plens.cc:3815-3823).
 static __global__ void k_courant(Dev dv, int expr_courant)
@@ -1214,7 +1276,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
             for (int v = 0; v < 5; ++v) sa.Rout[v * dv.nd + dof] = f32_to_f64(R[v]);
             return;
         }
-        const float dtu = f64_to_f32(s->dt_update);
+        const float dtu = f64_to_f32(rhs_step(dv, cell));
 #pragma unroll
         for (int v = 0; v < 5; ++v) ud[v] = dv.U[v * dv.nd + dof];
 #pragma unroll
@@ -1255,7 +1317,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
         for (int v = 0; v < 5; ++v) sa.Rout[v * dv.nd + dof] = R[v];
         return;
     }
-    const double dtu = s->dt_update;
+    const double dtu = rhs_step(dv, cell);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
         const double Rs = R[v] * dtu;

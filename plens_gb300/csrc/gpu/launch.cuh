@@ -107,6 +107,10 @@ struct Launch {
     }
     static int time_step(const Dev& dv, const GasP& g, double N15, int N, cudaStream_t st)
     {
+        if (dv.dt_cell) {  // local stepping: per-cell steps as well
+            k_time_step_cells<P, T><<<(unsigned)((dv.nc + 7) / 8), 256, 0, st>>>(dv, g, N15, N);
+            return 1;
+        }
         const int64_t per_block = 256 * kStepItems<T>;
         const int grid = (int)((dv.nd + per_block - 1) / per_block);
         k_time_step<P, T><<<grid, 256, 0, st>>>(dv, g, N15, N);

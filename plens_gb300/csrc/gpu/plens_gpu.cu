@@ -281,6 +281,12 @@ int launch_time_step(plens_ctx* c)
     c->launches += c->tab.time_step(c->dv, c->gas, c->N15, c->N, c->stream);
     k_dt_finalize<<<1, 1, 0, c->stream>>>(c->dv);
     c->launches += 1;
+    if (c->dv.dt_loc) {
+        k_local_dt<<<(unsigned)((c->nc + 255) / 256), 256, 0, c->stream>>>(
+            c->dv, c->prm.limit_local_step, c->prm.local_start_time, c->prm.local_nbr_factor,
+            c->prm.local_global_factor);
+        c->launches += 1;
+    }
     return check_launch(c, "time step kernels");
 }
 
@@ -557,6 +563,10 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         if ((r = dalloc(c, &d.sf3, 5 * c->nslot)) || (r = dalloc(c, &d.avars, 9 * nd))) return r;
         CK(cudaMemset(d.avars, 0, sizeof(double) * 9 * nd));
     }
+    if (prm->local_stepping) {
+        if ((r = dalloc(c, &d.dt_cell, nc)) || (r = dalloc(c, &d.dt_loc, nc))) return r;
+        CK(cudaMemset(d.dt_loc, 0, sizeof(double) * nc));
+    }
     if (c->learned) {
         if ((r = dalloc(c, &d.lo_list, nc)) || (r = dalloc(c, &d.lo_count, 1))) return r;
         if ((r = mlp_create(c->mlp, nc, c->allocs))) return fail(c, PLENS_GPU_E_CUDA, "mlp buffers");
@@ -816,7 +826,9 @@ int plens_gpu_get_cell_scalars(plens_ctx* c, double* alpha, double* alpha_d, dou
     CK(cudaStreamSynchronize(c->stream));
     if (alpha) CK(cudaMemcpy(alpha, c->dv.alpha, sizeof(double) * c->nc, cudaMemcpyDeviceToHost));
     if (alpha_d) CK(cudaMemcpy(alpha_d, c->dv.alpha_d, sizeof(double) * c->nc, cudaMemcpyDeviceToHost));
-    if (dt_cell) {
+    if (dt_cell && c->dv.dt_loc) {
+        CK(cudaMemcpy(dt_cell, c->dv.dt_loc, sizeof(double) * c->nc, cudaMemcpyDeviceToHost));
+    } else if (dt_cell) {
         Scalars h;
         CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
         for (int64_t i = 0; i < c->nc; ++i) dt_cell[i] = h.dt_update;

@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
         for (int v = 0; v < 5; ++v) sa.Rout[v * dv.nd + dof] = f32_to_f64(R[v]);
         return;
     }
-    const float dtu = f64_to_f32(s->dt_update);
+    const float dtu = f64_to_f32(rhs_step(dv, cell));
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
         const float Rs = R[v] * dtu;

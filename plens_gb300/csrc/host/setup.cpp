@@ -693,8 +693,11 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
         C.start_time = prm.get_double("time integration/start time");
         C.end_time = prm.get_double("time integration/end time");
         C.starting_output_counter = prm.get_integer("time integration/starting output counter");
-        if (prm.get_bool("time integration/request local stepping"))
-            throw std::runtime_error("local time stepping is not supported by this build");
+        pr.local_stepping = prm.get_bool("time integration/request local stepping") ? 1 : 0;
+        pr.local_start_time = prm.get_double("time integration/local stepping start time");
+        pr.limit_local_step = prm.get_bool("time integration/limit local time step") ? 1 : 0;
+        pr.local_nbr_factor = prm.get_double("time integration/local step neighbor factor");
+        pr.local_global_factor = prm.get_double("time integration/local step global factor");
         C.write_freq = prm.get_integer("data output/write frequency");
         C.output_dir = prm.get("data output/directory");
         C.base_file_name = prm.get("data output/base file name");
