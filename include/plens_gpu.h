@@ -121,6 +121,10 @@ typedef struct plens_params {
     double local_start_time;       /* per-cell steps only while t > this ("local stepping start time") */
     double local_nbr_factor;       /* dt_c <= factor * unlimited dt of each interior-face neighbour */
     double local_global_factor;    /* dt_c <= factor * global dt */
+    /* error norms of the output steps (PLENS::write, dgsem/plens.cc:4234-4243) */
+    int32_t calc_ss_error;         /* "calculate steady state error": rho E of each step start is kept */
+    int32_t calc_conv_error;       /* "convergence/calculate error" (variable: density) */
+    int32_t expr_conv_exact;       /* "convergence/exact solution": expression of x,y,z,t */
     /* precision / learned sensor (new; no counterpart in the reference) */
     int32_t precision;         /* enum plens_precision */
     int32_t sensor;            /* enum plens_sensor */
@@ -164,6 +168,11 @@ typedef struct plens_mesh_desc {
     const int32_t* ft_nbr_fdof;  /* [n_face_tasks][P^2] matching face-local dof on the other side */
     const double* ft_normal;     /* [n_face_tasks][P^2][3] unit outward normal of the owner side */
     const double* ft_xyz;        /* [n_face_tasks][P^2][3] face dof location */
+    /* QGauss(N+1) quadrature of the error norms (VectorTools::integrate_difference); null when
+     * no error norm is requested. Gauss points are numbered like the dofs (c*P^3 + i + P j + P^2 k). */
+    const double* gauss_interp;  /* [P][P]: GLL Lagrange basis i at Gauss point q, at [q*P+i] */
+    const double* q_wJ;          /* [ndof] quadrature weight x det J at the Gauss point */
+    const double* q_xyz;         /* [3][ndof] Gauss point location (convergence error only) */
 } plens_mesh_desc;
 
 typedef struct plens_ctx plens_ctx;
@@ -235,6 +244,15 @@ int plens_gpu_time_step_noalloc(const double* U, const double* Jinv, const doubl
 int plens_gpu_advance(plens_ctx* ctx, int64_t n_steps, double end_time);
 int plens_gpu_advance_async(plens_ctx* ctx, int64_t n_steps, double end_time);
 int plens_gpu_synchronize(plens_ctx* ctx);
+
+/* Error norms of the current state as PLENS::write logs them (dgsem/plens.cc:4234-4243), i.e.
+ * at stage 1 of the next step, after its time step: the steady-state error
+ * ||(rhoE - rhoE_old) / loc_dt|| / ||rhoE|| (calc_ss_error, 3985-4035; rhoE_old = rho E at the
+ * start of the previous step, zero before the first) and the L2 error of density against the
+ * exact-solution expression at the current time (calc_convergence_error, 4044-4098); L2 norms by
+ * QGauss(N+1) quadrature. Either output may be NULL; asking for a norm that was not requested at
+ * setup gives PLENS_GPU_E_INVALID. Synchronising. */
+int plens_gpu_error_norms(plens_ctx* ctx, double* ss_error, double* conv_error);
 
 /* Per-cell scalars of the last RHS: PLENS::gcrk_alpha, gcrk_alpha_d, loc_time_steps. */
 int plens_gpu_get_cell_scalars(plens_ctx* ctx, double* alpha, double* alpha_d, double* dt_cell);

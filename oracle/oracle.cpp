@@ -419,6 +419,9 @@ struct Oracle {
     std::vector<int> fmap;               // [6][P2] face dof -> cell dof
 
     std::vector<double> U, U0, R, R1, R0, avars, mu, kk, alpha, alpha_d, bvar;
+    // error norms: rho E at the start of the previous step (zero before the first), QGauss(N+1)
+    // data (GLL -> Gauss interpolation, weight x det J and location per Gauss point)
+    std::vector<double> rhoE_old, gauss, q_wJ, q_xyz;
     std::vector<double> sf;              // [5][nc*6*P2] surface flux of the current stage
     double time = 0, dt = 0;
     int64_t n_steps = 0;
@@ -1194,6 +1197,66 @@ struct Oracle {
         }
         time += dt;
         ++n_steps;
+        // PLENS::update keeps the step's starting rho E for the steady-state error (4507-4508)
+        if (!rhoE_old.empty()) std::copy(U0.begin() + 4 * nd, U0.begin() + 5 * nd, rhoE_old.begin());
+        return PLENS_GPU_OK;
+    }
+
+    // ------------------------------- calc_ss_error / calc_convergence_error (3985-4098)
+    // as write() calls them at stage 1 of the next step (after calc_rhs and calc_time_step): L2
+    // norms by QGauss(N+1) (VectorTools::integrate_difference + compute_global_error), the DG
+    // field interpolated from the GLL nodes to the Gauss points.
+    int error_norms(double* ss, double* conv)
+    {
+        if (q_wJ.empty()) return PLENS_GPU_E_INVALID;
+        if (int st = calc_rhs()) return st;
+        calc_time_step();
+        const bool want_conv = Pm.calc_conv_error && !q_xyz.empty();
+        std::vector<double> cell_sums(3 * nc, 0.0);
+#pragma omp parallel for
+        for (int64_t c = 0; c < nc; ++c) {
+            std::vector<double> a(3 * P3), b(3 * P3);
+            for (int l = 0; l < P3; ++l) {
+                const int64_t dof = c * P3 + l;
+                const double E = U[4 * nd + dof];
+                a[l] = E;
+                a[P3 + l] = rhoE_old.empty() ? 0.0 : (E - rhoE_old[dof]) / loc_dt[c];
+                a[2 * P3 + l] = U[dof];
+            }
+            for (int f = 0; f < 3; ++f)
+                for (int l = 0; l < P3; ++l) {  // along x
+                    const int i = l % P, j = (l / P) % P, k = l / P2;
+                    double s = 0;
+                    for (int m = 0; m < P; ++m) s += gauss[i * P + m] * a[f * P3 + m + P * j + P2 * k];
+                    b[f * P3 + l] = s;
+                }
+            for (int f = 0; f < 3; ++f)
+                for (int l = 0; l < P3; ++l) {  // along y
+                    const int i = l % P, j = (l / P) % P, k = l / P2;
+                    double s = 0;
+                    for (int m = 0; m < P; ++m) s += gauss[j * P + m] * b[f * P3 + i + P * m + P2 * k];
+                    a[f * P3 + l] = s;
+                }
+            double acc[3] = {0, 0, 0};
+            for (int l = 0; l < P3; ++l) {  // along z, then the quadrature
+                const int i = l % P, j = (l / P) % P, k = l / P2;
+                const int64_t q = c * P3 + l;
+                double u[3];
+                for (int f = 0; f < 3; ++f) {
+                    double s = 0;
+                    for (int m = 0; m < P; ++m) s += gauss[k * P + m] * a[f * P3 + i + P * j + P2 * m];
+                    u[f] = s;
+                }
+                if (want_conv) u[2] -= ev(Pm.expr_conv_exact, q_xyz[q], q_xyz[nd + q], q_xyz[2 * nd + q], time);
+                for (int f = 0; f < 3; ++f) acc[f] += q_wJ[q] * u[f] * u[f];
+            }
+            for (int f = 0; f < 3; ++f) cell_sums[f * nc + c] = acc[f];
+        }
+        double tot[3] = {0, 0, 0};
+        for (int f = 0; f < 3; ++f)
+            for (int64_t c = 0; c < nc; ++c) tot[f] += cell_sums[f * nc + c];
+        if (ss) *ss = std::sqrt(tot[1]) / std::sqrt(tot[0]);
+        if (conv) *conv = want_conv ? std::sqrt(tot[2]) : 0.0;
         return PLENS_GPU_OK;
     }
 };
@@ -1231,6 +1294,12 @@ void* oracle_create(const plens_mesh_desc* m, const plens_params* p)
     o->ft_nbr_fdof = cp(m->ft_nbr_fdof, nt * P2);
     o->ft_normal = cp(m->ft_normal, nt * P2 * 3);
     o->ft_xyz = cp(m->ft_xyz, nt * P2 * 3);
+    if (m->q_wJ && m->gauss_interp) {
+        o->gauss = cp(m->gauss_interp, P2);
+        o->q_wJ = cp(m->q_wJ, nd);
+        if (m->q_xyz) o->q_xyz = cp(m->q_xyz, 3 * nd);
+        if (p->calc_ss_error) o->rhoE_old.assign(nd, 0.0);
+    }
     o->bcs = cp(p->bcs, p->n_bc);
     o->expr_off = cp(p->expr_offset, p->n_expr);
     o->expr_len = cp(p->expr_length, p->n_expr);
@@ -1299,6 +1368,14 @@ int oracle_rhs(void* h, double* R, double* alpha, double* alpha_d, double* avars
     if (alpha_d) std::memcpy(alpha_d, o->alpha_d.data(), sizeof(double) * o->nc);
     if (avars) std::memcpy(avars, o->avars.data(), sizeof(double) * 9 * o->nd);
     return 0;
+}
+
+// error norms of the current state as write() logs them (see Oracle::error_norms)
+int oracle_error_norms(void* h, double* ss_error, double* conv_error)
+{
+    auto* o = static_cast<Oracle*>(h);
+    if (!o) return PLENS_GPU_E_INVALID;
+    return o->error_norms(ss_error, conv_error);
 }
 
 // what multiplies each cell's RHS in the last calc_time_step (loc_time_steps)

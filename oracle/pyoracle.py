@@ -37,6 +37,7 @@ def lib() -> C.CDLL:
         L.oracle_rhs.argtypes = [vp, vp, vp, vp, vp]
         L.oracle_time_step.argtypes = [vp, C.POINTER(dbl)]
         L.oracle_loc_time_steps.argtypes = [vp, vp]
+        L.oracle_error_norms.argtypes = [vp, C.POINTER(dbl), C.POINTER(dbl)]
         L.oracle_advance.argtypes = [vp, i64, dbl]
         L.oracle_first_bad_dof.argtypes = [vp]
         L.oracle_first_bad_dof.restype = i64
@@ -113,6 +114,12 @@ class Oracle:
         out = np.empty(self.n_cells)
         self._status(self.L.oracle_loc_time_steps(self.h, _p(out)), "loc_time_steps")
         return out
+
+    def error_norms(self):
+        """(steady-state error, convergence error) of the current state, as write() logs them."""
+        ss, cv = C.c_double(), C.c_double()
+        self._status(self.L.oracle_error_norms(self.h, C.byref(ss), C.byref(cv)), "error_norms")
+        return ss.value, cv.value
 
     def advance(self, n_steps, end_time=1e300):
         self._status(self.L.oracle_advance(self.h, n_steps, end_time), "advance")

@@ -61,6 +61,7 @@ class Params(C.Structure):
         ("expr_courant", C.c_int32), ("do_filtering", C.c_int32), ("rk_order", C.c_int32),
         ("local_stepping", C.c_int32), ("limit_local_step", C.c_int32), ("local_start_time", C.c_double),
         ("local_nbr_factor", C.c_double), ("local_global_factor", C.c_double),
+        ("calc_ss_error", C.c_int32), ("calc_conv_error", C.c_int32), ("expr_conv_exact", C.c_int32),
         ("precision", C.c_int32), ("sensor", C.c_int32), ("judge_every", C.c_int32),
         ("judge_alpha_tol", C.c_double),
         ("n_bc", C.c_int32), ("bcs", C.POINTER(BCDesc)),
@@ -81,6 +82,8 @@ class MeshDesc(C.Structure):
         ("ft_nbr_cell", C.POINTER(C.c_int32)), ("ft_nbr_face", C.POINTER(C.c_int32)),
         ("ft_bc", C.POINTER(C.c_int32)), ("ft_nbr_fdof", C.POINTER(C.c_int32)),
         ("ft_normal", C.POINTER(C.c_double)), ("ft_xyz", C.POINTER(C.c_double)),
+        ("gauss_interp", C.POINTER(C.c_double)), ("q_wJ", C.POINTER(C.c_double)),
+        ("q_xyz", C.POINTER(C.c_double)),
     ]
 
 
@@ -158,6 +161,7 @@ def gpu_lib() -> C.CDLL:
         L.plens_gpu_advance_async.argtypes = [vp, i64, dbl]
         L.plens_gpu_synchronize.argtypes = [vp]
         L.plens_gpu_get_cell_scalars.argtypes = [vp, vp, vp, vp]
+        L.plens_gpu_error_norms.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.plens_gpu_get_avars.argtypes = [vp, vp]
         L.plens_gpu_first_bad_dof.argtypes = [vp, C.POINTER(i64)]
         L.plens_gpu_set_sensor_weights.argtypes = [vp, vp]
@@ -232,6 +236,9 @@ class Case:
             "ft_bc": arr(m.ft_bc, nt), "ft_nbr_fdof": arr(m.ft_nbr_fdof, nt * P * P).reshape(nt, P * P),
             "ft_normal": arr(m.ft_normal, nt * P * P * 3).reshape(nt, P * P, 3),
             "ft_xyz": arr(m.ft_xyz, nt * P * P * 3).reshape(nt, P * P, 3),
+            "gauss_interp": arr(m.gauss_interp, P * P).reshape(P, P) if m.gauss_interp else None,
+            "q_wJ": arr(m.q_wJ, nd) if m.q_wJ else None,
+            "q_xyz": arr(m.q_xyz, 3 * nd).reshape(3, nd) if m.q_xyz else None,
         }
 
     def initial_state(self) -> np.ndarray:
@@ -381,6 +388,15 @@ class GpuSolver:
 
     def synchronize(self):
         self._check(self.L.plens_gpu_synchronize(self.h), "synchronize")
+
+    def error_norms(self):
+        """(steady-state error, convergence error) of the current state, as PLENS::write logs
+        them; a norm not requested at setup is returned as None."""
+        ss, cv = C.c_double(), C.c_double()
+        p = self.case.params
+        self._check(self.L.plens_gpu_error_norms(self.h, C.byref(ss) if p.calc_ss_error else None,
+                                                  C.byref(cv) if p.calc_conv_error else None), "error_norms")
+        return (ss.value if p.calc_ss_error else None), (cv.value if p.calc_conv_error else None)
 
     def cell_scalars(self):
         a = np.empty(self.n_cells)

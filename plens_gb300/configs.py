@@ -400,6 +400,20 @@ end
     return prm, {}, 3
 
 
+def with_error_norms(spec, ss_error: bool = True, conv_exact: str | None = None):
+    """``spec`` with the error norms of the output steps set: the steady-state error on or off,
+    and the density convergence error against ``conv_exact`` (an expression of x, y, z, t)."""
+    prm, files, degree = spec
+    lines = f"    set calculate steady state error = {'true' if ss_error else 'false'}\n"
+    if conv_exact is not None:
+        lines += ("    subsection convergence\n        set calculate error = true\n"
+                  "        set variable = density\n"
+                  f"        set exact solution = {conv_exact}\n    end\n")
+    key = "subsection data output\n"
+    assert prm.count(key) == 1
+    return prm.replace(key, key + lines), files, degree
+
+
 def make_case(spec, mapping_degree: int = 3):
     """Writes the auxiliary files of ``spec`` into a temporary directory and builds the Case."""
     from .api import Case

@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "diagnostics.cuh"
 #include "launch.cuh"
 #include "mlp.cuh"
 #include "plens_gpu.h"
@@ -178,6 +179,12 @@ struct plens_ctx {
     unsigned char* snap_host = nullptr;
     size_t snap_bytes = 0;
     bool snap_pending = false;
+    // error norms of the output steps: rho E of the previous step's start, the quadrature data,
+    // per-cell and total sums
+    double* rhoE_old = nullptr;
+    const double *q_wJ = nullptr, *q_xyz = nullptr;
+    double *err_cell = nullptr, *err_sum = nullptr;
+    GaussInterp gi{};
 };
 
 namespace {
@@ -306,6 +313,10 @@ int launch_step(plens_ctx* c, double end_time, bool judge = true)
     cudaStream_t st = c->stream;
     k_step_begin<<<1, 1, 0, st>>>(c->dv, end_time);
     c->launches += 1;
+    if (c->rhoE_old) {
+        k_save_rhoE<<<(unsigned)std::min<int64_t>((c->nd + 255) / 256, 152 * 8), 256, 0, st>>>(c->dv, c->rhoE_old);
+        c->launches += 1;
+    }
     if (c->learned) {
         k_snapshot<<<(unsigned)std::min<int64_t>((5 * c->nd / 2 + 255) / 256, 152 * 16), 256, 0, st>>>(c->dv);
         c->launches += 1;
@@ -563,6 +574,19 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         if ((r = dalloc(c, &d.sf3, 5 * c->nslot)) || (r = dalloc(c, &d.avars, 9 * nd))) return r;
         CK(cudaMemset(d.avars, 0, sizeof(double) * 9 * nd));
     }
+    if (prm->calc_ss_error || prm->calc_conv_error) {
+        if (!mesh->q_wJ || !mesh->gauss_interp || (prm->calc_conv_error && !mesh->q_xyz) ||
+            (prm->calc_conv_error && (prm->expr_conv_exact < 0 || prm->expr_conv_exact >= prm->n_expr)))
+            return fail(c, PLENS_GPU_E_INVALID, "error norms requested without their quadrature data or expression");
+        if ((r = dupload(c, &c->q_wJ, mesh->q_wJ, nd))) return r;
+        if (prm->calc_conv_error && (r = dupload(c, &c->q_xyz, mesh->q_xyz, 3 * nd))) return r;
+        if (prm->calc_ss_error) {
+            if ((r = dalloc(c, &c->rhoE_old, nd))) return r;
+            CK(cudaMemset(c->rhoE_old, 0, sizeof(double) * nd));  // rhoE_old before the first step
+        }
+        if ((r = dalloc(c, &c->err_cell, 3 * nc)) || (r = dalloc(c, &c->err_sum, 3))) return r;
+        for (int i = 0; i < c->P * c->P; ++i) c->gi.g[i] = mesh->gauss_interp[i];
+    }
     if (prm->local_stepping) {
         if ((r = dalloc(c, &d.dt_cell, nc)) || (r = dalloc(c, &d.dt_loc, nc))) return r;
         CK(cudaMemset(d.dt_loc, 0, sizeof(double) * nc));
@@ -818,6 +842,37 @@ int plens_gpu_advance(plens_ctx* c, int64_t n_steps, double end_time)
     }
     if (int r = plens_gpu_advance_async(c, n_steps, end_time)) return r;
     return sync_and_check(c);
+}
+
+int plens_gpu_error_norms(plens_ctx* c, double* ss_error, double* conv_error)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    if ((ss_error && !c->prm.calc_ss_error) || (conv_error && !c->prm.calc_conv_error))
+        return fail(c, PLENS_GPU_E_INVALID, "error norm not requested at setup");
+    if (!ss_error && !conv_error) return 0;
+    cudaStream_t st = c->stream;
+    // the time step of the current state: write() runs at stage 1 after calc_time_step
+    k_step_begin<<<1, 1, 0, st>>>(c->dv, 1e300);
+    c->launches += 1;
+    if (int r = launch_time_step(c)) return r;
+    const int expr = c->prm.calc_conv_error ? c->prm.expr_conv_exact : -1;
+    const unsigned threads = (unsigned)(((c->P * c->P * c->P) + 31) / 32 * 32);
+    switch (c->P) {
+    case 2: k_cell_errors<2><<<(unsigned)c->nc, threads, 0, st>>>(c->dv, c->gi, c->rhoE_old, c->q_wJ, c->q_xyz, expr, c->err_cell); break;
+    case 3: k_cell_errors<3><<<(unsigned)c->nc, threads, 0, st>>>(c->dv, c->gi, c->rhoE_old, c->q_wJ, c->q_xyz, expr, c->err_cell); break;
+    case 4: k_cell_errors<4><<<(unsigned)c->nc, threads, 0, st>>>(c->dv, c->gi, c->rhoE_old, c->q_wJ, c->q_xyz, expr, c->err_cell); break;
+    case 5: k_cell_errors<5><<<(unsigned)c->nc, threads, 0, st>>>(c->dv, c->gi, c->rhoE_old, c->q_wJ, c->q_xyz, expr, c->err_cell); break;
+    default: k_cell_errors<6><<<(unsigned)c->nc, threads, 0, st>>>(c->dv, c->gi, c->rhoE_old, c->q_wJ, c->q_xyz, expr, c->err_cell); break;
+    }
+    k_sum_errors<<<1, 1024, 0, st>>>(c->err_cell, c->nc, c->err_sum);
+    c->launches += 2;
+    if (int r = check_launch(c, "error norm kernels")) return r;
+    double h[3];
+    CK(cudaMemcpyAsync(h, c->err_sum, sizeof(h), cudaMemcpyDeviceToHost, st));
+    if (int r = sync_and_check(c)) return r;
+    if (ss_error) *ss_error = std::sqrt(h[1]) / std::sqrt(h[0]);
+    if (conv_error) *conv_error = std::sqrt(h[2]);
+    return 0;
 }
 
 int plens_gpu_get_cell_scalars(plens_ctx* c, double* alpha, double* alpha_d, double* dt_cell)

@@ -83,7 +83,8 @@ std::string counter_name(const std::string& base, int64_t counter)
 
 // PLENS::run + write (dgsem/plens.cc:1509-1550, 4170-4322): the state is written at every
 // `write frequency`-th step and at the end -- a .vtu file per output (one process: no .pvtu), the
-// .pvd collection, the .times log (counter, time, wall time) and a restart archive (.ar, read
+// .pvd collection, the .times log (counter, time, wall time), the .ss_error / .conv_error logs
+// when those norms are requested, and a restart archive (.ar, read
 // back by the "from archive restart" initial condition). Each output is an asynchronous device
 // snapshot: the next `write frequency` steps are already running on the GPU while the host
 // writes the files of the previous output.
@@ -100,6 +101,18 @@ void PLENS::run()
     }
     const std::string base = case_->base_file_name;
     std::ofstream times(dir + "/" + base + ".times", std::ios::app);
+    // the error logs of write() (dgsem/plens.cc:4291-4319): counter, time, error
+    const bool want_ss = case_->params.calc_ss_error != 0, want_conv = case_->params.calc_conv_error != 0;
+    std::ofstream ss_log, conv_log;
+    if (want_ss) ss_log.open(dir + "/" + base + ".ss_error", std::ios::app);
+    if (want_conv) conv_log.open(dir + "/" + base + ".conv_error", std::ios::app);
+    double ss_err = 0, conv_err = 0;
+    // the norms of the state about to be snapshot (write() computes them at stage 1 of the step)
+    auto error_norms = [&]() {
+        if (want_ss || want_conv)
+            check(plens_gpu_error_norms(ctx_, want_ss ? &ss_err : nullptr, want_conv ? &conv_err : nullptr), ctx_,
+                  "error_norms");
+    };
     const auto t0 = std::chrono::steady_clock::now();
     auto wall = [&] { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
     const bool viscous = !(case_->params.mu0 < 1e-16);
@@ -128,12 +141,15 @@ void PLENS::run()
         write_archive(dir + "/" + name + ".ar", *case_, U.data(), t, n, counter);
         times << counter << " " << t << " " << wall() << "\n";
         times.flush();
+        if (want_ss) ss_log << counter << " " << t << " " << ss_err << "\n" << std::flush;
+        if (want_conv) conv_log << counter << " " << t << " " << conv_err << "\n" << std::flush;
         ++counter;
     };
 
     double t = case_->start_time, dt = 0;
     int64_t n = 0;
     check(plens_gpu_get_time(ctx_, &t, &n, &dt), ctx_, "get_time");
+    error_norms();
     check(plens_gpu_snapshot_begin(ctx_), ctx_, "snapshot_begin");
     while (t < case_->end_time) {
         if (learned) {
@@ -148,6 +164,7 @@ void PLENS::run()
         check(plens_gpu_get_time(ctx_, &t, &n, &dt), ctx_, "get_time");
         std::printf("Current time: %.9g, dt: %.6g, time steps: %lld, elapsed wall time: %.3f\n", t, dt, (long long)n,
                     wall());
+        error_norms();
         check(plens_gpu_snapshot_begin(ctx_), ctx_, "snapshot_begin");
     }
     write_snapshot();

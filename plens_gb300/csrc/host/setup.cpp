@@ -495,6 +495,9 @@ void Case::finalize_pointers()
     mesh.ft_nbr_fdof = ft_nbr_fdof.data();
     mesh.ft_normal = ft_normal.data();
     mesh.ft_xyz = ft_xyz.data();
+    mesh.gauss_interp = gauss_interp.empty() ? nullptr : gauss_interp.data();
+    mesh.q_wJ = q_wJ.empty() ? nullptr : q_wJ.data();
+    mesh.q_xyz = q_xyz.empty() ? nullptr : q_xyz.data();
     params.n_bc = static_cast<int32_t>(bcs.size());
     params.bcs = bcs.data();
     params.n_expr = exprs.size();
@@ -698,6 +701,14 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
         pr.limit_local_step = prm.get_bool("time integration/limit local time step") ? 1 : 0;
         pr.local_nbr_factor = prm.get_double("time integration/local step neighbor factor");
         pr.local_global_factor = prm.get_double("time integration/local step global factor");
+        pr.calc_ss_error = prm.get_bool("data output/calculate steady state error") ? 1 : 0;
+        pr.calc_conv_error = prm.get_bool("data output/convergence/calculate error") ? 1 : 0;
+        pr.expr_conv_exact = -1;
+        if (pr.calc_conv_error) {
+            if (prm.get("data output/convergence/variable") != "density")
+                throw std::runtime_error("Currently, only density variable is supported for convergence error calculation.");
+            pr.expr_conv_exact = C.exprs.add(prm.get("data output/convergence/exact solution"));
+        }
         C.write_freq = prm.get_integer("data output/write frequency");
         C.output_dir = prm.get("data output/directory");
         C.base_file_name = prm.get("data output/base file name");
@@ -803,6 +814,62 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
             C.h_min[c] = std::sqrt(hmin2);
             for (int v = 0; v < 8; ++v)
                 for (int d = 0; d < 3; ++d) C.cell_center[3 * c + d] += 0.125 * mesh.vertices[mesh.cells[c][v]][d];
+        }
+    }
+
+    // ------------------------------------------------- quadrature of the error norms
+    // integrate_difference with QGauss(N+1) (dgsem/plens.cc:3985-4035, 4044-4098): per Gauss
+    // point the weight times det J of the same mapping, and its location for the exact solution.
+    if (C.params.calc_ss_error || C.params.calc_conv_error) {
+        std::vector<double> xg, wg;
+        gauss_1d(P, xg, wg);
+        C.gauss_interp.assign(static_cast<size_t>(P) * P, 0);
+        for (int q = 0; q < P; ++q)
+            for (int i = 0; i < P; ++i) C.gauss_interp[q * P + i] = lagrange(xi_n, i, xg[q]);
+        std::vector<double> Lg(static_cast<size_t>(P) * M1), dLg(static_cast<size_t>(P) * M1);
+        for (int q = 0; q < P; ++q)
+            for (int s = 0; s < M1; ++s) {
+                Lg[q * M1 + s] = lagrange(xi_s, s, xg[q]);
+                dLg[q * M1 + s] = lagrange_deriv(xi_s, s, xg[q]);
+            }
+        const bool want_xyz = C.params.calc_conv_error != 0;
+        C.q_wJ.assign(nd, 0);
+        if (want_xyz) C.q_xyz.assign(3 * nd, 0);
+#pragma omp parallel
+        {
+            std::vector<std::array<double, 3>> sup(static_cast<size_t>(M1) * M1 * M1);
+#pragma omp for
+            for (int64_t c = 0; c < nc; ++c) {
+                for (int k = 0; k < M1; ++k)
+                    for (int j = 0; j < M1; ++j)
+                        for (int i = 0; i < M1; ++i) {
+                            const double xi[3] = {xi_s[i], xi_s[j], xi_s[k]};
+                            sup[i + M1 * (j + M1 * k)] = manifold_point(mesh, c, xi);
+                        }
+                for (int l = 0; l < P3; ++l) {
+                    const int ti[3] = {l % P, (l / P) % P, l / P2};
+                    double x[3] = {0, 0, 0}, J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                    for (int k = 0; k < M1; ++k)
+                        for (int j = 0; j < M1; ++j)
+                            for (int i = 0; i < M1; ++i) {
+                                const auto& X = sup[i + M1 * (j + M1 * k)];
+                                const double li = Lg[ti[0] * M1 + i], lj = Lg[ti[1] * M1 + j], lk = Lg[ti[2] * M1 + k];
+                                const double g[3] = {dLg[ti[0] * M1 + i] * lj * lk, li * dLg[ti[1] * M1 + j] * lk,
+                                                     li * lj * dLg[ti[2] * M1 + k]};
+                                for (int d = 0; d < 3; ++d) {
+                                    x[d] += X[d] * li * lj * lk;
+                                    for (int e = 0; e < 3; ++e) J[d][e] += X[d] * g[e];
+                                }
+                            }
+                    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+                    const int64_t q = c * P3 + l;
+                    C.q_wJ[q] = wg[ti[0]] * wg[ti[1]] * wg[ti[2]] * std::fabs(det);
+                    if (want_xyz)
+                        for (int d = 0; d < 3; ++d) C.q_xyz[d * nd + q] = x[d];
+                }
+            }
         }
     }
 

@@ -71,6 +71,8 @@ struct Case {
     std::vector<int32_t> cell_nbr, cell_face_bc;
     std::vector<int32_t> ft_cell, ft_face, ft_nbr_cell, ft_nbr_face, ft_bc, ft_nbr_fdof;
     std::vector<double> ft_normal, ft_xyz;
+    // quadrature of the error norms (empty unless requested)
+    std::vector<double> gauss_interp, q_wJ, q_xyz;
     // parameters
     std::vector<plens_bc_desc> bcs;
     ExprTable exprs;
