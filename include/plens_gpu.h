@@ -318,6 +318,55 @@ int plens_gpu_mlp_loss_grad(const float* x, const float* y, int64_t n, const flo
 int plens_gpu_mlp_infer(const float* x, int64_t n, const float* params, float alpha_max,
                         float* alpha /* [n] */);
 
+/* ------------------------------------------------------- geometry setup on the GPU
+ * The two parts of the reference's setup chain whose cost grows with the mesh and the degree:
+ *  - calc_metric_terms (dgsem/plens.cc:1646-1682) with MetricTerms<3>::reinit
+ *    (dgsem/metric_terms.cc:67-142): location, J, det J, J^-1 and the contravariant vectors
+ *    Ja^i = a_j x a_k (cyclic) at every node of a tensor rule, from the degree-m Lagrange
+ *    interpolant of each cell's (m+1)^3 support points (MappingQGeneric(m));
+ *  - form_neighbor_face_matchings (dgsem/plens.cc:1574-1627): for every face task and face dof
+ *    the matching face dof of the other side, found by location (O(P^4) per face), with the
+ *    unit outward normal of FEFaceValues::normal_vector (dgsem/plens.cc:1751-1756, 1797).
+ * The support points (the manifold description), the neighbour/periodic topology and the face
+ * task list stay on the host (plens_host.h). The arithmetic is the host setup's, operation for
+ * operation and without multiply-add contraction, so both produce the same bits. */
+typedef struct plens_geometry_job {
+    /* mapping at the nodes of a tensor rule (the GLL nodes, or the Gauss points of the error
+     * norms); node l of cell c is c*n_points^3 + l, l = i + n_points (j + n_points k) */
+    int32_t n_points;         /* rule points per direction */
+    int32_t n_support;        /* support points per direction, mapping degree + 1 */
+    int64_t n_cells;
+    const double* support;    /* [n_cells][n_support^3][3], point s = i + n_support (j + n_support k) */
+    const double* basis;      /* [n_points][n_support]: 1D Lagrange basis of the support points */
+    const double* dbasis;     /* [n_points][n_support]: its derivative */
+    double* xyz;              /* out [3][n_nodes], or NULL */
+    double* detJ;             /* out [n_nodes], or NULL */
+    double* Ja;               /* out [9][n_nodes] as in plens_mesh_desc, or NULL */
+    double* Jinv;             /* out [9][n_nodes] as in plens_mesh_desc, or NULL */
+    int64_t first_bad_cell;   /* out: first cell with det J <= 0 at a node, or -1 */
+    /* face dofs of the face tasks (n_face_tasks = 0: none). Needs the GLL rule of the degree
+     * (n_points = degree + 1) with xyz and Ja requested. */
+    int64_t n_face_tasks;
+    const int32_t* ft_cell;      /* as in plens_mesh_desc */
+    const int32_t* ft_face;
+    const int32_t* ft_nbr_cell;  /* -1: no other side, the face dof matches itself */
+    const int32_t* ft_nbr_face;
+    const int32_t* ft_skip_dir;  /* periodic direction, left out of the match distance (the match
+                                    must then keep the face-dof order), or -1 */
+    const double* ft_tol;        /* match tolerance of the task (distance < tol) */
+    int32_t* ft_nbr_fdof;        /* out [n_face_tasks][P^2] */
+    double* ft_normal;           /* out [n_face_tasks][P^2][3] */
+    double* ft_xyz;              /* out [n_face_tasks][P^2][3] */
+    int64_t first_unmatched;     /* out: first task*P^2 + q without a matching face dof, or -1 */
+    int64_t first_misoriented;   /* out: first periodic task*P^2 + q matched to another q, or -1 */
+} plens_geometry_job;
+
+/* Runs a geometry job on the current device: allocates its device buffers, computes, copies the
+ * outputs to the job's host arrays and frees the buffers before returning. Returns
+ * PLENS_GPU_E_INVALID for bad sizes or pointers (the first_* outputs are results, not errors). */
+int plens_gpu_setup_geometry(plens_geometry_job* job);
+typedef int (*plens_geometry_fn)(plens_geometry_job* job);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,6 +24,12 @@ typedef struct plens_case plens_case;
  * failure *out is NULL and plens_case_last_error() holds the message. */
 int plens_case_create(const char* prm_text, const char* base_dir, int mapping_degree,
                       int fe_degree, plens_case** out);
+/* As plens_case_create, with the function that runs the geometry jobs (metric terms and face-dof
+ * matching) when the prm entry "GB300/geometry setup" is "gpu": normally plens_gpu_setup_geometry
+ * of the GPU library, passed in so that this library needs no GPU. With "host" (the default)
+ * or a NULL function the host computes them. */
+int plens_case_create_ex(const char* prm_text, const char* base_dir, int mapping_degree,
+                         int fe_degree, plens_geometry_fn geometry, plens_case** out);
 const char* plens_case_last_error(void);
 void plens_case_destroy(plens_case* c);
 
@@ -33,6 +39,10 @@ const plens_params* plens_case_params(const plens_case* c);
 plens_params* plens_case_params_mut(plens_case* c);
 int64_t plens_case_n_cells(const plens_case* c);
 int64_t plens_case_n_dofs(const plens_case* c);
+/* Wall seconds of the setup phases: [0] mesh and parameters, [1] geometry (support points,
+ * metric terms, face dofs, error-norm quadrature), [2] topology, BCs and face-task list,
+ * [3] initial condition. */
+int plens_case_setup_times(const plens_case* c, double* seconds /* [4] */);
 /* Initial state [5][ndof] (PLENS::set_IC) and dof locations [3][ndof]. */
 int plens_case_initial_state(const plens_case* c, double* U);
 int plens_case_dof_xyz(const plens_case* c, double* xyz);

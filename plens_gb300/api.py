@@ -105,6 +105,7 @@ def host_lib() -> C.CDLL:
         L = _load("libplens_host.so")
         vp, i64, dbl, i32 = C.c_void_p, C.c_int64, C.c_double, C.c_int32
         L.plens_case_create.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.POINTER(vp)]
+        L.plens_case_create_ex.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, vp, C.POINTER(vp)]
         L.plens_case_last_error.restype = C.c_char_p
         L.plens_case_destroy.argtypes = [vp]
         L.plens_case_mesh.argtypes = [vp]
@@ -118,6 +119,7 @@ def host_lib() -> C.CDLL:
         L.plens_case_n_dofs.argtypes = [vp]
         L.plens_case_n_dofs.restype = i64
         L.plens_case_initial_state.argtypes = [vp, vp]
+        L.plens_case_setup_times.argtypes = [vp, vp]
         L.plens_case_dof_xyz.argtypes = [vp, vp]
         L.plens_case_start_time.argtypes = [vp]
         L.plens_case_start_time.restype = dbl
@@ -175,6 +177,7 @@ def gpu_lib() -> C.CDLL:
         L.plens_gpu_set_sensor_tensor_cores.argtypes = [vp, C.c_int]
         L.plens_gpu_snapshot_end.argtypes = [vp, vp, vp, vp, vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(dbl)]
         L.plens_gpu_set_kernel_timing.argtypes = [vp, C.c_int]
+        L.plens_gpu_setup_geometry.argtypes = [vp]
         L.plens_gpu_kernel_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(i64)]
         _gpu = L
     return _gpu
@@ -185,13 +188,20 @@ def _ptr(a: np.ndarray) -> int:
 
 
 class Case:
-    """input.prm text -> mesh description, parameters and initial state (host only)."""
+    """input.prm text -> mesh description, parameters and initial state.
+
+    The setup runs on the host; with ``set geometry setup = gpu`` in the prm's ``GB300``
+    subsection the metric terms and face dofs are computed by the CUDA library's
+    ``plens_gpu_setup_geometry`` (same bits), which must then be built."""
 
     def __init__(self, prm_text: str, fe_degree: int, mapping_degree: int = 2, base_dir: str = "."):
         L = host_lib()
         h = C.c_void_p()
-        rc = L.plens_case_create(prm_text.encode(), str(base_dir).encode(), mapping_degree,
-                                 fe_degree, C.byref(h))
+        geometry = None
+        if (LIB_DIR / "libplens_gpu.so").exists():
+            geometry = C.cast(gpu_lib().plens_gpu_setup_geometry, C.c_void_p)
+        rc = L.plens_case_create_ex(prm_text.encode(), str(base_dir).encode(), mapping_degree,
+                                    fe_degree, geometry, C.byref(h))
         if rc != 0:
             raise PlensError(L.plens_case_last_error().decode())
         self._h = h
@@ -240,6 +250,12 @@ class Case:
             "q_wJ": arr(m.q_wJ, nd) if m.q_wJ else None,
             "q_xyz": arr(m.q_xyz, 3 * nd).reshape(3, nd) if m.q_xyz else None,
         }
+
+    def setup_times(self) -> dict:
+        """Wall seconds of the setup phases (mesh, geometry, topology, initial condition)."""
+        t = np.zeros(4)
+        self._L.plens_case_setup_times(self._h, _ptr(t))
+        return dict(zip(("mesh", "geometry", "topology", "initial_condition"), t.tolist()))
 
     def initial_state(self) -> np.ndarray:
         U = np.empty((5, self.n_dofs), dtype=np.float64)

@@ -29,7 +29,7 @@ GENCODE = "arch=compute_103a,code=sm_103a"
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall", "-Wno-unused-function"]
 
 HOST_SRCS = ["host/expr_compile.cpp", "host/prm.cpp", "host/setup.cpp", "host/output.cpp", "host/capi.cpp"]
-GPU_SRCS = ["gpu/plens_gpu.cu", "gpu/mlp.cu", "gpu/noalloc.cu"]
+GPU_SRCS = ["gpu/plens_gpu.cu", "gpu/mlp.cu", "gpu/noalloc.cu", "gpu/geometry.cu"]
 # kernels_inst.cu is compiled once per (P, precision)
 GPU_INST = [(P, prec) for P in (2, 3, 4, 5, 6) for prec in ("fp64", "mixed")]
 DRIVER_SRCS = ["host/plens_driver.cpp", "host/main.cpp"]

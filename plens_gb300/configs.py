@@ -414,6 +414,14 @@ def with_error_norms(spec, ss_error: bool = True, conv_exact: str | None = None)
     return prm.replace(key, key + lines), files, degree
 
 
+def with_gpu_geometry(spec):
+    """``spec`` with the metric terms and face dofs computed on the GPU (``GB300/geometry setup``)."""
+    prm, files, degree = spec
+    key = "subsection GB300\n"
+    assert prm.count(key) == 1
+    return prm.replace(key, key + "    set geometry setup = gpu\n"), files, degree
+
+
 def make_case(spec, mapping_degree: int = 3):
     """Writes the auxiliary files of ``spec`` into a temporary directory and builds the Case."""
     from .api import Case

@@ -21,6 +21,12 @@ extern "C" {
 int plens_case_create(const char* prm_text, const char* base_dir, int mapping_degree,
                       int fe_degree, plens_case** out)
 {
+    return plens_case_create_ex(prm_text, base_dir, mapping_degree, fe_degree, nullptr, out);
+}
+
+int plens_case_create_ex(const char* prm_text, const char* base_dir, int mapping_degree,
+                         int fe_degree, plens_geometry_fn geometry, plens_case** out)
+{
     if (out) *out = nullptr;
     if (!prm_text || !out) {
         g_last_error = "null argument";
@@ -31,7 +37,7 @@ int plens_case_create(const char* prm_text, const char* base_dir, int mapping_de
         plens::declare_parameters(prm);
         prm.parse_input_from_string(prm_text);
         auto* h = new plens_case();
-        h->c = plens::build_case(prm, mapping_degree, fe_degree, base_dir ? base_dir : "");
+        h->c = plens::build_case(prm, mapping_degree, fe_degree, base_dir ? base_dir : "", geometry);
         *out = h;
         return 0;
     } catch (const std::exception& e) {
@@ -47,6 +53,13 @@ const plens_params* plens_case_params(const plens_case* c) { return &c->c->param
 plens_params* plens_case_params_mut(plens_case* c) { return &c->c->params; }
 int64_t plens_case_n_cells(const plens_case* c) { return c->c->n_cells; }
 int64_t plens_case_n_dofs(const plens_case* c) { return c->c->n_dofs; }
+
+int plens_case_setup_times(const plens_case* c, double* seconds)
+{
+    if (!c || !seconds) return 1;
+    for (int i = 0; i < 4; ++i) seconds[i] = c->c->setup_seconds[i];
+    return 0;
+}
 
 int plens_case_initial_state(const plens_case* c, double* U)
 {

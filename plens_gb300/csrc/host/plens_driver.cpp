@@ -40,7 +40,7 @@ void PLENS::declare_parameters() { plens::declare_parameters(prm_); }
 // triggers it if it has not run yet.
 void PLENS::build_if_needed()
 {
-    if (!case_) case_ = build_case(prm_, mhod_, degree_, base_dir_);
+    if (!case_) case_ = build_case(prm_, mhod_, degree_, base_dir_, &plens_gpu_setup_geometry);
 }
 void PLENS::read_mesh() { build_if_needed(); }
 void PLENS::set_NS() { build_if_needed(); }

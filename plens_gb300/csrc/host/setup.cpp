@@ -3,6 +3,7 @@
 #include "output.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <fstream>
 #include <map>
@@ -463,6 +464,7 @@ void declare_parameters(ParameterHandler& prm)
     prm.declare_entry("GB300/judge alpha tolerance", "0.05");
     prm.declare_entry("GB300/constant viscosity", "false", "CONST_VISCOSITY build switch");
     prm.declare_entry("GB300/2d", "false", "PLENS_2D build switch");
+    prm.declare_entry("GB300/geometry setup", "host", "host|gpu: where the metric terms and face dofs are computed");
 }
 
 void prim_to_cons(double gamma, double rho, const double vel[3], double p, double cons[5])
@@ -545,13 +547,155 @@ int normal_node_of_face_dof(int P, int face, int q)
     return face_to_cell_dof(P, face, q);
 }
 
+// Support points of MappingQGeneric(m) for every cell: the manifold point at each tensor point of
+// the 1D support nodes xi_s, [n_cells][M1^3][3] with point i + M1 (j + M1 k).
+std::vector<double> support_points(const HexMesh& mesh, const std::vector<double>& xi_s)
+{
+    const int M1 = static_cast<int>(xi_s.size()), M3 = M1 * M1 * M1;
+    const int64_t nc = static_cast<int64_t>(mesh.cells.size());
+    std::vector<double> sup(static_cast<size_t>(nc) * M3 * 3);
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < nc; ++c)
+        for (int k = 0; k < M1; ++k)
+            for (int j = 0; j < M1; ++j)
+                for (int i = 0; i < M1; ++i) {
+                    const double xi[3] = {xi_s[i], xi_s[j], xi_s[k]};
+                    const auto p = manifold_point(mesh, c, xi);
+                    for (int d = 0; d < 3; ++d) sup[(static_cast<size_t>(c) * M3 + i + M1 * (j + M1 * k)) * 3 + d] = p[d];
+                }
+    return sup;
+}
+
+// Host form of plens_gpu_setup_geometry (include/plens_gpu.h), the same job in the same
+// arithmetic: MetricTerms<3>::reinit at the nodes of a tensor rule (dgsem/metric_terms.cc:67-142:
+// J from the mapping, det J, J^-1 by cofactors, Ja^d = a_{d+1} x a_{d+2}) and the face-dof
+// matching of form_neighbor_face_matchings (dgsem/plens.cc:1574-1627) with the unit normals of
+// FEFaceValues (dgsem/plens.cc:1751-1756, 1797).
+int host_setup_geometry(plens_geometry_job* jb)
+{
+    const int np = jb->n_points, ns = jb->n_support, np2 = np * np, np3 = np2 * np, ns3 = ns * ns * ns;
+    const int64_t nc = jb->n_cells, nn = nc * np3;
+    const double* Ls = jb->basis;
+    const double* dLs = jb->dbasis;
+    std::vector<double> xyz_tmp, ja_tmp;
+    double* xyz = jb->xyz;
+    double* Ja = jb->Ja;
+    if (jb->n_face_tasks > 0 && (!xyz || !Ja)) return PLENS_GPU_E_INVALID;
+    int64_t bad = INT64_MAX;
+#pragma omp parallel for schedule(static) reduction(min : bad)
+    for (int64_t c = 0; c < nc; ++c) {
+        const double* sup = jb->support + static_cast<size_t>(c) * ns3 * 3;
+        for (int l = 0; l < np3; ++l) {
+            const int ti[3] = {l % np, (l / np) % np, l / np2};
+            double x[3] = {0, 0, 0}, J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            for (int k = 0; k < ns; ++k)
+                for (int j = 0; j < ns; ++j)
+                    for (int i = 0; i < ns; ++i) {
+                        const double* X = sup + (i + ns * (j + ns * k)) * 3;
+                        const double li = Ls[ti[0] * ns + i], lj = Ls[ti[1] * ns + j], lk = Ls[ti[2] * ns + k];
+                        const double g[3] = {dLs[ti[0] * ns + i] * lj * lk, li * dLs[ti[1] * ns + j] * lk,
+                                             li * lj * dLs[ti[2] * ns + k]};
+                        for (int d = 0; d < 3; ++d) {
+                            x[d] += X[d] * li * lj * lk;
+                            for (int e = 0; e < 3; ++e) J[d][e] += X[d] * g[e];
+                        }
+                    }
+            const int64_t node = c * np3 + l;
+            if (xyz)
+                for (int d = 0; d < 3; ++d) xyz[d * nn + node] = x[d];
+            const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                               J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+            if (!(det > 0)) bad = std::min(bad, c);
+            if (jb->detJ) jb->detJ[node] = det;
+            if (jb->Jinv) {
+                double inv[3][3];
+                inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+                inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+                inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+                inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+                inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+                inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+                inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+                inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+                inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+                for (int r = 0; r < 3; ++r)
+                    for (int cc = 0; cc < 3; ++cc) jb->Jinv[(r * 3 + cc) * nn + node] = inv[r][cc];
+            }
+            // covariant vectors a_d = column d of J; Ja^d = a_{d+1} x a_{d+2}
+            if (Ja)
+                for (int d = 0; d < 3; ++d) {
+                    const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
+                    const double a1[3] = {J[0][d1], J[1][d1], J[2][d1]};
+                    const double a2[3] = {J[0][d2], J[1][d2], J[2][d2]};
+                    const double cr[3] = {a1[1] * a2[2] - a1[2] * a2[1], a1[2] * a2[0] - a1[0] * a2[2],
+                                          a1[0] * a2[1] - a1[1] * a2[0]};
+                    for (int e = 0; e < 3; ++e) Ja[(d * 3 + e) * nn + node] = cr[e];
+                }
+        }
+    }
+    jb->first_bad_cell = (bad == INT64_MAX) ? -1 : bad;
+
+    // face dofs: the first face dof of the other side within the tolerance (periodic direction
+    // left out of the distance), the unit outward normal at the node FEFaceValues uses, the location
+    const int64_t nt = jb->n_face_tasks;
+    int64_t unmatched = INT64_MAX, misoriented = INT64_MAX;
+#pragma omp parallel for schedule(static) reduction(min : unmatched, misoriented)
+    for (int64_t t = 0; t < nt; ++t) {
+        const int64_t c = jb->ft_cell[t], oc = jb->ft_nbr_cell[t];
+        const int f = jb->ft_face[t], of = jb->ft_nbr_face[t], pdir = jb->ft_skip_dir[t];
+        const double tol = jb->ft_tol[t];
+        for (int q = 0; q < np2; ++q) {
+            const int64_t idx = t * np2 + q;
+            const int64_t own = c * np3 + face_to_cell_dof(np, f, q);
+            int match = (oc < 0) ? q : -1;
+            if (oc >= 0) {
+                for (int q2 = 0; q2 < np2 && match < 0; ++q2) {
+                    const int64_t other = oc * np3 + face_to_cell_dof(np, of, q2);
+                    double s2 = 0;
+                    for (int d = 0; d < 3; ++d) {
+                        if (d == pdir) continue;
+                        const double df = xyz[d * nn + own] - xyz[d * nn + other];
+                        s2 += df * df;
+                    }
+                    if (std::sqrt(s2) < tol) match = q2;
+                }
+                if (match < 0) unmatched = std::min(unmatched, idx);
+                else if (pdir >= 0 && match != q) misoriented = std::min(misoriented, idx);
+            }
+            jb->ft_nbr_fdof[idx] = match;
+            const int64_t ln = c * np3 + normal_node_of_face_dof(np, f, q);
+            const int dir = f / 2;
+            const double sgn = (f % 2 == 0) ? -1.0 : 1.0;
+            double n[3], nrm = 0;
+            for (int e = 0; e < 3; ++e) {
+                n[e] = Ja[(dir * 3 + e) * nn + ln];
+                nrm += n[e] * n[e];
+            }
+            nrm = std::sqrt(nrm);
+            for (int e = 0; e < 3; ++e) jb->ft_normal[idx * 3 + e] = sgn * n[e] / nrm;
+            for (int e = 0; e < 3; ++e) jb->ft_xyz[idx * 3 + e] = xyz[e * nn + own];
+        }
+    }
+    jb->first_unmatched = (unmatched == INT64_MAX) ? -1 : unmatched;
+    jb->first_misoriented = (misoriented == INT64_MAX) ? -1 : misoriented;
+    return PLENS_GPU_OK;
+}
+
 }  // namespace
 
 std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree, int fe_degree,
-                                 const std::string& base_dir)
+                                 const std::string& base_dir, plens_geometry_fn geometry)
 {
     auto cs = std::make_unique<Case>();
     Case& C = *cs;
+    auto clock_now = [] { return std::chrono::steady_clock::now(); };
+    auto lap = clock_now();
+    auto charge = [&](int phase) {
+        const auto t = clock_now();
+        C.setup_seconds[phase] += std::chrono::duration<double>(t - lap).count();
+        lap = t;
+    };
     if (fe_degree < 1 || fe_degree > 5) throw std::runtime_error("fe degree must lie in [1,5]");
     if (mapping_degree < 1) throw std::runtime_error("High order mapping degree must be >= 1.");
     C.degree = fe_degree;
@@ -723,155 +867,47 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
         if (!C.sensor_weights_file.empty()) C.sensor_weights_file = path(C.sensor_weights_file);
     }
 
-    // --------------------------------------------------- mapping + metric terms per node
-    // calc_metric_terms (plens.cc:1646-1682) with MetricTerms<3>::reinit (metric_terms.cc:67-142):
-    // J at the GLL nodes from the mapping, detJ, Jinv, Ja^i = a_j x a_k (cyclic).
+    // ------------------------------------------------------- 1D rules, cell sizes, geometry
     std::vector<double> xi_n, w_n;
     gll_1d(P, xi_n, w_n);
     const int m_deg = C.mapping_degree, M1 = m_deg + 1;
     std::vector<double> xi_s, w_s;
     gll_1d(M1, xi_s, w_s);
-    // 1D support-basis values and derivatives at the DG nodes
-    std::vector<double> Ls(static_cast<size_t>(P) * M1), dLs(static_cast<size_t>(P) * M1);
-    for (int i = 0; i < P; ++i)
-        for (int s = 0; s < M1; ++s) {
-            Ls[i * M1 + s] = lagrange(xi_s, s, xi_n[i]);
-            dLs[i * M1 + s] = lagrange_deriv(xi_s, s, xi_n[i]);
-        }
-    C.detJ.assign(nd, 0);
-    C.Ja.assign(9 * nd, 0);
-    C.Jinv.assign(9 * nd, 0);
-    C.dof_xyz.assign(3 * nd, 0);
+    charge(0);
     C.h_min.assign(nc, 0);
     C.cell_center.assign(3 * nc, 0);
-    {
-        std::vector<std::array<double, 3>> sup(static_cast<size_t>(M1) * M1 * M1);
-        for (int64_t c = 0; c < nc; ++c) {
-            for (int k = 0; k < M1; ++k)
-                for (int j = 0; j < M1; ++j)
-                    for (int i = 0; i < M1; ++i) {
-                        const double xi[3] = {xi_s[i], xi_s[j], xi_s[k]};
-                        sup[i + M1 * (j + M1 * k)] = manifold_point(mesh, c, xi);
-                    }
-            for (int l = 0; l < P3; ++l) {
-                const int ti[3] = {l % P, (l / P) % P, l / P2};
-                double x[3] = {0, 0, 0}, J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-                for (int k = 0; k < M1; ++k)
-                    for (int j = 0; j < M1; ++j)
-                        for (int i = 0; i < M1; ++i) {
-                            const auto& X = sup[i + M1 * (j + M1 * k)];
-                            const double li = Ls[ti[0] * M1 + i], lj = Ls[ti[1] * M1 + j],
-                                         lk = Ls[ti[2] * M1 + k];
-                            const double g[3] = {dLs[ti[0] * M1 + i] * lj * lk,
-                                                 li * dLs[ti[1] * M1 + j] * lk,
-                                                 li * lj * dLs[ti[2] * M1 + k]};
-                            for (int d = 0; d < 3; ++d) {
-                                x[d] += X[d] * li * lj * lk;
-                                for (int e = 0; e < 3; ++e) J[d][e] += X[d] * g[e];
-                            }
-                        }
-                const int64_t dof = c * P3 + l;
-                for (int d = 0; d < 3; ++d) C.dof_xyz[d * nd + dof] = x[d];
-                const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
-                                   J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                                   J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-                if (!(det > 0)) throw std::runtime_error("cell " + std::to_string(c) + " has a non-positive Jacobian");
-                C.detJ[dof] = det;
-                // inverse by cofactors
-                double inv[3][3];
-                inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
-                inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
-                inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
-                inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
-                inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
-                inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
-                inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
-                inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
-                inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
-                for (int r = 0; r < 3; ++r)
-                    for (int cc = 0; cc < 3; ++cc) C.Jinv[(r * 3 + cc) * nd + dof] = inv[r][cc];
-                // covariant vectors a_d = column d of J; Ja^d = a_{d+1} x a_{d+2}
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < nc; ++c) {
+        // minimum_vertex_distance (all vertex pairs) and centre (vertex average)
+        double hmin2 = 1e300;
+        for (int a = 0; a < 8; ++a)
+            for (int b = a + 1; b < 8; ++b) {
+                double s2 = 0;
                 for (int d = 0; d < 3; ++d) {
-                    const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
-                    const double a1[3] = {J[0][d1], J[1][d1], J[2][d1]};
-                    const double a2[3] = {J[0][d2], J[1][d2], J[2][d2]};
-                    const double cr[3] = {a1[1] * a2[2] - a1[2] * a2[1], a1[2] * a2[0] - a1[0] * a2[2],
-                                          a1[0] * a2[1] - a1[1] * a2[0]};
-                    for (int e = 0; e < 3; ++e) C.Ja[(d * 3 + e) * nd + dof] = cr[e];
+                    const double df = mesh.vertices[mesh.cells[c][a]][d] - mesh.vertices[mesh.cells[c][b]][d];
+                    s2 += df * df;
                 }
+                hmin2 = std::min(hmin2, s2);
             }
-            // minimum_vertex_distance (all vertex pairs) and centre (vertex average)
-            double hmin2 = 1e300;
-            for (int a = 0; a < 8; ++a)
-                for (int b = a + 1; b < 8; ++b) {
-                    double s2 = 0;
-                    for (int d = 0; d < 3; ++d) {
-                        const double df = mesh.vertices[mesh.cells[c][a]][d] - mesh.vertices[mesh.cells[c][b]][d];
-                        s2 += df * df;
-                    }
-                    hmin2 = std::min(hmin2, s2);
-                }
-            C.h_min[c] = std::sqrt(hmin2);
-            for (int v = 0; v < 8; ++v)
-                for (int d = 0; d < 3; ++d) C.cell_center[3 * c + d] += 0.125 * mesh.vertices[mesh.cells[c][v]][d];
-        }
+        C.h_min[c] = std::sqrt(hmin2);
+        for (int v = 0; v < 8; ++v)
+            for (int d = 0; d < 3; ++d) C.cell_center[3 * c + d] += 0.125 * mesh.vertices[mesh.cells[c][v]][d];
     }
-
-    // ------------------------------------------------- quadrature of the error norms
-    // integrate_difference with QGauss(N+1) (dgsem/plens.cc:3985-4035, 4044-4098): per Gauss
-    // point the weight times det J of the same mapping, and its location for the exact solution.
-    if (C.params.calc_ss_error || C.params.calc_conv_error) {
-        std::vector<double> xg, wg;
-        gauss_1d(P, xg, wg);
-        C.gauss_interp.assign(static_cast<size_t>(P) * P, 0);
-        for (int q = 0; q < P; ++q)
-            for (int i = 0; i < P; ++i) C.gauss_interp[q * P + i] = lagrange(xi_n, i, xg[q]);
-        std::vector<double> Lg(static_cast<size_t>(P) * M1), dLg(static_cast<size_t>(P) * M1);
-        for (int q = 0; q < P; ++q)
-            for (int s = 0; s < M1; ++s) {
-                Lg[q * M1 + s] = lagrange(xi_s, s, xg[q]);
-                dLg[q * M1 + s] = lagrange_deriv(xi_s, s, xg[q]);
-            }
-        const bool want_xyz = C.params.calc_conv_error != 0;
-        C.q_wJ.assign(nd, 0);
-        if (want_xyz) C.q_xyz.assign(3 * nd, 0);
-#pragma omp parallel
-        {
-            std::vector<std::array<double, 3>> sup(static_cast<size_t>(M1) * M1 * M1);
-#pragma omp for
-            for (int64_t c = 0; c < nc; ++c) {
-                for (int k = 0; k < M1; ++k)
-                    for (int j = 0; j < M1; ++j)
-                        for (int i = 0; i < M1; ++i) {
-                            const double xi[3] = {xi_s[i], xi_s[j], xi_s[k]};
-                            sup[i + M1 * (j + M1 * k)] = manifold_point(mesh, c, xi);
-                        }
-                for (int l = 0; l < P3; ++l) {
-                    const int ti[3] = {l % P, (l / P) % P, l / P2};
-                    double x[3] = {0, 0, 0}, J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-                    for (int k = 0; k < M1; ++k)
-                        for (int j = 0; j < M1; ++j)
-                            for (int i = 0; i < M1; ++i) {
-                                const auto& X = sup[i + M1 * (j + M1 * k)];
-                                const double li = Lg[ti[0] * M1 + i], lj = Lg[ti[1] * M1 + j], lk = Lg[ti[2] * M1 + k];
-                                const double g[3] = {dLg[ti[0] * M1 + i] * lj * lk, li * dLg[ti[1] * M1 + j] * lk,
-                                                     li * lj * dLg[ti[2] * M1 + k]};
-                                for (int d = 0; d < 3; ++d) {
-                                    x[d] += X[d] * li * lj * lk;
-                                    for (int e = 0; e < 3; ++e) J[d][e] += X[d] * g[e];
-                                }
-                            }
-                    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
-                                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-                    const int64_t q = c * P3 + l;
-                    C.q_wJ[q] = wg[ti[0]] * wg[ti[1]] * wg[ti[2]] * std::fabs(det);
-                    if (want_xyz)
-                        for (int d = 0; d < 3; ++d) C.q_xyz[d * nd + q] = x[d];
-                }
-            }
-        }
-    }
+    // The geometry jobs (metric terms, face dofs) run on the host, or with "GB300/geometry setup =
+    // gpu" through `geometry` (plens_gpu_setup_geometry); both give the same bits.
+    const std::string geo_mode = prm.get("GB300/geometry setup");
+    if (geo_mode != "host" && geo_mode != "gpu") throw std::runtime_error("GB300/geometry setup must be host|gpu");
+    const bool geo_gpu = geo_mode == "gpu";
+    if (geo_gpu && !geometry)
+        throw std::runtime_error("GB300/geometry setup = gpu needs the GPU library's geometry function");
+    auto run_job = [&](plens_geometry_job& jb) {
+        const int rc = geo_gpu ? geometry(&jb) : host_setup_geometry(&jb);
+        if (rc != PLENS_GPU_OK)
+            throw std::runtime_error(std::string("geometry setup failed on the ") + (geo_gpu ? "GPU" : "host") +
+                                     " with status " + std::to_string(rc));
+    };
+    const std::vector<double> sup = support_points(mesh, xi_s);
+    charge(1);
 
     // ------------------------------------------------------------------- topology
     C.cell_nbr.assign(6 * nc, -1);
@@ -1012,9 +1048,11 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
 
     // ------------------------------------------------------------------- face tasks
     // interior faces once from the owner (lower cell index, plens.cc:1857), boundary faces once
-    // per side; neighbour face-dof matching by node location within 1e-8 h_min
+    // per side. The neighbour face-dof matching by node location within 1e-8 h_min (1e-6 h_min
+    // across a periodic pair, the periodic direction left out) runs in the geometry job below
     // (form_neighbor_face_matchings, plens.cc:1574-1627).
-    auto node_xyz = [&](int64_t c, int l, int d) { return C.dof_xyz[d * nd + c * P3 + l]; };
+    std::vector<int32_t> ft_skip_dir;
+    std::vector<double> ft_tol;
     for (int64_t c = 0; c < nc; ++c)
         for (int f = 0; f < 6; ++f) {
             const int32_t nbr = C.cell_nbr[6 * c + f];
@@ -1029,42 +1067,99 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
             C.ft_nbr_cell.push_back(static_cast<int32_t>(oc));
             C.ft_nbr_face.push_back(of);
             C.ft_bc.push_back(bc);
-            const double tol = (bc < 0 ? 1e-8 : 1e-6) * C.h_min[c];
-            const int pdir = (bc >= 0 && C.bcs[bc].type == PLENS_BC_PERIODIC) ? periodic.at(bc).dir : -1;
-            for (int q = 0; q < P2; ++q) {
-                const int l = face_to_cell_dof(P, f, q);
-                int match = (oc < 0) ? q : -1;
-                if (oc >= 0) {
-                    for (int q2 = 0; q2 < P2 && match < 0; ++q2) {
-                        const int l2 = face_to_cell_dof(P, of, q2);
-                        double s2 = 0;
-                        for (int d = 0; d < 3; ++d) {
-                            if (d == pdir) continue;
-                            const double df = node_xyz(c, l, d) - node_xyz(oc, l2, d);
-                            s2 += df * df;
-                        }
-                        if (std::sqrt(s2) < tol) match = q2;
-                    }
-                    if (match < 0) throw std::runtime_error("no matching face dof across face " + std::to_string(f) + " of cell " + std::to_string(c));
-                    if (pdir >= 0 && match != q)
-                        throw std::runtime_error("At least one periodic face pair doesn't have expected orientation");
-                }
-                C.ft_nbr_fdof.push_back(match);
-                // unit outward normal at the node FEFaceValues uses for index q
-                const int ln = normal_node_of_face_dof(P, f, q);
-                const int dir = f / 2;
-                const double sgn = (f % 2 == 0) ? -1.0 : 1.0;
-                double n[3], nn = 0;
-                for (int e = 0; e < 3; ++e) {
-                    n[e] = C.Ja[(dir * 3 + e) * nd + c * P3 + ln];
-                    nn += n[e] * n[e];
-                }
-                nn = std::sqrt(nn);
-                for (int e = 0; e < 3; ++e) C.ft_normal.push_back(sgn * n[e] / nn);
-                for (int e = 0; e < 3; ++e) C.ft_xyz.push_back(node_xyz(c, l, e));
-            }
+            ft_tol.push_back((bc < 0 ? 1e-8 : 1e-6) * C.h_min[c]);
+            ft_skip_dir.push_back((bc >= 0 && C.bcs[bc].type == PLENS_BC_PERIODIC) ? periodic.at(bc).dir : -1);
         }
 
+    charge(2);
+    // ------------------------------------------------------ metric terms and face dofs
+    // calc_metric_terms (plens.cc:1646-1682) with MetricTerms<3>::reinit (metric_terms.cc:67-142):
+    // J at the GLL nodes from the mapping, detJ, Jinv, Ja^i = a_j x a_k (cyclic); then the face
+    // dofs of every face task with the unit outward normal at the node FEFaceValues uses.
+    {
+        std::vector<double> Ls(static_cast<size_t>(P) * M1), dLs(static_cast<size_t>(P) * M1);
+        for (int i = 0; i < P; ++i)
+            for (int s = 0; s < M1; ++s) {
+                Ls[i * M1 + s] = lagrange(xi_s, s, xi_n[i]);
+                dLs[i * M1 + s] = lagrange_deriv(xi_s, s, xi_n[i]);
+            }
+        C.detJ.assign(nd, 0);
+        C.Ja.assign(9 * nd, 0);
+        C.Jinv.assign(9 * nd, 0);
+        C.dof_xyz.assign(3 * nd, 0);
+        const int64_t nt = static_cast<int64_t>(C.ft_cell.size());
+        C.ft_nbr_fdof.assign(static_cast<size_t>(nt) * P2, -1);
+        C.ft_normal.assign(static_cast<size_t>(nt) * P2 * 3, 0);
+        C.ft_xyz.assign(static_cast<size_t>(nt) * P2 * 3, 0);
+        plens_geometry_job jb{};
+        jb.n_points = P;
+        jb.n_support = M1;
+        jb.n_cells = nc;
+        jb.support = sup.data();
+        jb.basis = Ls.data();
+        jb.dbasis = dLs.data();
+        jb.xyz = C.dof_xyz.data();
+        jb.detJ = C.detJ.data();
+        jb.Ja = C.Ja.data();
+        jb.Jinv = C.Jinv.data();
+        jb.n_face_tasks = nt;
+        jb.ft_cell = C.ft_cell.data();
+        jb.ft_face = C.ft_face.data();
+        jb.ft_nbr_cell = C.ft_nbr_cell.data();
+        jb.ft_nbr_face = C.ft_nbr_face.data();
+        jb.ft_skip_dir = ft_skip_dir.data();
+        jb.ft_tol = ft_tol.data();
+        jb.ft_nbr_fdof = C.ft_nbr_fdof.data();
+        jb.ft_normal = C.ft_normal.data();
+        jb.ft_xyz = C.ft_xyz.data();
+        run_job(jb);
+        if (jb.first_bad_cell >= 0)
+            throw std::runtime_error("cell " + std::to_string(jb.first_bad_cell) + " has a non-positive Jacobian");
+        const int64_t um = jb.first_unmatched, mo = jb.first_misoriented;
+        if (um >= 0 && (mo < 0 || um < mo)) {
+            const int64_t t = um / P2;
+            throw std::runtime_error("no matching face dof across face " + std::to_string(C.ft_face[t]) + " of cell " +
+                                     std::to_string(C.ft_cell[t]));
+        }
+        if (mo >= 0) throw std::runtime_error("At least one periodic face pair doesn't have expected orientation");
+    }
+
+    // ------------------------------------------------- quadrature of the error norms
+    // integrate_difference with QGauss(N+1) (dgsem/plens.cc:3985-4035, 4044-4098): per Gauss
+    // point the weight times det J of the same mapping, and its location for the exact solution.
+    if (C.params.calc_ss_error || C.params.calc_conv_error) {
+        std::vector<double> xg, wg;
+        gauss_1d(P, xg, wg);
+        C.gauss_interp.assign(static_cast<size_t>(P) * P, 0);
+        for (int q = 0; q < P; ++q)
+            for (int i = 0; i < P; ++i) C.gauss_interp[q * P + i] = lagrange(xi_n, i, xg[q]);
+        std::vector<double> Lg(static_cast<size_t>(P) * M1), dLg(static_cast<size_t>(P) * M1);
+        for (int q = 0; q < P; ++q)
+            for (int s = 0; s < M1; ++s) {
+                Lg[q * M1 + s] = lagrange(xi_s, s, xg[q]);
+                dLg[q * M1 + s] = lagrange_deriv(xi_s, s, xg[q]);
+            }
+        const bool want_xyz = C.params.calc_conv_error != 0;
+        std::vector<double> qdet(nd);
+        if (want_xyz) C.q_xyz.assign(3 * nd, 0);
+        plens_geometry_job jq{};
+        jq.n_points = P;
+        jq.n_support = M1;
+        jq.n_cells = nc;
+        jq.support = sup.data();
+        jq.basis = Lg.data();
+        jq.dbasis = dLg.data();
+        jq.xyz = want_xyz ? C.q_xyz.data() : nullptr;
+        jq.detJ = qdet.data();
+        run_job(jq);
+        C.q_wJ.assign(nd, 0);
+        for (int64_t q = 0; q < nd; ++q) {
+            const int l = static_cast<int>(q % P3);
+            C.q_wJ[q] = wg[l % P] * wg[(l / P) % P] * wg[l / P2] * std::fabs(qdet[q]);
+        }
+    }
+
+    charge(1);
     // ------------------------------------------------------------------- set_IC
     C.U0.assign(5 * nd, 0.0);
     {
@@ -1203,14 +1298,59 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
                         modes.push_back(md);
                     }
             std::vector<double> u(3 * nd, 0.0);
-            // the dofs are independent (threads over dofs; each dof sums its modes in order), the
-            // rms is summed serially so the field does not depend on the thread count
-#pragma omp parallel for schedule(static)
-            for (int64_t dof = 0; dof < nd; ++dof) {
-                const double x[3] = {C.dof_xyz[dof], C.dof_xyz[nd + dof], C.dof_xyz[2 * nd + dof]};
-                for (const auto& md : modes) {
-                    const double s = std::cos(md.k[0] * x[0] + md.k[1] * x[1] + md.k[2] * x[2] + md.ph);
-                    for (int d = 0; d < 3; ++d) u[d * nd + dof] += md.a[d] * s;
+            // cos(k.x + ph) = Re(e^{i k0 x} e^{i k1 y} e^{i k2 z} e^{i ph}) with the integer
+            // wavenumbers' exponentials tabulated per dof: three complex products per mode instead
+            // of a cosine. The dofs are independent (threads over dofs; each dof sums its modes in
+            // order), the rms is summed serially so the field does not depend on the thread count.
+            std::vector<double> ph_c(modes.size()), ph_s(modes.size());
+            for (size_t m = 0; m < modes.size(); ++m) {
+                ph_c[m] = std::cos(modes[m].ph);
+                ph_s[m] = std::sin(modes[m].ph);
+            }
+            // blocks of B dofs, tables [d][k][dof of block]: the innermost loop runs over the
+            // block's dofs with unit stride and vectorises
+            constexpr int B = 64;
+            const int NK = 2 * K + 1;
+            const int64_t nblk = (nd + B - 1) / B;
+#pragma omp parallel
+            {
+                std::vector<double> ec(3 * NK * B), es(3 * NK * B), acc(3 * B);
+#pragma omp for schedule(static)
+                for (int64_t blk = 0; blk < nblk; ++blk) {
+                    const int64_t d0 = blk * B;
+                    const int nb = static_cast<int>(std::min<int64_t>(B, nd - d0));
+                    for (int d = 0; d < 3; ++d)
+                        for (int k = -K; k <= K; ++k)
+                            for (int b = 0; b < nb; ++b) {
+                                const double x = C.dof_xyz[d * nd + d0 + b];
+                                ec[(d * NK + k + K) * B + b] = std::cos(k * x);
+                                es[(d * NK + k + K) * B + b] = std::sin(k * x);
+                            }
+                    std::fill(acc.begin(), acc.end(), 0.0);
+                    for (size_t m = 0; m < modes.size(); ++m) {
+                        const auto& md = modes[m];
+                        const double* c0 = &ec[(0 * NK + static_cast<int>(md.k[0]) + K) * B];
+                        const double* s0 = &es[(0 * NK + static_cast<int>(md.k[0]) + K) * B];
+                        const double* c1 = &ec[(1 * NK + static_cast<int>(md.k[1]) + K) * B];
+                        const double* s1 = &es[(1 * NK + static_cast<int>(md.k[1]) + K) * B];
+                        const double* c2 = &ec[(2 * NK + static_cast<int>(md.k[2]) + K) * B];
+                        const double* s2 = &es[(2 * NK + static_cast<int>(md.k[2]) + K) * B];
+                        const double pc = ph_c[m], ps = ph_s[m], a0 = md.a[0], a1 = md.a[1], a2 = md.a[2];
+                        double* u0 = &acc[0];
+                        double* u1 = &acc[B];
+                        double* u2 = &acc[2 * B];
+#pragma omp simd
+                        for (int b = 0; b < B; ++b) {
+                            const double ar = c0[b] * c1[b] - s0[b] * s1[b], ai = c0[b] * s1[b] + s0[b] * c1[b];
+                            const double br = ar * c2[b] - ai * s2[b], bi = ar * s2[b] + ai * c2[b];
+                            const double sv = br * pc - bi * ps;
+                            u0[b] += a0 * sv;
+                            u1[b] += a1 * sv;
+                            u2[b] += a2 * sv;
+                        }
+                    }
+                    for (int d = 0; d < 3; ++d)
+                        for (int b = 0; b < nb; ++b) u[d * nd + d0 + b] = acc[d * B + b];
                 }
             }
             double usq = 0;
@@ -1277,6 +1417,7 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
             if (!(rho > 0) || !(e > 0)) throw std::runtime_error("initial condition is not positive at dof " + std::to_string(dof));
         }
     }
+    charge(3);
     C.prm_echo = prm.print_parameters();
     C.finalize_pointers();
     return cs;

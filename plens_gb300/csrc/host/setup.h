@@ -86,6 +86,9 @@ struct Case {
     // initial state [5][ndof]
     std::vector<double> U0;
     std::string prm_echo;
+    // wall seconds of the setup phases: mesh and parameters, geometry (support points, metric
+    // terms, face dofs, error-norm quadrature), topology/BCs/face-task list, initial condition
+    double setup_seconds[4] = {0, 0, 0, 0};
 
     void finalize_pointers();  // points params/mesh at the owned vectors
 };
@@ -95,8 +98,10 @@ struct Case {
 void declare_parameters(ParameterHandler& prm);
 
 // Builds a Case from parsed parameters. `base_dir` resolves relative file names (mesh, IC).
+// `geometry` runs the metric-term and face-dof jobs when "GB300/geometry setup" is "gpu"
+// (plens_gpu_setup_geometry of the GPU library); with "host" they run here.
 std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree, int fe_degree,
-                                 const std::string& base_dir);
+                                 const std::string& base_dir, plens_geometry_fn geometry = nullptr);
 
 // Conservative state from primitives (NavierStokes::prim_to_cons, navier_stokes.h:366-379).
 void prim_to_cons(double gamma, double rho, const double vel[3], double p, double cons[5]);

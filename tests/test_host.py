@@ -6,7 +6,7 @@ import math
 import numpy as np
 import pytest
 
-from helpers import make
+from helpers import make, mirrored_box_prm
 from plens_gb300 import configs
 from plens_gb300.api import Case, PlensError, eval_expression, gll_1d
 
@@ -185,3 +185,23 @@ subsection BCs
         np.testing.assert_allclose(Ja[d].T, np.tile(expect[d], (27, 1)), atol=1e-13)
     np.testing.assert_allclose(m["detJ"], 8.0, rtol=1e-14)
     assert m["h_min"][0] == pytest.approx(1.0)
+
+
+# ------------------------------------------------------------------- geometry setup switch
+
+def test_geometry_setup_switch(tmp_path):
+    """"GB300/geometry setup" takes host|gpu; gpu needs the GPU library's geometry function, which
+    plens_case_create (without _ex) does not pass; the host computes a non-positive Jacobian
+    error as the reference's setup would stop on it."""
+    from plens_gb300.api import host_lib
+    prm, files, deg = configs.sod(n=4)
+    with pytest.raises(PlensError, match="must be host[|]gpu"):
+        make((prm.replace("subsection GB300\n", "subsection GB300\n    set geometry setup = cpu\n"), files, deg))
+    L = host_lib()
+    import ctypes
+    h = ctypes.c_void_p()
+    gprm = configs.with_gpu_geometry((prm, files, deg))[0]
+    assert L.plens_case_create(gprm.encode(), b".", 3, deg, ctypes.byref(h)) != 0
+    assert b"needs the GPU library's geometry function" in L.plens_case_last_error()
+    with pytest.raises(PlensError, match="cell 0 has a non-positive Jacobian"):
+        Case(mirrored_box_prm(tmp_path, "host"), 2, base_dir=str(tmp_path))
