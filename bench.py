@@ -34,7 +34,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "DOF-stage updates/s: FP32+learned sensor vs FP64 plain, GB300, rho L1 err<=1e-4"
 UNIT = "DOF-stage/s"
-BYTES_PER_DOF_STAGE = 280  # U r/w 80 + two registers read 80 + one written 40 + Ja,detJ 80
+# Algorithmic bytes of one DOF-stage through the volume kernel. FP64 form: U r/w 80 + two RK
+# registers read 80 + one written 40 + Ja, detJ 80 = 280. Mixed form: the registers hold dt*R, an
+# FP32 result, in FP32 (2x20 read + 20 written) and the kernel reads the FP32 rounding of Ja and
+# detJ (40): U r/w 80 + 40 + 20 + 40 = 180.
+BYTES_PER_DOF_STAGE = {"plain": 280, "modal": 180, "learned": 180}
 WORKLOAD = "double Mach reflection 240x60x1 cells, N=3, 921600 DoFs, RK4(3)5[3R+]N, HLLC + Chandrashekhar"
 
 
@@ -527,7 +531,8 @@ def main():
         job[k] = {"value": nd * 5 * args.steps * ws / t, "ms_per_step": 1e3 * t / args.steps,
                   "e2e": nd * 5 * r["e2e_steps"] * ws / te,
                   "volume_kernel_ms": r["vol_ms"] / max(r["vol_n"], 1),
-                  "achieved_gbs": BYTES_PER_DOF_STAGE * nd / (r["vol_ms"] / max(r["vol_n"], 1) / 1e3) / 1e9}
+                  "bytes_per_dof_stage": BYTES_PER_DOF_STAGE[k],
+                  "achieved_gbs": BYTES_PER_DOF_STAGE[k] * nd / (r["vol_ms"] / max(r["vol_n"], 1) / 1e3) / 1e9}
     # accuracy of the FP32 forms against the plain FP64 form after the same steps
     job["modal"]["rel_l1_vs_fp64_plain"] = dict(zip(("rho", "momentum", "rhoE"), _rel_l1(modal["U"], plain["U"])))
     if learned is not None:
@@ -566,7 +571,8 @@ def main():
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_kind": peak_kind, "kernel": f"k_volume_mx (mixed form, {fast_sensor} sensor)",
             "traffic": _traffic_from_profile("k_volume_mx_dmr.md"),
-            "note": "achieved: algorithmic 280 B per DOF-stage x 921600 DoFs per launch / mean CUDA-event "
+            "note": "achieved: algorithmic 180 B per DOF-stage (FP64 state r/w, FP32 registers and metric "
+                    "images) x 921600 DoFs per launch / mean CUDA-event "
                     "launch time of the kernel-timing pass; traffic: ncu DRAM bytes of a stage-1 launch "
                     "(no RK register read yet), profiles/k_volume_mx_dmr.md",
         },

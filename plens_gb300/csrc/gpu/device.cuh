@@ -90,6 +90,10 @@ struct Dev {
     int64_t nc, nd, ntask, nslot;
     // mesh
     const double *detJ, *Ja, *Jinv, *h_min, *center;
+    // mixed form: the FP32 rounding (f64_to_f32) of detJ, Ja and Jinv, made once on the device at
+    // context creation -- the value every FP32 consumer of the FP64 metric terms would compute
+    // (null in the FP64 form)
+    const float *detJf, *Jaf, *Jinvf;
     const int32_t *cell_nbr;
     const uint8_t *cell_wall;
     const int32_t *ft_cell, *ft_face, *ft_nbr_cell, *ft_nbr_face, *ft_bc, *ft_nbr_fdof;
@@ -100,10 +104,13 @@ struct Dev {
     const int32_t *fd_own, *fd_nbr, *fs_own, *fs_nbr;
     // the mixed form's inviscid face list: the face dofs above with each periodic pair of face
     // tasks computed once (the partner's slot receives -F, as an interior face's neighbour does)
-    // when the scheme does not read alpha; per entry the task face dof, both dofs and slots, and
-    // the boundary condition to apply (-1: none)
+    // when the scheme does not read alpha. Per entry two 16-byte words: (own dof, other dof,
+    // own slot, other slot) and (the FP32 unit normal, the task face dof as integer bits). The
+    // other dof is -1 exactly where a boundary condition supplies the ghost state; the other
+    // slot is set for interior faces and merged periodic pairs.
     int64_t n_mx;
-    const int32_t *mx_fd, *mx_own, *mx_nbr, *mx_sown, *mx_snbr, *mx_bc;
+    const int4* mx_dofs;
+    const float4* mx_geom;
     const plens_bc_desc* bcs;
     int n_bc;
     const plens_expr_insn* expr_code;
@@ -184,6 +191,14 @@ template <class T> __device__ __forceinline__ double to_f64(T x)
     if constexpr (sizeof(T) == 8) return x; else return f32_to_f64(x);
 }
 
+// A metric term in the arithmetic type: the FP64 array (plain form) or its FP32 rounding (mixed
+// form), which equals to_real<float> of the FP64 value bit for bit.
+template <class T>
+__device__ __forceinline__ T metric(const double* f64, const float* f32, int64_t i)
+{
+    if constexpr (sizeof(T) == 8) return f64[i]; else return f32[i];
+}
+
 // One node's state in the arithmetic type: the FP64 state (plain form) or its FP32 image (mixed).
 template <class T>
 __device__ __forceinline__ void load_state(const Dev& dv, int64_t dof, T c[5])
@@ -195,9 +210,11 @@ __device__ __forceinline__ void load_state(const Dev& dv, int64_t dof, T c[5])
     }
 }
 
-// The face-value and auxiliary-variable buffers are intermediates of one RHS: the mixed form
-// stores them in FP32 inside the FP64-sized allocations.
+// The face-value and auxiliary-variable buffers are intermediates of one RHS, and the RK4
+// registers hold dt*R, an FP32 result in the mixed form: the mixed form stores all of them in
+// FP32 inside the FP64-sized allocations (exactly, for the registers).
 template <class T> __device__ __forceinline__ T* as_real(double* p) { return reinterpret_cast<T*>(p); }
+template <class T> __device__ __forceinline__ const T* as_real(const double* p) { return reinterpret_cast<const T*>(p); }
 
 // assert_positivity (dgsem/plens.cc:2531-2546, navier_stokes.cc:326-337): rho > 0 and e > 0,
 // decided in FP64 with the reference's expressions.

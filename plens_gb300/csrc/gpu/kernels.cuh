@@ -43,6 +43,13 @@ static __global__ void k_dt_finalize(Dev dv)
 }
 
 // mixed form: the FP32 image of the state after the host or a restore changed U
+// FP32 rounding of an FP64 array (the mixed form's metric images)
+static __global__ void k_round_f32(const double* __restrict__ in, float* __restrict__ out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = f64_to_f32(in[i]);
+}
+
 static __global__ void k_state_image(Dev dv)
 {
     const int64_t n = 5 * dv.nd;
@@ -105,7 +112,7 @@ __device__ __forceinline__ T dof_stable_step(const Dev& dv, const GasP& g, doubl
     for (int row = 0; row < 3; ++row) {
         T acc = T(0);
 #pragma unroll
-        for (int col = 0; col < 3; ++col) acc += to_real<T>(dv.Jinv[(col * 3 + row) * dv.nd + dof]) * vel[col];
+        for (int col = 0; col < 3; ++col) acc += metric<T>(dv.Jinv, dv.Jinvf, (col * 3 + row) * dv.nd + dof) * vel[col];
         adv[row] = acc;
     }
     T madv = adv[0];
@@ -750,7 +757,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
 #pragma unroll
         for (int v = 0; v < 5; ++v) sE[(cl * 5 + v) * P3 + node] = e[v];
 #pragma unroll
-        for (int m = 0; m < 9; ++m) sJa[(cl * 9 + m) * P3 + node] = to_real<T>(dv.Ja[m * dv.nd + dof]);
+        for (int m = 0; m < 9; ++m) sJa[(cl * 9 + m) * P3 + node] = metric<T>(dv.Ja, dv.Jaf, m * dv.nd + dof);
         for (int sl = node; sl < 6 * P2; sl += P3) {
             T fc[5], fe[5];
 #pragma unroll
@@ -797,7 +804,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
                 }
             }
         }
-        const T jinv = fdiv(T(1.0), to_real<T>(dv.detJ[cell * P3 + node]));
+        const T jinv = fdiv(T(1.0), metric<T>(dv.detJ, dv.detJf, cell * P3 + node));
 #pragma unroll
         for (int v = 0; v < 5; ++v) grad[gd][v] = acc[v] * jinv;
     }
@@ -922,7 +929,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                                Q[4 * P3 + node] * Q[4 * P3 + node];
         }
 #pragma unroll
-        for (int m = 0; m < 9; ++m) J[m * P3 + node] = to_real<T>(dv.Ja[m * dv.nd + dof]);
+        for (int m = 0; m < 9; ++m) J[m * P3 + node] = metric<T>(dv.Ja, dv.Jaf, m * dv.nd + dof);
         if (VISC) {
 #pragma unroll
             for (int m = 0; m < 9; ++m) Av[m * P3 + node] = as_real<T>(dv.avars)[m * dv.nd + dof];
@@ -1066,8 +1073,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
 
     // ---- phase B: HO inviscid = volume + surface, scaled by 1/(-detJ)
     const int ti[3] = {node % P, (node / P) % P, node / P2};
-    const double detJ = valid ? dv.detJ[dof] : 1.0;
-    const T detJt = to_real<T>(detJ);
+    const T detJt = valid ? metric<T>(dv.detJ, dv.detJf, dof) : T(1);
     T ho[5] = {0, 0, 0, 0, 0};
     if (valid) {
 #pragma unroll
@@ -1261,8 +1267,8 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
 
     // ---- phase D: blend, then either store the residual or advance the RK registers
     if constexpr (sizeof(T) == 4) {
-        // mixed form: blend and register combination in FP32 (the residual is an FP32 result),
-        // registers stored and the state accumulated in FP64
+        // mixed form: blend and register combination in FP32 (the residual is an FP32 result,
+        // and so is dt*R, which the registers hold in FP32), the state accumulated in FP64
         float R[5];
         const float ad = VISC ? f64_to_f32(dv.alpha_d[cell]) : 0.0f;
 #pragma unroll
@@ -1286,9 +1292,9 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
             if (sa.mode == 1) {
                 float inc;
                 if (sa.stage == 1) inc = sa.fc2 * Rs;
-                else if (sa.stage == 2) inc = sa.fc1 * f64_to_f32(sa.R1[k]) + sa.fc2 * Rs;
-                else inc = sa.fc0 * f64_to_f32(sa.R0[k]) + sa.fc1 * f64_to_f32(sa.R1[k]) + sa.fc2 * Rs;
-                sa.Rw[k] = f32_to_f64(Rs);
+                else if (sa.stage == 2) inc = sa.fc1 * as_real<float>(sa.R1)[k] + sa.fc2 * Rs;
+                else inc = sa.fc0 * as_real<float>(sa.R0)[k] + sa.fc1 * as_real<float>(sa.R1)[k] + sa.fc2 * Rs;
+                as_real<float>(sa.Rw)[k] = Rs;
                 const double un = ud[v] + f32_to_f64(inc);
                 dv.U[k] = un;
                 dv.Uf[k] = f64_to_f32(un);

@@ -512,7 +512,8 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
             const int isf = prm->inv_surf_flux;
             const bool merge = isf != PLENS_ISF_CHANDRASHEKHAR && isf != PLENS_ISF_RUSANOV_HLLC &&
                                isf != PLENS_ISF_RUSANOV_AUSM_PLUS_UP;
-            std::vector<int32_t> mfd, mown, mnbr, msown, msnbr, mbc;
+            std::vector<int4> mdofs;
+            std::vector<float4> mgeom;
             for (int64_t t = 0; t < nt; ++t) {
                 const int bc = mesh->ft_bc[t];
                 const bool periodic = bc >= 0 && bc < prm->n_bc && prm->bcs[bc].type == PLENS_BC_PERIODIC;
@@ -521,26 +522,24 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
                 if (periodic && merge && pkey < key) continue;  // the partner's task computes it
                 for (int q = 0; q < P2; ++q) {
                     const int64_t k = t * P2 + q;
-                    mfd.push_back((int32_t)k);
-                    mown.push_back(own[k]);
-                    mnbr.push_back(nbr[k]);
-                    msown.push_back(sown[k]);
+                    int32_t slot_nb = snbr[k];
                     if (periodic && merge) {
                         const int64_t nb = mesh->ft_nbr_cell[t];
                         const int fn = mesh->ft_nbr_face[t], qn = mesh->ft_nbr_fdof[k];
-                        msnbr.push_back((int32_t)((nb * 6 + fn) * P2 + qn));
-                        mbc.push_back(-1);
-                    } else {
-                        msnbr.push_back(snbr[k]);
-                        mbc.push_back(bc);
+                        slot_nb = (int32_t)((nb * 6 + fn) * P2 + qn);
                     }
+                    mdofs.push_back(make_int4(own[k], nbr[k], sown[k], slot_nb));
+                    // round to nearest, as f64_to_f32 on the device
+                    const float n0 = (float)mesh->ft_normal[3 * k], n1 = (float)mesh->ft_normal[3 * k + 1],
+                                n2 = (float)mesh->ft_normal[3 * k + 2];
+                    int32_t kk = (int32_t)k;
+                    float kf;
+                    std::memcpy(&kf, &kk, sizeof(kf));
+                    mgeom.push_back(make_float4(n0, n1, n2, kf));
                 }
             }
-            d.n_mx = (int64_t)mfd.size();
-            if ((r = dupload(c, &d.mx_fd, mfd.data(), mfd.size())) || (r = dupload(c, &d.mx_own, mown.data(), mown.size())) ||
-                (r = dupload(c, &d.mx_nbr, mnbr.data(), mnbr.size())) ||
-                (r = dupload(c, &d.mx_sown, msown.data(), msown.size())) ||
-                (r = dupload(c, &d.mx_snbr, msnbr.data(), msnbr.size())) || (r = dupload(c, &d.mx_bc, mbc.data(), mbc.size())))
+            d.n_mx = (int64_t)mdofs.size();
+            if ((r = dupload(c, &d.mx_dofs, mdofs.data(), mdofs.size())) || (r = dupload(c, &d.mx_geom, mgeom.data(), mgeom.size())))
                 return r;
         }
     }
@@ -558,6 +557,24 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         if ((r = dupload(c, &d.cell_wall, wall.data(), nc))) return r;
     }
     if (c->mixed && (r = dalloc(c, &d.Uf, 5 * nd))) return r;
+    if (c->mixed) {
+        // the FP32 rounding of the metric terms, once (every FP32 consumer reads these instead of
+        // rounding the FP64 arrays itself: the same values)
+        float *detJf = nullptr, *Jaf = nullptr, *Jinvf = nullptr;
+        if ((r = dalloc(c, &detJf, nd)) || (r = dalloc(c, &Jaf, 9 * nd)) || (r = dalloc(c, &Jinvf, 9 * nd))) return r;
+        // the uploads above ran on the legacy stream, which this non-blocking stream does not
+        // wait for (a pageable cudaMemcpy may return before its DMA lands)
+        CK(cudaDeviceSynchronize());
+        const unsigned grid = (unsigned)std::min<int64_t>((9 * nd + 255) / 256, 152 * 16);
+        k_round_f32<<<grid, 256, 0, c->stream>>>(d.detJ, detJf, nd);
+        k_round_f32<<<grid, 256, 0, c->stream>>>(d.Ja, Jaf, 9 * nd);
+        k_round_f32<<<grid, 256, 0, c->stream>>>(d.Jinv, Jinvf, 9 * nd);
+        c->launches += 3;
+        if ((r = check_launch(c, "metric images"))) return r;
+        d.detJf = detJf;
+        d.Jaf = Jaf;
+        d.Jinvf = Jinvf;
+    }
     if ((r = dalloc(c, &d.U, 5 * nd)) || (r = dalloc(c, &d.alpha_raw, nc)) || (r = dalloc(c, &d.alpha, nc)) ||
         (r = dalloc(c, &d.alpha_d, nc)) || (r = dalloc(c, &d.sf, 5 * c->nslot)) || (r = dalloc(c, &c->sc, 1)) ||
         (r = dalloc(c, &c->Rout, 5 * nd)))

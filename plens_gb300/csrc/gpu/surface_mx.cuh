@@ -12,27 +12,28 @@ namespace plens_gpu {
 
 // per face dof: what the loop carries between iterations
 struct FaceItem {
-    int64_t idx;     // face dof of the task list (-1: none)
-    int32_t gd, gdn; // own dof, other dof (interior or periodic partner; -1 for other BCs)
-    int32_t bc;
+    int32_t idx;      // face dof of the task list (-1: none)
+    int32_t gd, gdn;  // own dof, other dof (interior or periodic partner; -1 where a BC gives the ghost)
     int32_t slot, slot_nb;  // face slots of both sides (-1: no neighbour slot)
     float n[3];
 };
 
-// entry i of the mixed face list; idx = the task face dof (normal, location, task)
+// entry i of the mixed face list: two 16-byte loads
 __device__ __forceinline__ FaceItem face_item(const Dev& dv, int64_t i, int64_t total)
 {
     FaceItem it;
     it.idx = -1;
     if (i < total) {
-        it.idx = dv.mx_fd[i];
-        it.gd = dv.mx_own[i];
-        it.gdn = dv.mx_nbr[i];
-        it.bc = dv.mx_bc[i];
-        it.slot = dv.mx_sown[i];
-        it.slot_nb = dv.mx_snbr[i];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) it.n[d] = f64_to_f32(dv.ft_normal[it.idx * 3 + d]);
+        const int4 a = __ldg(dv.mx_dofs + i);
+        const float4 b = __ldg(dv.mx_geom + i);
+        it.gd = a.x;
+        it.gdn = a.y;
+        it.slot = a.z;
+        it.slot_nb = a.w;
+        it.n[0] = b.x;
+        it.n[1] = b.y;
+        it.n[2] = b.z;
+        it.idx = __float_as_int(b.w);
     }
     return it;
 }
@@ -71,17 +72,17 @@ __global__ void __launch_bounds__(128, 4) k_surface_inv_mx(Dev dv, GasP g, doubl
         const int64_t ti = cur.idx / P2;
         float fb = 0.0f;
         if (blended) {
+            // own alpha on boundary faces (periodic included: not merged for these schemes),
+            // the mean of both cells' on interior faces (the only ones with a neighbour slot)
             const int64_t c = dv.ft_cell[ti];
             float a = f64_to_f32(dv.alpha[c]);
-            if (cur.bc < 0) a = 0.5f * (a + f64_to_f32(dv.alpha[dv.ft_nbr_cell[ti]]));
+            if (cur.slot_nb >= 0) a = 0.5f * (a + f64_to_f32(dv.alpha[dv.ft_nbr_cell[ti]]));
             fb = (a <= 0.0f) ? 0.0f : (a <= 1.0f ? a : 1.0f);
         }
-        if (cur.bc >= 0) {
-            const plens_bc_desc& b = dv.bcs[cur.bc];
-            if (b.type != PLENS_BC_PERIODIC) {  // periodic: the partner's state is the ghost
-                float av[9] = {}, ag[9];
-                bc_ghost<float>(2, dv, g, b, cs, av, cur.n, dv.ft_xyz + cur.idx * 3, s->time, -1, c2, ag);
-            }
+        if (cur.gdn < 0) {  // a boundary condition gives the ghost state (periodic: the partner's)
+            const plens_bc_desc& b = dv.bcs[dv.ft_bc[ti]];
+            float av[9] = {}, ag[9];
+            bc_ghost<float>(2, dv, g, b, cs, av, cur.n, dv.ft_xyz + (int64_t)cur.idx * 3, s->time, -1, c2, ag);
         }
         float fl[5];
         inv_surf_flux_mx(cs, c2, cur.n, gm, g.isf, fb, fl);

@@ -4,8 +4,8 @@
 // every per-block input staged in shared memory by TMA bulk copies. For even P each cell's P^3
 // values of a variable are a multiple of 16 bytes, so a block's CPB cells are one contiguous,
 // 16-byte aligned chunk per variable: one thread issues the copies, two mbarriers signal them --
-// the state, metrics and Jacobians that the flux phase needs first, then the face values and the
-// RK registers, which arrive while the fluxes are computed.
+// the FP32 state image and metric images that the flux phase needs first, then the FP64 state,
+// the face values and the RK registers, which arrive while the fluxes are computed.
 #pragma once
 
 #include "async.cuh"
@@ -19,25 +19,29 @@ struct MxSmem {
     static constexpr int P2 = P * P, P3 = P2 * P, CPB = CellBlock<P>::CPB, NB = CPB * P3, NF = CPB * 6 * P2;
     static constexpr int NQ = 10;  // rho, 1/rho, v0, v1, v2, p, beta, ln rho, ln beta, |v|^2
     static constexpr size_t up16(size_t x) { return (x + 15) / 16 * 16; }
-    // staged inputs (FP64 state/metrics/registers, FP32 face values and auxiliary variables)
+    // staged inputs: the FP64 state (for the update), its FP32 image (for the fluxes), the FP32
+    // metric images, the FP32 RK registers, FP32 face values and auxiliary variables
     static constexpr size_t oU = 0;                                   // double [5][NB]
-    static constexpr size_t oDet = oU + up16(8 * 5 * NB);             // double [NB]
-    static constexpr size_t oR0 = oDet + up16(8 * NB);                // double [5][NB]
-    static constexpr size_t oR1 = oR0 + up16(8 * 5 * NB);             // double [5][NB]
-    static constexpr size_t oSf = oR1 + up16(8 * 5 * NB);             // float [5][NF]
+    static constexpr size_t oUf = oU + up16(8 * 5 * NB);              // float [5][NB]
+    static constexpr size_t oDet = oUf + up16(4 * 5 * NB);            // float [NB]
+    static constexpr size_t oJ = oDet + up16(4 * NB);                 // float [9][NB]
+    static constexpr size_t oR0 = oJ + up16(4 * 9 * NB);              // float [5][NB]
+    static constexpr size_t oR1 = oR0 + up16(4 * 5 * NB);             // float [5][NB]
+    static constexpr size_t oSf = oR1 + up16(4 * 5 * NB);             // float [5][NF]
     static constexpr size_t oSf3 = oSf + up16(4 * 5 * NF);            // float [5][NF] (viscous)
     static constexpr size_t oAv = oSf3 + (VISC ? up16(4 * 5 * NF) : 0);  // float [9][NB] (viscous)
-    // Ja (double [9][NB]) is staged where the flux partial sums go once it is converted
-    static constexpr size_t oAcc = oAv + (VISC ? up16(4 * 9 * NB) : 0);
-    static constexpr size_t accBytes = (8 * 9 * NB > 4 * 15 * NB) ? 8 * 9 * NB : 4 * 15 * NB;
-    static constexpr size_t oQ = oAcc + up16(accBytes);               // float [CPB][NQ][P3]
-    static constexpr size_t oC = oQ + up16(4 * NQ * NB);              // float [CPB][5][P3]
-    static constexpr size_t oJ = oC + up16(4 * 5 * NB);               // float [CPB][9][P3]
-    static constexpr size_t bytes = oJ + up16(4 * 9 * NB);
+    static constexpr size_t oAcc = oAv + (VISC ? up16(4 * 9 * NB) : 0);  // float [CPB][15][P3]
+    static constexpr size_t oQ = oAcc + up16(4 * 15 * NB);            // float [CPB][NQ][P3]
+    static constexpr size_t bytes = oQ + up16(4 * NQ * NB);
 };
 
+// Resident blocks per SM the register allocation is sized for: six 128-thread blocks at P = 2, 4
+// (80 registers, the shared-memory limit is also six); two 224-thread blocks at P = 6.
+template <int P>
+constexpr int vol_mx_min_blocks() { return P == 6 ? 2 : 6; }
+
 template <int P, bool VISC>
-__global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, Ops ops, GasP g, StageArgs sa)
+__global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>()) k_volume_mx(Dev dv, Ops ops, GasP g, StageArgs sa)
 {
     static_assert(P % 2 == 0, "bulk staging needs 16-byte aligned per-cell chunks (even P)");
     using CB = CellBlock<P>;
@@ -46,17 +50,16 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bars[2];
     double* stU = reinterpret_cast<double*>(smem_raw + L::oU);
-    double* stDet = reinterpret_cast<double*>(smem_raw + L::oDet);
-    double* stR0 = reinterpret_cast<double*>(smem_raw + L::oR0);
-    double* stR1 = reinterpret_cast<double*>(smem_raw + L::oR1);
+    float* stUf = reinterpret_cast<float*>(smem_raw + L::oUf);
+    float* stDet = reinterpret_cast<float*>(smem_raw + L::oDet);
+    float* stJ = reinterpret_cast<float*>(smem_raw + L::oJ);
+    float* stR0 = reinterpret_cast<float*>(smem_raw + L::oR0);
+    float* stR1 = reinterpret_cast<float*>(smem_raw + L::oR1);
     float* stSf = reinterpret_cast<float*>(smem_raw + L::oSf);
     float* stSf3 = reinterpret_cast<float*>(smem_raw + L::oSf3);
     float* stAv = reinterpret_cast<float*>(smem_raw + L::oAv);
-    double* stJa = reinterpret_cast<double*>(smem_raw + L::oAcc);
     float* sAcc = reinterpret_cast<float*>(smem_raw + L::oAcc);
     float* sQ = reinterpret_cast<float*>(smem_raw + L::oQ);
-    float* sC = reinterpret_cast<float*>(smem_raw + L::oC);
-    float* sJ = reinterpret_cast<float*>(smem_raw + L::oJ);
 
     Scalars* s = dv.sc;
     if (!s->active) return;
@@ -74,22 +77,24 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         const uint32_t bd = (uint32_t)(8 * ncb * P3), bf = (uint32_t)(4 * ncb * 6 * P2), bv = (uint32_t)(4 * ncb * P3);
         const int64_t d0 = cell0 * P3, f0 = cell0 * 6 * P2;
-        mbar_arrive_expect_tx(&bars[0], bd * (5 + 9 + 1));
+        mbar_arrive_expect_tx(&bars[0], bv * (5 + 9 + 1));
 #pragma unroll
-        for (int v = 0; v < 5; ++v) tma_load_1d(stU + v * NB, dv.U + v * dv.nd + d0, bd, &bars[0]);
+        for (int v = 0; v < 5; ++v) tma_load_1d(stUf + v * NB, dv.Uf + v * dv.nd + d0, bv, &bars[0]);
 #pragma unroll
-        for (int m = 0; m < 9; ++m) tma_load_1d(stJa + m * NB, dv.Ja + m * dv.nd + d0, bd, &bars[0]);
-        tma_load_1d(stDet, dv.detJ + d0, bd, &bars[0]);
-        uint32_t late = bf * 5 + (need_r0 ? bd * 5 : 0) + (need_r1 ? bd * 5 : 0) + (VISC ? bf * 5 + bv * 9 : 0);
+        for (int m = 0; m < 9; ++m) tma_load_1d(stJ + m * NB, dv.Jaf + m * dv.nd + d0, bv, &bars[0]);
+        tma_load_1d(stDet, dv.detJf + d0, bv, &bars[0]);
+        uint32_t late = bd * 5 + bf * 5 + (need_r0 ? bv * 5 : 0) + (need_r1 ? bv * 5 : 0) + (VISC ? bf * 5 + bv * 9 : 0);
         mbar_arrive_expect_tx(&bars[1], late);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) tma_load_1d(stU + v * NB, dv.U + v * dv.nd + d0, bd, &bars[1]);
 #pragma unroll
         for (int v = 0; v < 5; ++v) tma_load_1d(stSf + v * NF, as_real<float>(dv.sf) + v * dv.nslot + f0, bf, &bars[1]);
         if (need_r0)
 #pragma unroll
-            for (int v = 0; v < 5; ++v) tma_load_1d(stR0 + v * NB, sa.R0 + v * dv.nd + d0, bd, &bars[1]);
+            for (int v = 0; v < 5; ++v) tma_load_1d(stR0 + v * NB, as_real<float>(sa.R0) + v * dv.nd + d0, bv, &bars[1]);
         if (need_r1)
 #pragma unroll
-            for (int v = 0; v < 5; ++v) tma_load_1d(stR1 + v * NB, sa.R1 + v * dv.nd + d0, bd, &bars[1]);
+            for (int v = 0; v < 5; ++v) tma_load_1d(stR1 + v * NB, as_real<float>(sa.R1) + v * dv.nd + d0, bv, &bars[1]);
         if (VISC) {
 #pragma unroll
             for (int v = 0; v < 5; ++v) tma_load_1d(stSf3 + v * NF, as_real<float>(dv.sf3) + v * dv.nslot + f0, bf, &bars[1]);
@@ -109,18 +114,15 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
 
     const float gm = f64_to_f32(g.gamma);
     float* Q = sQ + cl * NQ * P3;
-    float* Cc = sC + cl * 5 * P3;
-    float* J = sJ + cl * 9 * P3;
+    const float* Cc = stUf + cl * P3;  // the FP32 state image: variable v at node n is Cc[v * NB + n]
+    const float* J = stJ + cl * P3;  // component m of Ja at node n of this cell: J[m * NB + n]
     float* Acc = sAcc + cl * 15 * P3;
     const int64_t dof = cell * P3 + node;
     const int bn = cl * P3 + node;  // node index within the block's staged chunks
     if (valid) {
         float c[5];
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
-            c[v] = f64_to_f32(stU[v * NB + bn]);
-            Cc[v * P3 + node] = c[v];
-        }
+        for (int v = 0; v < 5; ++v) c[v] = Cc[v * NB + node];
         const float p = get_p(c, gm);
         const float ri = 1.0f / c[0];
         const float v0 = c[1] * ri, v1 = c[2] * ri, v2 = c[3] * ri, beta = 0.5f * c[0] / p;
@@ -134,17 +136,23 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
         Q[7 * P3 + node] = __logf(c[0]);
         Q[8 * P3 + node] = __logf(beta);
         Q[9 * P3 + node] = v0 * v0 + v1 * v1 + v2 * v2;
-#pragma unroll
-        for (int m = 0; m < 9; ++m) J[m * P3 + node] = f64_to_f32(stJa[m * NB + bn]);
     }
-    __syncthreads();  // Ja staging is reused for the partial sums from here on
+    __syncthreads();
     const double alpha = valid ? dv.alpha[cell] : 0.0;
     const float alpha_t = f64_to_f32(alpha);
 
-    // ---- phase A: two-point volume fluxes per line
-    if (valid) {
+    // ---- phase A: two-point volume fluxes per line. The block's line tasks are numbered flat,
+    // cell after cell, so the threads past the last task -- whole warps at P = 4 -- issue nothing
+    // here and leave their issue slots to the other blocks.
+    {
+        constexpr int TPC = 3 * P2;  // line tasks per cell
         const float hg = __fdividef(0.5f, gm - 1.0f), gf = __fdividef(gm, gm - 1.0f);
-        for (int task = node; task < 3 * P2; task += P3) {
+        for (int ft = tid; ft < ncb * TPC; ft += CB::THREADS) {
+            const int tc = ft / TPC, task = ft - tc * TPC;
+            const float* Qa = sQ + tc * NQ * P3;
+            const float* Ca = stUf + tc * P3;
+            const float* Jt = stJ + tc * P3;
+            float* At = sAcc + tc * 15 * P3;
             const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
             float acc[P][5];
 #pragma unroll
@@ -159,8 +167,8 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                     const int ni = line_node<P>(dir, la, lb, i);
                     float qi[10];
 #pragma unroll
-                    for (int k = 0; k < 10; ++k) qi[k] = Q[k * P3 + ni];
-                    const float ji[3] = {J[(dir * 3) * P3 + ni], J[(dir * 3 + 1) * P3 + ni], J[(dir * 3 + 2) * P3 + ni]};
+                    for (int k = 0; k < 10; ++k) qi[k] = Qa[k * P3 + ni];
+                    const float ji[3] = {Jt[(dir * 3) * NB + ni], Jt[(dir * 3 + 1) * NB + ni], Jt[(dir * 3 + 2) * NB + ni]};
                     if (i == 0 || i == N) {
                         float F[5];
                         chandrashekhar_same_f32(qi, ji, gf, F);
@@ -173,9 +181,9 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                         const int nm = line_node<P>(dir, la, lb, m);
                         float qm[10];
 #pragma unroll
-                        for (int k = 0; k < 10; ++k) qm[k] = Q[k * P3 + nm];
-                        const float nv[3] = {ji[0] + J[(dir * 3) * P3 + nm], ji[1] + J[(dir * 3 + 1) * P3 + nm],
-                                             ji[2] + J[(dir * 3 + 2) * P3 + nm]};
+                        for (int k = 0; k < 10; ++k) qm[k] = Qa[k * P3 + nm];
+                        const float nv[3] = {ji[0] + Jt[(dir * 3) * NB + nm], ji[1] + Jt[(dir * 3 + 1) * NB + nm],
+                                             ji[2] + Jt[(dir * 3 + 2) * NB + nm]};
                         float F[5];
                         chandrashekhar_pair_f32(qi, qm, nv, hg, F);
                         const float di = opD<float>(ops, i * P + m), dm = opD<float>(ops, m * P + i);
@@ -193,18 +201,18 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                     const int ni = line_node<P>(dir, la, lb, i);
                     float qi[7];
 #pragma unroll
-                    for (int k = 0; k < 7; ++k) qi[k] = Q[k * P3 + ni];
-                    const float ci[5] = {Cc[ni], Cc[P3 + ni], Cc[2 * P3 + ni], Cc[3 * P3 + ni], Cc[4 * P3 + ni]};
+                    for (int k = 0; k < 7; ++k) qi[k] = Qa[k * P3 + ni];
+                    const float ci[5] = {Ca[ni], Ca[NB + ni], Ca[2 * NB + ni], Ca[3 * NB + ni], Ca[4 * NB + ni]};
 #pragma unroll
                     for (int m = i; m < P; ++m) {
                         const int nm = line_node<P>(dir, la, lb, m);
                         float qm[7];
 #pragma unroll
-                        for (int k = 0; k < 7; ++k) qm[k] = Q[k * P3 + nm];
-                        const float cm[5] = {Cc[nm], Cc[P3 + nm], Cc[2 * P3 + nm], Cc[3 * P3 + nm], Cc[4 * P3 + nm]};
+                        for (int k = 0; k < 7; ++k) qm[k] = Qa[k * P3 + nm];
+                        const float cm[5] = {Ca[nm], Ca[NB + nm], Ca[2 * NB + nm], Ca[3 * NB + nm], Ca[4 * NB + nm]};
                         float nv[3];
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) nv[d] = 0.5f * (J[(dir * 3 + d) * P3 + ni] + J[(dir * 3 + d) * P3 + nm]);
+                        for (int d = 0; d < 3; ++d) nv[d] = 0.5f * (Jt[(dir * 3 + d) * NB + ni] + Jt[(dir * 3 + d) * NB + nm]);
                         float nn = sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
                         const float dn[3] = {__fdividef(nv[0], nn), __fdividef(nv[1], nn), __fdividef(nv[2], nn)};
                         float F[5];
@@ -223,7 +231,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
             for (int i = 0; i < P; ++i) {
                 const int ni = line_node<P>(dir, la, lb, i);
 #pragma unroll
-                for (int v = 0; v < 5; ++v) Acc[(dir * 5 + v) * P3 + ni] = acc[i][v];
+                for (int v = 0; v < 5; ++v) At[(dir * 5 + v) * P3 + ni] = acc[i][v];
             }
         }
     }
@@ -236,13 +244,13 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
 
     // ---- phase B: HO inviscid = volume + surface, scaled by 1/(-detJ)
     const int ti[3] = {node % P, (node / P) % P, node / P2};
-    const float detJ = valid ? f64_to_f32(stDet[bn]) : 1.0f;
+    const float detJ = valid ? stDet[bn] : 1.0f;
     const float* sfb = stSf + cl * 6 * P2;  // this cell's face slots; variable stride NF
     float ho[5] = {0, 0, 0, 0, 0};
     if (valid) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) ho[v] = Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node];
-        const float ci[5] = {Cc[node], Cc[P3 + node], Cc[2 * P3 + node], Cc[3 * P3 + node], Cc[4 * P3 + node]};
+        const float ci[5] = {Cc[node], Cc[NB + node], Cc[2 * NB + node], Cc[3 * NB + node], Cc[4 * NB + node]};
 #pragma unroll
         for (int sd = 0; sd < 3; ++sd) {
 #pragma unroll
@@ -251,7 +259,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                 const int f = 2 * sd + lr;
                 const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
                 // (F* - F_in(n/|n|)) |n| = F* |n| - F_in(n): the physical flux is linear in n
-                const float jn[3] = {J[(sd * 3) * P3 + node], J[(sd * 3 + 1) * P3 + node], J[(sd * 3 + 2) * P3 + node]};
+                const float jn[3] = {J[(sd * 3) * NB + node], J[(sd * 3 + 1) * NB + node], J[(sd * 3 + 2) * NB + node]};
                 const float nn = sqrtf(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
                 float fin[5];
                 inv_flux(ci, jn, gm, fin);
@@ -277,10 +285,10 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
 #pragma unroll
         for (int m = 0; m < 9; ++m) av[m] = valid ? stAv[m * NB + bn] : 0.0f;
         if (valid) {
-            const float ci[5] = {Cc[node], Cc[P3 + node], Cc[2 * P3 + node], Cc[3 * P3 + node], Cc[4 * P3 + node]};
+            const float ci[5] = {Cc[node], Cc[NB + node], Cc[2 * NB + node], Cc[3 * NB + node], Cc[4 * NB + node]};
 #pragma unroll
             for (int md = 0; md < 3; ++md) {
-                const float jn[3] = {J[(md * 3) * P3 + node], J[(md * 3 + 1) * P3 + node], J[(md * 3 + 2) * P3 + node]};
+                const float jn[3] = {J[(md * 3) * NB + node], J[(md * 3 + 1) * NB + node], J[(md * 3 + 2) * NB + node]};
                 float F[5];
                 dif_flux(ci, av, jn, F);  // linear in the direction: F(n/|n|) |n| = F(n)
 #pragma unroll
@@ -298,7 +306,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                     for (int v = 0; v < 5; ++v) hd[v] += dvl * Acc[(md * 5 + v) * P3 + lo];
                 }
             }
-            const float ci[5] = {Cc[node], Cc[P3 + node], Cc[2 * P3 + node], Cc[3 * P3 + node], Cc[4 * P3 + node]};
+            const float ci[5] = {Cc[node], Cc[NB + node], Cc[2 * NB + node], Cc[3 * NB + node], Cc[4 * NB + node]};
             const float* sf3b = stSf3 + cl * 6 * P2;
 #pragma unroll
             for (int sd = 0; sd < 3; ++sd) {
@@ -307,7 +315,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                     if (ti[sd] != (lr ? N : 0)) continue;
                     const int f = 2 * sd + lr;
                     const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
-                    const float jn[3] = {J[(sd * 3) * P3 + node], J[(sd * 3 + 1) * P3 + node], J[(sd * 3 + 2) * P3 + node]};
+                    const float jn[3] = {J[(sd * 3) * NB + node], J[(sd * 3 + 1) * NB + node], J[(sd * 3 + 2) * NB + node]};
                     const float nn = sqrtf(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
                     float fin[5];
                     dif_flux(ci, av, jn, fin);
@@ -335,9 +343,19 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
     if (any_lo) {
         __syncthreads();
         const bool do_lo = valid && stored_gt0<float>(alpha);
-        if (do_lo) {
-            const float fb = (alpha_t <= 0.0f) ? 0.0f : (alpha_t <= 1.0f ? alpha_t : 1.0f);
-            for (int task = node; task < 3 * P2; task += P3) {
+        {
+            // line tasks numbered flat over the block's cells, as in phase A
+            constexpr int TPC = 3 * P2;
+            for (int ft = tid; ft < ncb * TPC; ft += CB::THREADS) {
+                const int tc = ft / TPC, task = ft - tc * TPC;
+                const double a_t = dv.alpha[cell0 + tc];
+                if (!stored_gt0<float>(a_t)) continue;
+                const float at = f64_to_f32(a_t);
+                const float fb = (at <= 0.0f) ? 0.0f : (at <= 1.0f ? at : 1.0f);
+                const float* Ca = stUf + tc * P3;
+                const float* Jt = stJ + tc * P3;
+                float* At = sAcc + tc * 15 * P3;
+                const float* sfa = stSf + tc * 6 * P2;
                 const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
                 float acc[P][5];
 #pragma unroll
@@ -347,7 +365,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                 // running subcell normal n_(i-1,i) = Ja_0 + sum_{l<i} sum_m Q_lm Ja_m
                 // (metric_terms.cc:106-141)
                 const int n0 = line_node<P>(dir, la, lb, 0);
-                float sn[3] = {J[(dir * 3) * P3 + n0], J[(dir * 3 + 1) * P3 + n0], J[(dir * 3 + 2) * P3 + n0]};
+                float sn[3] = {Jt[(dir * 3) * NB + n0], Jt[(dir * 3 + 1) * NB + n0], Jt[(dir * 3 + 2) * NB + n0]};
 #pragma unroll
                 for (int id = 1; id < P; ++id) {
 #pragma unroll
@@ -355,13 +373,13 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                         const int nm = line_node<P>(dir, la, lb, m);
                         const float qlm = opQ<float>(ops, (id - 1) * P + m);
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) sn[d] += qlm * J[(dir * 3 + d) * P3 + nm];
+                        for (int d = 0; d < 3; ++d) sn[d] += qlm * Jt[(dir * 3 + d) * NB + nm];
                     }
                     const int nl = line_node<P>(dir, la, lb, id - 1), nr = line_node<P>(dir, la, lb, id);
                     const float nn = sqrtf(sn[0] * sn[0] + sn[1] * sn[1] + sn[2] * sn[2]);
                     const float dn[3] = {__fdividef(sn[0], nn), __fdividef(sn[1], nn), __fdividef(sn[2], nn)};
-                    const float cL[5] = {Cc[nl], Cc[P3 + nl], Cc[2 * P3 + nl], Cc[3 * P3 + nl], Cc[4 * P3 + nl]};
-                    const float cR[5] = {Cc[nr], Cc[P3 + nr], Cc[2 * P3 + nr], Cc[3 * P3 + nr], Cc[4 * P3 + nr]};
+                    const float cL[5] = {Ca[nl], Ca[NB + nl], Ca[2 * NB + nl], Ca[3 * NB + nl], Ca[4 * NB + nl]};
+                    const float cR[5] = {Ca[nr], Ca[NB + nr], Ca[2 * NB + nr], Ca[3 * NB + nr], Ca[4 * NB + nr]};
                     float F[5];
                     inv_surf_flux_mx(cL, cR, dn, gm, g.isf, fb, F);
                     const float wl = __fdividef(nn, opW<float>(ops, id - 1)), wr = __fdividef(nn, opW<float>(ops, id));
@@ -378,17 +396,17 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
                     const int ni = line_node<P>(dir, la, lb, i);
                     const int f = 2 * dir + lr;
                     const int q = la + P * lb;
-                    const float j0 = J[(dir * 3) * P3 + ni], j1 = J[(dir * 3 + 1) * P3 + ni], j2 = J[(dir * 3 + 2) * P3 + ni];
+                    const float j0 = Jt[(dir * 3) * NB + ni], j1 = Jt[(dir * 3 + 1) * NB + ni], j2 = Jt[(dir * 3 + 2) * NB + ni];
                     const float nn = sqrtf(j0 * j0 + j1 * j1 + j2 * j2);
                     const float sw = __fdividef(nn, opW<float>(ops, lr * N));  // contrib_sign * flux_sign = +1
 #pragma unroll
-                    for (int v = 0; v < 5; ++v) acc[i][v] += sfb[v * NF + f * P2 + q] * sw;
+                    for (int v = 0; v < 5; ++v) acc[i][v] += sfa[v * NF + f * P2 + q] * sw;
                 }
 #pragma unroll
                 for (int i = 0; i < P; ++i) {
                     const int ni = line_node<P>(dir, la, lb, i);
 #pragma unroll
-                    for (int v = 0; v < 5; ++v) Acc[(dir * 5 + v) * P3 + ni] = acc[i][v];
+                    for (int v = 0; v < 5; ++v) At[(dir * 5 + v) * P3 + ni] = acc[i][v];
                 }
             }
         }
@@ -401,8 +419,8 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
     }
     if (!valid) return;
 
-    // ---- phase D: blend and register combination in FP32 (the residual is an FP32 result);
-    // registers stored and the state accumulated in FP64
+    // ---- phase D: blend and register combination in FP32 (the residual is an FP32 result, and
+    // so is dt*R, which the registers hold in FP32); the state accumulated in FP64
     float R[5];
     const float ad = VISC ? f64_to_f32(dv.alpha_d[cell]) : 0.0f;
 #pragma unroll
@@ -425,9 +443,9 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, 5) k_volume_mx(Dev dv, 
         if (sa.mode == 1) {
             float inc;
             if (sa.stage == 1) inc = sa.fc2 * Rs;
-            else if (sa.stage == 2) inc = sa.fc1 * f64_to_f32(stR1[v * NB + bn]) + sa.fc2 * Rs;
-            else inc = sa.fc0 * f64_to_f32(stR0[v * NB + bn]) + sa.fc1 * f64_to_f32(stR1[v * NB + bn]) + sa.fc2 * Rs;
-            sa.Rw[k] = f32_to_f64(Rs);
+            else if (sa.stage == 2) inc = sa.fc1 * stR1[v * NB + bn] + sa.fc2 * Rs;
+            else inc = sa.fc0 * stR0[v * NB + bn] + sa.fc1 * stR1[v * NB + bn] + sa.fc2 * Rs;
+            as_real<float>(sa.Rw)[k] = Rs;
             const double un = u + f32_to_f64(inc);
             dv.U[k] = un;
             dv.Uf[k] = f64_to_f32(un);
