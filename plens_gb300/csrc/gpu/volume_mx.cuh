@@ -141,6 +141,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>())
     const double alpha = valid ? dv.alpha[cell] : 0.0;
     const float alpha_t = f64_to_f32(alpha);
 
+    bool late_waited = false, late_ok = true;
     // ---- phase A: two-point volume fluxes per line. The block's line tasks are numbered flat,
     // cell after cell, so the threads past the last task -- whole warps at P = 4 -- issue nothing
     // here and leave their issue slots to the other blocks.
@@ -227,6 +228,39 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>())
                     }
                 }
             }
+            // surface term of the line's two end nodes, which lie on faces 2 dir and 2 dir + 1 at
+            // face dof la + P lb (calc_cell_ho_inv_residual, dgsem/plens.cc:3237-3268):
+            // -sign (F* - F_in(n/|n|)) |n| / w = -sign (F* |n| - F_in(n)) / w, the physical flux
+            // being linear in n. Every lane of a warp takes both ends; per node the surface terms
+            // would diverge (a corner node has three, an interior node none). Needs the face
+            // values of the late copy group: each thread waits for it once (bounded; the block
+            // decides on the outcome below).
+            if (!late_waited) {
+                late_ok = mbar_wait0(&bars[1]);
+                late_waited = true;
+            }
+            if (late_ok) {
+                const float* sfa = stSf + tc * 6 * P2;
+                const int q = la + P * lb;
+#pragma unroll
+                for (int lr = 0; lr < 2; ++lr) {
+                    const int i = lr ? N : 0;
+                    const int ni = line_node<P>(dir, la, lb, i);
+                    const int f = 2 * dir + lr;
+                    const float jn[3] = {Jt[(dir * 3) * NB + ni], Jt[(dir * 3 + 1) * NB + ni], Jt[(dir * 3 + 2) * NB + ni]};
+                    const float nn = sqrtf(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
+                    const float ci[5] = {Ca[ni], Ca[NB + ni], Ca[2 * NB + ni], Ca[3 * NB + ni], Ca[4 * NB + ni]};
+                    float fin[5];
+                    inv_flux(ci, jn, gm, fin);
+                    const float ss = lr ? -1.0f : 1.0f;
+                    const float rw = __fdividef(1.0f, opW<float>(ops, lr * N));
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        const float fs = -ss * sfa[v * NF + f * P2 + q];
+                        acc[i][v] += -ss * (fs * nn - fin[v]) * rw;
+                    }
+                }
+            }
 #pragma unroll
             for (int i = 0; i < P; ++i) {
                 const int ni = line_node<P>(dir, la, lb, i);
@@ -236,45 +270,21 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>())
         }
     }
     // face values, registers (and viscous inputs) staged; partial sums visible
-    if (!__syncthreads_and(mbar_wait0(&bars[1]) ? 1 : 0)) {
+    if (!__syncthreads_and((late_ok && mbar_wait0(&bars[1])) ? 1 : 0)) {
         if (tid == 0) s->err = PLENS_GPU_E_TIMEOUT;
         mbar_wait0(&bars[1]);
         return;
     }
 
-    // ---- phase B: HO inviscid = volume + surface, scaled by 1/(-detJ)
+    // ---- phase B: HO inviscid = volume + surface (summed per direction in phase A), scaled by
+    // 1/(-detJ)
     const int ti[3] = {node % P, (node / P) % P, node / P2};
     const float detJ = valid ? stDet[bn] : 1.0f;
-    const float* sfb = stSf + cl * 6 * P2;  // this cell's face slots; variable stride NF
     float ho[5] = {0, 0, 0, 0, 0};
     if (valid) {
-#pragma unroll
-        for (int v = 0; v < 5; ++v) ho[v] = Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node];
-        const float ci[5] = {Cc[node], Cc[NB + node], Cc[2 * NB + node], Cc[3 * NB + node], Cc[4 * NB + node]};
-#pragma unroll
-        for (int sd = 0; sd < 3; ++sd) {
-#pragma unroll
-            for (int lr = 0; lr < 2; ++lr) {
-                if (ti[sd] != (lr ? N : 0)) continue;
-                const int f = 2 * sd + lr;
-                const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
-                // (F* - F_in(n/|n|)) |n| = F* |n| - F_in(n): the physical flux is linear in n
-                const float jn[3] = {J[(sd * 3) * NB + node], J[(sd * 3 + 1) * NB + node], J[(sd * 3 + 2) * NB + node]};
-                const float nn = sqrtf(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
-                float fin[5];
-                inv_flux(ci, jn, gm, fin);
-                const float ss = lr ? -1.0f : 1.0f;
-                const float rw = __fdividef(1.0f, opW<float>(ops, lr * N));
-#pragma unroll
-                for (int v = 0; v < 5; ++v) {
-                    const float fs = -ss * sfb[v * NF + f * P2 + q];
-                    ho[v] += -ss * (fs * nn - fin[v]) * rw;
-                }
-            }
-        }
         const float js = __fdividef(-1.0f, detJ);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) ho[v] *= js;
+        for (int v = 0; v < 5; ++v) ho[v] = (Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node]) * js;
     }
 
     // ---- viscous HO residual: nodal viscous fluxes along each contravariant direction
