@@ -81,11 +81,14 @@ struct Launch {
     }
     static int volume(bool visc, const Dev& dv, const Ops& ops, const GasP& g, const StageArgs& sa, cudaStream_t st)
     {
-        // mixed form, even P: the TMA-staged kernel
+        // mixed form, even P, Chandrashekhar volume flux (the configurations' scheme): the
+        // TMA-staged kernel; the other volume fluxes take the generic kernel
         if constexpr (sizeof(T) == 4 && P % 2 == 0) {
-            if (visc) volume_mx<true>(dv, ops, g, sa, st);
-            else volume_mx<false>(dv, ops, g, sa, st);
-            return 1;
+            if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) {
+                if (visc) volume_mx<true>(dv, ops, g, sa, st);
+                else volume_mx<false>(dv, ops, g, sa, st);
+                return 1;
+            }
         }
         const size_t bytes = VolSmem<P, T>::bytes(visc);
         if (visc) {

@@ -1,4 +1,5 @@
-// volume_mx.cuh -- the mixed form's volume kernel for even P (N = 1, 3, 5): the same residual as
+// volume_mx.cuh -- the mixed form's volume kernel for even P (N = 1, 3, 5) and the Chandrashekhar
+// volume flux (the other volume fluxes take k_volume<P, float>): the same residual as
 // k_volume (calc_cell_ho_inv_residual, calc_cell_ho_dif_residual, calc_cell_lo_inv_residual, the
 // blend of calc_rhs and the register update; dgsem/plens.cc:3153-3583, 3753-3775, 4353-4400), with
 // every per-block input staged in shared memory by TMA bulk copies. For even P each cell's P^3
@@ -160,71 +161,38 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>())
             for (int i = 0; i < P; ++i)
 #pragma unroll
                 for (int v = 0; v < 5; ++v) acc[i][v] = 0.0f;
-            if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) {
-                // unnormalised directions, per-node logarithms; the diagonal term only at the two
-                // end nodes (D_ii = 0 at interior GLL nodes)
+            // Chandrashekhar (the only volume flux this kernel is launched for): unnormalised
+            // directions, per-node logarithms; the diagonal term only at the two end nodes
+            // (D_ii = 0 at interior GLL nodes)
 #pragma unroll
-                for (int i = 0; i < P; ++i) {
-                    const int ni = line_node<P>(dir, la, lb, i);
-                    float qi[10];
+            for (int i = 0; i < P; ++i) {
+                const int ni = line_node<P>(dir, la, lb, i);
+                float qi[10];
 #pragma unroll
-                    for (int k = 0; k < 10; ++k) qi[k] = Qa[k * P3 + ni];
-                    const float ji[3] = {Jt[(dir * 3) * NB + ni], Jt[(dir * 3 + 1) * NB + ni], Jt[(dir * 3 + 2) * NB + ni]};
-                    if (i == 0 || i == N) {
-                        float F[5];
-                        chandrashekhar_same_f32(qi, ji, gf, F);
-                        const float dd = opD2<float>(ops, i * P + i);
+                for (int k = 0; k < 10; ++k) qi[k] = Qa[k * P3 + ni];
+                const float ji[3] = {Jt[(dir * 3) * NB + ni], Jt[(dir * 3 + 1) * NB + ni], Jt[(dir * 3 + 2) * NB + ni]};
+                if (i == 0 || i == N) {
+                    float F[5];
+                    chandrashekhar_same_f32(qi, ji, gf, F);
+                    const float dd = opD2<float>(ops, i * P + i);
 #pragma unroll
-                        for (int v = 0; v < 5; ++v) acc[i][v] += dd * F[v];
-                    }
-#pragma unroll
-                    for (int m = i + 1; m < P; ++m) {
-                        const int nm = line_node<P>(dir, la, lb, m);
-                        float qm[10];
-#pragma unroll
-                        for (int k = 0; k < 10; ++k) qm[k] = Qa[k * P3 + nm];
-                        const float nv[3] = {ji[0] + Jt[(dir * 3) * NB + nm], ji[1] + Jt[(dir * 3 + 1) * NB + nm],
-                                             ji[2] + Jt[(dir * 3 + 2) * NB + nm]};
-                        float F[5];
-                        chandrashekhar_pair_f32(qi, qm, nv, hg, F);
-                        const float di = opD<float>(ops, i * P + m), dm = opD<float>(ops, m * P + i);
-#pragma unroll
-                        for (int v = 0; v < 5; ++v) {
-                            acc[i][v] += di * F[v];
-                            acc[m][v] += dm * F[v];
-                        }
-                    }
+                    for (int v = 0; v < 5; ++v) acc[i][v] += dd * F[v];
                 }
-            } else {
-                // other volume fluxes: the reference's normalised form
 #pragma unroll
-                for (int i = 0; i < P; ++i) {
-                    const int ni = line_node<P>(dir, la, lb, i);
-                    float qi[7];
+                for (int m = i + 1; m < P; ++m) {
+                    const int nm = line_node<P>(dir, la, lb, m);
+                    float qm[10];
 #pragma unroll
-                    for (int k = 0; k < 7; ++k) qi[k] = Qa[k * P3 + ni];
-                    const float ci[5] = {Ca[ni], Ca[NB + ni], Ca[2 * NB + ni], Ca[3 * NB + ni], Ca[4 * NB + ni]};
+                    for (int k = 0; k < 10; ++k) qm[k] = Qa[k * P3 + nm];
+                    const float nv[3] = {ji[0] + Jt[(dir * 3) * NB + nm], ji[1] + Jt[(dir * 3 + 1) * NB + nm],
+                                         ji[2] + Jt[(dir * 3 + 2) * NB + nm]};
+                    float F[5];
+                    chandrashekhar_pair_f32(qi, qm, nv, hg, F);
+                    const float di = opD<float>(ops, i * P + m), dm = opD<float>(ops, m * P + i);
 #pragma unroll
-                    for (int m = i; m < P; ++m) {
-                        const int nm = line_node<P>(dir, la, lb, m);
-                        float qm[7];
-#pragma unroll
-                        for (int k = 0; k < 7; ++k) qm[k] = Qa[k * P3 + nm];
-                        const float cm[5] = {Ca[nm], Ca[NB + nm], Ca[2 * NB + nm], Ca[3 * NB + nm], Ca[4 * NB + nm]};
-                        float nv[3];
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) nv[d] = 0.5f * (Jt[(dir * 3 + d) * NB + ni] + Jt[(dir * 3 + d) * NB + nm]);
-                        float nn = sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
-                        const float dn[3] = {__fdividef(nv[0], nn), __fdividef(nv[1], nn), __fdividef(nv[2], nn)};
-                        float F[5];
-                        if (g.ivf == PLENS_IVF_KENNEDY_GRUBER) kennedy_gruber_vol(qi, qm, get_e(ci), get_e(cm), dn, gm, F);
-                        else ismail_roe_vol(ci, cm, dn, gm, F);
-                        const float di = opD2<float>(ops, i * P + m) * nn, dm = opD2<float>(ops, m * P + i) * nn;
-#pragma unroll
-                        for (int v = 0; v < 5; ++v) {
-                            acc[i][v] += di * F[v];
-                            if (m != i) acc[m][v] += dm * F[v];
-                        }
+                    for (int v = 0; v < 5; ++v) {
+                        acc[i][v] += di * F[v];
+                        acc[m][v] += dm * F[v];
                     }
                 }
             }
