@@ -31,22 +31,28 @@ struct Launch {
         k_blender<P, T><<<grid_cells(dv.nc), CB::THREADS, 0, st>>>(dv, ops, g, bp);
         return 1;
     }
+    template <bool HLLC>
+    static void surface_inv_mx(const Dev& dv, const GasP& g, double* out, cudaStream_t st)
+    {
+        static int blocks = 0;
+        if (!blocks) {
+            int dev = 0, nsm = 0, occ = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_surface_inv_mx<P, HLLC>, 128, 0);
+            blocks = (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
+        }
+        const int64_t need = (dv.n_mx + 127) / 128;
+        k_surface_inv_mx<P, HLLC><<<(int)(need < blocks ? need : blocks), 128, 0, st>>>(dv, g, out);
+    }
     static int surface(int stage, const Dev& dv, const GasP& g, double* out, cudaStream_t st)
     {
         const int64_t n = dv.ntask * P * P;
         const int grid = (int)((n + 127) / 128);
         if constexpr (sizeof(T) == 4) {
             if (stage == 2) {  // persistent, software-pipelined
-                static int blocks = 0;
-                if (!blocks) {
-                    int dev = 0, nsm = 0, occ = 0;
-                    cudaGetDevice(&dev);
-                    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_surface_inv_mx<P>, 128, 0);
-                    blocks = (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
-                }
-                const int64_t need = (dv.n_mx + 127) / 128;
-                k_surface_inv_mx<P><<<(int)(need < blocks ? need : blocks), 128, 0, st>>>(dv, g, out);
+                if (g.isf == PLENS_ISF_HLLC) surface_inv_mx<true>(dv, g, out, st);
+                else surface_inv_mx<false>(dv, g, out, st);
                 return 1;
             }
         }

@@ -45,8 +45,10 @@ __device__ __forceinline__ void face_states(const Dev& dv, const FaceItem& it, f
     if (it.gdn >= 0) load_state<float>(dv, it.gdn, c2);
 }
 
-template <int P>
-__global__ void __launch_bounds__(128, 4) k_surface_inv_mx(Dev dv, GasP g, double* out)
+// HLLC: the configurations' surface flux, instantiated on its own so that the kernel carries no
+// code of the other schemes (the alpha-blended ones read alpha; HLLC does not)
+template <int P, bool HLLC>
+__global__ void __launch_bounds__(128, HLLC ? 5 : 4) k_surface_inv_mx(Dev dv, GasP g, double* out)
 {
     constexpr int P2 = P * P;
     Scalars* s = dv.sc;
@@ -54,8 +56,8 @@ __global__ void __launch_bounds__(128, 4) k_surface_inv_mx(Dev dv, GasP g, doubl
     const int64_t total = dv.n_mx;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const float gm = f64_to_f32(g.gamma);
-    const bool blended = g.isf == PLENS_ISF_CHANDRASHEKHAR || g.isf == PLENS_ISF_RUSANOV_HLLC ||
-                         g.isf == PLENS_ISF_RUSANOV_AUSM_PLUS_UP;
+    const bool blended = !HLLC && (g.isf == PLENS_ISF_CHANDRASHEKHAR || g.isf == PLENS_ISF_RUSANOV_HLLC ||
+                                   g.isf == PLENS_ISF_RUSANOV_AUSM_PLUS_UP);
     float* o = as_real<float>(out);
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     FaceItem cur = face_item(dv, i, total);
@@ -85,7 +87,8 @@ __global__ void __launch_bounds__(128, 4) k_surface_inv_mx(Dev dv, GasP g, doubl
             bc_ghost<float>(2, dv, g, b, cs, av, cur.n, dv.ft_xyz + (int64_t)cur.idx * 3, s->time, -1, c2, ag);
         }
         float fl[5];
-        inv_surf_flux_mx(cs, c2, cur.n, gm, g.isf, fb, fl);
+        if constexpr (HLLC) hllc_n_f32(cs, c2, cur.n, gm, fl);
+        else inv_surf_flux_mx(cs, c2, cur.n, gm, g.isf, fb, fl);
         const int64_t slot = cur.slot, slot_nb = cur.slot_nb;
 #pragma unroll
         for (int v = 0; v < 5; ++v) o[v * dv.nslot + slot] = fl[v];
