@@ -151,6 +151,11 @@ struct plens_ctx {
     LaunchTable tab{};
     double N15 = 1;
     cudaStream_t stream = nullptr;
+    // the troubled-cell indicator (blender or learned sensor, then the smoothing) runs on a side
+    // stream, forked from and joined back into `stream` within each RHS: it overlaps the face
+    // kernels, which do not read alpha unless the surface flux blends with it
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int64_t launches = 0;
     std::string err = "no error";
     std::vector<void*> allocs;
@@ -251,19 +256,33 @@ int refresh_image(plens_ctx* c)
 int launch_rhs(plens_ctx* c, const StageArgs& sa)
 {
     cudaStream_t st = c->stream;
+    // fork: the indicator chain on the side stream (it reads the state and writes only alpha,
+    // alpha_d, the troubled-cell list and the positivity status)
+    cudaError_t e = cudaEventRecord(c->ev_fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+    if (e != cudaSuccess) return cuda_fail(c, e, "indicator fork");
+    if (c->learned) {
+        c->launches += mlp_sensor_launch(c->mlp, c->dv, c->ops, c->gas, c->bp, c->P, c->side);
+    } else {
+        c->launches += c->tab.blender(c->dv, c->ops, c->gas, c->bp, c->side);
+        k_alpha_smooth<<<(unsigned)((c->nc + 127) / 128), 128, 0, c->side>>>(c->dv, c->bp);
+        ++c->launches;
+    }
+    e = cudaEventRecord(c->ev_join, c->side);
+    if (e != cudaSuccess) return cuda_fail(c, e, "indicator join");
     if (c->viscous) {
         c->launches += c->tab.surface(1, c->dv, c->gas, c->dv.sf, st);
         c->launches += c->tab.aux(c->dv, c->ops, c->gas, st);
+        c->launches += c->tab.surface(3, c->dv, c->gas, c->dv.sf3, st);
     }
-    if (c->learned) {
-        c->launches += mlp_sensor_launch(c->mlp, c->dv, c->ops, c->gas, c->bp, c->P, st);
-    } else {
-        c->launches += c->tab.blender(c->dv, c->ops, c->gas, c->bp, st);
-        k_alpha_smooth<<<(unsigned)((c->nc + 127) / 128), 128, 0, st>>>(c->dv, c->bp);
-        ++c->launches;
-    }
-    if (c->viscous) c->launches += c->tab.surface(3, c->dv, c->gas, c->dv.sf3, st);
-    c->launches += c->tab.surface(2, c->dv, c->gas, c->dv.sf, st);
+    // the alpha-blended surface fluxes wait for alpha; the others run beside the indicator
+    const int isf = c->prm.inv_surf_flux;
+    const bool blended = isf == PLENS_ISF_CHANDRASHEKHAR || isf == PLENS_ISF_RUSANOV_HLLC ||
+                         isf == PLENS_ISF_RUSANOV_AUSM_PLUS_UP;
+    if (!blended) c->launches += c->tab.surface(2, c->dv, c->gas, c->dv.sf, st);
+    e = cudaStreamWaitEvent(st, c->ev_join, 0);
+    if (e != cudaSuccess) return cuda_fail(c, e, "indicator join");
+    if (blended) c->launches += c->tab.surface(2, c->dv, c->gas, c->dv.sf, st);
     if (c->timing) {
         if (c->ev_used == c->ev_pool.size()) {
             cudaEvent_t a, b;
@@ -444,6 +463,9 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
     c->bp.do_filter = prm->do_filtering;
 
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     const int64_t nd = c->nd, nc = c->nc, nt = c->ntask;
     Dev& d = c->dv;
     d.nc = nc;
@@ -660,7 +682,11 @@ int plens_gpu_destroy(plens_ctx* c)
     if (c->snap_ready) cudaEventDestroy(c->snap_ready);
     if (c->snap_done) cudaEventDestroy(c->snap_done);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->side) cudaStreamSynchronize(c->side);
     for (void* p : c->allocs) cudaFree(p);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return 0;
