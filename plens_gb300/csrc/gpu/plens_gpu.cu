@@ -156,6 +156,12 @@ struct plens_ctx {
     // kernels, which do not read alpha unless the surface flux blends with it
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the start of a step (stable time step, rho E and state snapshots) runs on a third stream
+    // beside stage 1's indicator and face kernels; stage 1's volume kernel, the first to need dt
+    // or to write the state, joins it
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_step_fork = nullptr, ev_step_join = nullptr;
+    bool step_join_pending = false;
     int64_t launches = 0;
     std::string err = "no error";
     std::vector<void*> allocs;
@@ -281,7 +287,9 @@ int launch_rhs(plens_ctx* c, const StageArgs& sa)
                          isf == PLENS_ISF_RUSANOV_AUSM_PLUS_UP;
     if (!blended) c->launches += c->tab.surface(2, c->dv, c->gas, c->dv.sf, st);
     e = cudaStreamWaitEvent(st, c->ev_join, 0);
+    if (e == cudaSuccess && c->step_join_pending) e = cudaStreamWaitEvent(st, c->ev_step_join, 0);
     if (e != cudaSuccess) return cuda_fail(c, e, "indicator join");
+    c->step_join_pending = false;
     if (blended) c->launches += c->tab.surface(2, c->dv, c->gas, c->dv.sf, st);
     if (c->timing) {
         if (c->ev_used == c->ev_pool.size()) {
@@ -300,15 +308,16 @@ int launch_rhs(plens_ctx* c, const StageArgs& sa)
     return check_launch(c, "rhs kernels");
 }
 
-int launch_time_step(plens_ctx* c)
+int launch_time_step(plens_ctx* c, cudaStream_t st = nullptr)
 {
-    k_courant<<<1, 1, 0, c->stream>>>(c->dv, c->prm.expr_courant);
+    if (!st) st = c->stream;
+    k_courant<<<1, 1, 0, st>>>(c->dv, c->prm.expr_courant);
     c->launches += 1;
-    c->launches += c->tab.time_step(c->dv, c->gas, c->N15, c->N, c->stream);
-    k_dt_finalize<<<1, 1, 0, c->stream>>>(c->dv);
+    c->launches += c->tab.time_step(c->dv, c->gas, c->N15, c->N, st);
+    k_dt_finalize<<<1, 1, 0, st>>>(c->dv);
     c->launches += 1;
     if (c->dv.dt_loc) {
-        k_local_dt<<<(unsigned)((c->nc + 255) / 256), 256, 0, c->stream>>>(
+        k_local_dt<<<(unsigned)((c->nc + 255) / 256), 256, 0, st>>>(
             c->dv, c->prm.limit_local_step, c->prm.local_start_time, c->prm.local_nbr_factor,
             c->prm.local_global_factor);
         c->launches += 1;
@@ -332,16 +341,24 @@ int launch_step(plens_ctx* c, double end_time, bool judge = true)
     cudaStream_t st = c->stream;
     k_step_begin<<<1, 1, 0, st>>>(c->dv, end_time);
     c->launches += 1;
+    // fork the start of the step: it reads the state, which nothing writes before stage 1's
+    // volume kernel, and writes dt, the snapshots and the clock copy, which nothing reads before it
+    cudaError_t e = cudaEventRecord(c->ev_step_fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->aux, c->ev_step_fork, 0);
+    if (e != cudaSuccess) return cuda_fail(c, e, "step fork");
     if (c->rhoE_old) {
-        k_save_rhoE<<<(unsigned)std::min<int64_t>((c->nd + 255) / 256, 152 * 8), 256, 0, st>>>(c->dv, c->rhoE_old);
+        k_save_rhoE<<<(unsigned)std::min<int64_t>((c->nd + 255) / 256, 152 * 8), 256, 0, c->aux>>>(c->dv, c->rhoE_old);
         c->launches += 1;
     }
     if (c->learned) {
-        k_snapshot<<<(unsigned)std::min<int64_t>((5 * c->nd / 2 + 255) / 256, 152 * 16), 256, 0, st>>>(c->dv);
+        k_snapshot<<<(unsigned)std::min<int64_t>((5 * c->nd / 2 + 255) / 256, 152 * 16), 256, 0, c->aux>>>(c->dv);
         c->launches += 1;
         if (judge) c->launches += mlp_step_begin(c->mlp, c->dv, c->prm.judge_every, st);
     }
-    if (int r = launch_time_step(c)) return r;
+    if (int r = launch_time_step(c, c->aux)) return r;
+    e = cudaEventRecord(c->ev_step_join, c->aux);
+    if (e != cudaSuccess) return cuda_fail(c, e, "step join");
+    c->step_join_pending = true;
     if (c->prm.rk_order == 4) {
         // registers rotate: stage s writes dt*R into R[w]; R1 = previous, R0 = previous-previous
         int w = 0, r1 = -1, r0 = -1;
@@ -466,6 +483,9 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
     CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->ev_step_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_step_join, cudaEventDisableTiming));
     const int64_t nd = c->nd, nc = c->nc, nt = c->ntask;
     Dev& d = c->dv;
     d.nc = nc;
@@ -683,10 +703,14 @@ int plens_gpu_destroy(plens_ctx* c)
     if (c->snap_done) cudaEventDestroy(c->snap_done);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->side) cudaStreamSynchronize(c->side);
+    if (c->aux) cudaStreamSynchronize(c->aux);
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_step_fork) cudaEventDestroy(c->ev_step_fork);
+    if (c->ev_step_join) cudaEventDestroy(c->ev_step_join);
     if (c->side) cudaStreamDestroy(c->side);
+    if (c->aux) cudaStreamDestroy(c->aux);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return 0;
