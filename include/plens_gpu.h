@@ -198,7 +198,9 @@ int plens_gpu_set_kernel_timing(plens_ctx* ctx, int enable);
 int plens_gpu_kernel_timing(plens_ctx* ctx, double* volume_ms, int64_t* volume_launches);
 
 /* ----------------------------------------------------------------- state I/O
- * Replaces the g_cvars / gcrk_cvars buffer copies of PLENS::update (dgsem/plens.cc:4487-4514). */
+ * Replaces the g_cvars / gcrk_cvars buffer copies of PLENS::update (dgsem/plens.cc:4487-4514).
+ * A page-locked (pinned, mapped) host buffer is read or written by the GPU through its device
+ * mapping in one pass; any other host buffer goes through cudaMemcpy. */
 int plens_gpu_set_state(plens_ctx* ctx, const double* U /* [5][ndof] */);
 int plens_gpu_get_state(plens_ctx* ctx, double* U /* [5][ndof] */);
 /* Simulation clock kept on the device (PLENS::cur_time, PLENS::n_time_steps). */

@@ -42,7 +42,6 @@ static __global__ void k_dt_finalize(Dev dv)
     s->dt = (dt > (s->end_time - s->time)) ? s->end_time - s->time : dt;
 }
 
-// mixed form: the FP32 image of the state after the host or a restore changed U
 // FP32 rounding of an FP64 array (the mixed form's metric images)
 static __global__ void k_round_f32(const double* __restrict__ in, float* __restrict__ out, int64_t n)
 {
@@ -50,6 +49,26 @@ static __global__ void k_round_f32(const double* __restrict__ in, float* __restr
         out[i] = f64_to_f32(in[i]);
 }
 
+// The state from (and to) a page-locked host buffer read through its device mapping: one pass
+// over the host link that also writes the mixed form's FP32 image.
+static __global__ void k_state_in(Dev dv, const double* __restrict__ src)
+{
+    const int64_t n = 5 * dv.nd;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double u = src[i];
+        dv.U[i] = u;
+        if (dv.Uf) dv.Uf[i] = f64_to_f32(u);
+    }
+}
+
+static __global__ void k_state_out(Dev dv, double* __restrict__ dst)
+{
+    const int64_t n = 5 * dv.nd;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = dv.U[i];
+}
+
+// mixed form: the FP32 image of the state after the host or a restore changed U
 static __global__ void k_state_image(Dev dv)
 {
     const int64_t n = 5 * dv.nd;

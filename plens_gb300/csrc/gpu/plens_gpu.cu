@@ -248,6 +248,20 @@ int check_launch(plens_ctx* c, const char* what)
     return 0;
 }
 
+// The device address of a host buffer that kernels may read and write directly: page-locked and
+// mapped memory (cudaHostAlloc, cudaHostRegister; torch's pinned tensors), whose attributes name a
+// device pointer. Null for anything else (pageable memory, device memory, errors), which then
+// goes through the copy engines.
+void* mapped_device_ptr(const void* host)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();  // clear the error of an unknown pointer
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
+}
+
 // mixed form: the FP32 image of the state after U was written outside the update kernels
 int refresh_image(plens_ctx* c)
 {
@@ -723,8 +737,17 @@ void* plens_gpu_stream(const plens_ctx* c) { return c ? (void*)c->stream : nullp
 int plens_gpu_set_state(plens_ctx* c, const double* U)
 {
     if (!c || !U || !c->dv.U) return PLENS_GPU_E_INVALID;
-    CK(cudaMemcpyAsync(c->dv.U, U, sizeof(double) * 5 * c->nd, cudaMemcpyHostToDevice, c->stream));
-    if (int r = refresh_image(c)) return r;
+    const int64_t n = 5 * c->nd;
+    if (const double* mapped = static_cast<const double*>(mapped_device_ptr(U))) {
+        // page-locked host buffer: the SMs read it over the host link and write the state and its
+        // FP32 image in one pass (faster than a copy engine, and no second pass for the image)
+        k_state_in<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, c->stream>>>(c->dv, mapped);
+        c->launches += 1;
+        if (int r = check_launch(c, "state in")) return r;
+    } else {
+        CK(cudaMemcpyAsync(c->dv.U, U, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        if (int r = refresh_image(c)) return r;
+    }
     CK(cudaStreamSynchronize(c->stream));
     return 0;
 }
@@ -732,7 +755,14 @@ int plens_gpu_set_state(plens_ctx* c, const double* U)
 int plens_gpu_get_state(plens_ctx* c, double* U)
 {
     if (!c || !U || !c->dv.U) return PLENS_GPU_E_INVALID;
-    CK(cudaMemcpyAsync(U, c->dv.U, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToHost, c->stream));
+    const int64_t n = 5 * c->nd;
+    if (double* mapped = static_cast<double*>(mapped_device_ptr(U))) {
+        k_state_out<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, c->stream>>>(c->dv, mapped);
+        c->launches += 1;
+        if (int r = check_launch(c, "state out")) return r;
+    } else {
+        CK(cudaMemcpyAsync(U, c->dv.U, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    }
     CK(cudaStreamSynchronize(c->stream));
     return 0;
 }
