@@ -205,3 +205,11 @@ def test_geometry_setup_switch(tmp_path):
     assert b"needs the GPU library's geometry function" in L.plens_case_last_error()
     with pytest.raises(PlensError, match="cell 0 has a non-positive Jacobian"):
         Case(mirrored_box_prm(tmp_path, "host"), 2, base_dir=str(tmp_path))
+
+
+def test_setup_phase_times():
+    """The setup reports its phase times (mesh, geometry, topology, initial condition)."""
+    c = make(configs.dmr(nx=12, ny=4))
+    t = c.setup_times()
+    assert list(t) == ["mesh", "geometry", "topology", "initial_condition"]
+    assert all(v >= 0 for v in t.values()) and t["geometry"] > 0
