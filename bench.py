@@ -5,9 +5,12 @@ synthetic inputs generated in code (IC, BCs and seeded noise of the configuratio
 one RK4(3)5[3R+]N time step (5 RHS evaluations + register updates + the CFL min-reduction).
 DOF-stage updates/s = DoFs * 5 * steps / time.
 
-Forms measured: the plain FP64 form and the FP32 form (flux differencing in FP32, registers in
-FP64) with the learned troubled-cell sensor when trained weights are available
-(plens_gb300/sensor_weights.bin), else with the modal sensor; `value` is the headline form.
+Forms measured: the plain FP64 form; the mixed form (flux differencing, surface fluxes and the
+indicator in FP32; the state, the metric terms, the 1/det J scaling, the three RK registers and
+their accumulation in FP64) with the modal troubled-cell sensor and with the learned one (trained
+weights in plens_gb300/sensor_weights.bin); and, for comparison, the mixed_r32 form (FP32 RK
+registers and FP32 metric images) with the learned sensor. `value` is the mixed form with the
+learned sensor (the modal one when no weights are shipped).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -34,11 +37,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "DOF-stage updates/s: FP32+learned sensor vs FP64 plain, GB300, rho L1 err<=1e-4"
 UNIT = "DOF-stage/s"
-# Algorithmic bytes of one DOF-stage through the volume kernel. FP64 form: U r/w 80 + two RK
-# registers read 80 + one written 40 + Ja, detJ 80 = 280. Mixed form: the registers hold dt*R, an
-# FP32 result, in FP32 (2x20 read + 20 written) and the kernel reads the FP32 rounding of Ja and
-# detJ (40): U r/w 80 + 40 + 20 + 40 = 180.
-BYTES_PER_DOF_STAGE = {"plain": 280, "modal": 180, "learned": 180}
+# Algorithmic bytes of one DOF-stage through the volume kernel. FP64 and mixed forms: U r/w 80 +
+# two RK registers read 80 + one written 40 + Ja and detJ (the mixed form: Ja and 1/detJ) 80 = 280.
+# mixed_r32 form: the registers hold dt*R in FP32 (2x20 read + 20 written) and the kernel reads the
+# FP32 images of Ja and detJ (40): U r/w 80 + 40 + 20 + 40 = 180.
+BYTES_PER_DOF_STAGE = {"plain": 280, "modal": 280, "learned": 280, "learned_r32": 180}
 WORKLOAD = "double Mach reflection 240x60x1 cells, N=3, 921600 DoFs, RK4(3)5[3R+]N, HLLC + Chandrashekhar"
 
 
@@ -243,13 +246,14 @@ def _form_case(workload: str, precision: str, sensor: str, cache: dict | None = 
     if workload not in cache:
         cache[workload] = configs.make_case(_spec(workload, "fp64", "modal"))
     case = cache[workload]
-    case.params.precision = 1 if precision == "mixed" else 0
+    from plens_gb300.api import PRECISIONS
+    case.params.precision = PRECISIONS[precision]
     case.params.sensor = 1 if sensor == "learned" else 0
     return case
 
 
 def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_index: int, weights=None,
-                 workload: str = "dmr", cache: dict | None = None, tensor_cores: bool = False):
+                 workload: str = "dmr", cache: dict | None = None, tensor_cores: bool = False, e2e: bool = True):
     import torch
 
     from plens_gb300.api import GpuSolver
@@ -288,6 +292,10 @@ def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_in
     stats = g.sensor_stats() if sensor == "learned" else None
     Ug = g.get_state()
 
+    if not e2e:
+        g.close()
+        return {"case": case, "ms": ms, "launches": launches, "vol_ms": vol_ms, "vol_n": vol_n,
+                "clocks": cs.summary(), "stats": stats, "U": Ug}
     # end to end through the C ABI with pinned host buffers: per step the state goes host ->
     # device, one step runs, the new state comes back
     pin_in = torch.empty((5, case.n_dofs), dtype=torch.float64).pin_memory()
@@ -386,7 +394,7 @@ def run_workload_report(args):
     weights = _sensor_weights()
     forms = [("fp64_plain", "fp64", "modal"), ("fp32_modal", "mixed", "modal")]
     if weights is not None:
-        forms.append(("fp32_learned", "mixed", "learned"))
+        forms += [("fp32_learned", "mixed", "learned"), ("fp32_r32_learned", "mixed_r32", "learned")]
     out = {"workload": args.workload, "accuracy_window": wl["note"] if not args.accuracy_steps else f"{acc_steps} steps"}
     states = {}
     windows = [acc_steps] if args.accuracy_steps else wl.get("windows", [acc_steps])
@@ -427,7 +435,7 @@ def run_workload_report(args):
             st["fallback_rate"] = st["fallbacks"] / max(st["judged"] * case.n_cells, 1)
             rec["accuracy_run"]["sensor_stats"] = st
         g.close()
-    for name in ("fp32_modal", "fp32_learned", "fp64_perturbed_1e-12"):
+    for name in ("fp32_modal", "fp32_learned", "fp32_r32_learned", "fp64_perturbed_1e-12"):
         for w in windows:
             if (name, w) in states and ("fp64_plain", w) in states:
                 out[name].setdefault("rel_l1_vs_fp64", {})[f"{w}_steps"] = dict(
@@ -471,6 +479,27 @@ def run_workload_report(args):
     print(json.dumps(out), flush=True)
 
 
+FORMS = {"plain": ("fp64", "modal"), "modal": ("mixed", "modal"), "learned": ("mixed", "learned"),
+         "modal_r32": ("mixed_r32", "modal"), "learned_r32": ("mixed_r32", "learned")}
+
+
+def run_single_form(args):
+    """One form on the double Mach reflection workload: device time per step and the volume
+    kernel's mean launch time (no end-to-end pass, no accuracy comparison)."""
+    import torch
+
+    torch.cuda.set_device(0)
+    prec, sensor = FORMS[args.form]
+    r = measure_form(prec, sensor, args.steps, args.warmup, 0, _sensor_weights() if sensor == "learned" else None,
+                     tensor_cores=args.sensor_tensor_cores, e2e=False)
+    nd = r["case"].n_dofs
+    vol = r["vol_ms"] / max(r["vol_n"], 1)
+    print(json.dumps({"form": args.form, "precision": prec, "sensor": sensor, "steps": args.steps,
+                      "ms_per_step": r["ms"] / args.steps, "dof_stage_per_s": nd * 5 * args.steps / (r["ms"] / 1e3),
+                      "volume_kernel_ms": vol, "gpu_launches": r["launches"], "clocks": r["clocks"],
+                      "sensor_stats": r["stats"]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -484,6 +513,9 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=0, help="override the accuracy window (steps)")
     ap.add_argument("--sensor-tensor-cores", action="store_true",
                     help="the learned sensor's hidden layers on the tensor cores (tcgen05, 3xTF32)")
+    ap.add_argument("--form", default="", choices=["", "plain", "modal", "learned", "modal_r32", "learned_r32"],
+                    help="time one form only and print its numbers (a short run for profiling) instead of "
+                         "the benchmark line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -491,6 +523,9 @@ def main():
         return
     if args.workload:
         run_workload_report(args)
+        return
+    if args.form:
+        run_single_form(args)
         return
 
     import torch
@@ -517,13 +552,16 @@ def main():
     learned = (measure_form("mixed", "learned", args.steps, args.warmup, device.index, weights, cache=cache,
                             tensor_cores=args.sensor_tensor_cores)
                if weights is not None else None)
+    learned_r32 = (measure_form("mixed_r32", "learned", args.steps, args.warmup, device.index, weights, cache=cache,
+                                tensor_cores=args.sensor_tensor_cores)
+                   if weights is not None else None)
     fast = learned if learned is not None else modal
     fast_sensor = "learned" if learned is not None else "modal"
 
     case = plain["case"]
     nd = case.n_dofs
     job = {}
-    for k, r in (("plain", plain), ("modal", modal), ("learned", learned)):
+    for k, r in (("plain", plain), ("modal", modal), ("learned", learned), ("learned_r32", learned_r32)):
         if r is None:
             continue
         t = max_over_ranks(r["ms"] / 1e3, device)
@@ -536,8 +574,9 @@ def main():
     # accuracy of the FP32 forms against the plain FP64 form after the same steps
     job["modal"]["rel_l1_vs_fp64_plain"] = dict(zip(("rho", "momentum", "rhoE"), _rel_l1(modal["U"], plain["U"])))
     if learned is not None:
-        job["learned"]["rel_l1_vs_fp64_plain"] = dict(zip(("rho", "momentum", "rhoE"), _rel_l1(learned["U"], plain["U"])))
-        job["learned"]["sensor_stats"] = learned["stats"]
+        for k, r in (("learned", learned), ("learned_r32", learned_r32)):
+            job[k]["rel_l1_vs_fp64_plain"] = dict(zip(("rho", "momentum", "rhoE"), _rel_l1(r["U"], plain["U"])))
+            job[k]["sensor_stats"] = r["stats"]
 
     if rank != 0:
         return
@@ -555,7 +594,8 @@ def main():
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 flux differencing + f64 state/registers",
+        "dtype": "f32 flux differencing, surface fluxes, indicator; f64 state, metric terms, 1/detJ scaling, "
+                 "RK registers and their accumulation",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": f"mixed FP32 + {fast_sensor} sensor"
                    + (" (network on tensor cores)" if args.sensor_tensor_cores and learned is not None else ""),
@@ -565,16 +605,18 @@ def main():
             "fp64_plain": job["plain"],
             "fp32_modal_sensor": job["modal"],
             "fp32_learned_sensor": job.get("learned"),
+            "fp32_r32_learned_sensor": dict(job["learned_r32"], dtype="f32 flux differencing, f32 RK registers and "
+                                            "metric images, f64 state") if "learned_r32" in job else None,
             "multiple_headline_over_fp64_plain": hd["value"] / job["plain"]["value"],
         },
         "roofline": {
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_kind": peak_kind, "kernel": f"k_volume_mx (mixed form, {fast_sensor} sensor)",
             "traffic": _traffic_from_profile("k_volume_mx_dmr.md"),
-            "note": "achieved: algorithmic 180 B per DOF-stage (FP64 state r/w, FP32 registers and metric "
-                    "images) x 921600 DoFs per launch / mean CUDA-event "
-                    "launch time of the kernel-timing pass; traffic: ncu DRAM bytes of a stage-1 launch "
-                    "(no RK register read yet), profiles/k_volume_mx_dmr.md",
+            "note": "achieved: algorithmic 280 B per DOF-stage (FP64 state r/w 80, two FP64 registers read "
+                    "80, one written 40, FP64 Ja and 1/detJ 80) x 921600 DoFs per launch / mean CUDA-event "
+                    "launch time of the kernel-timing pass; traffic: ncu DRAM bytes per launch from "
+                    "profiles/k_volume_mx_dmr.md",
         },
         "e2e": {"value": hd["e2e"], "unit": UNIT, "h2d_bytes_per_step": fast["bytes_state"],
                 "d2h_bytes_per_step": fast["bytes_state"]},

@@ -94,7 +94,16 @@ typedef struct plens_expr_insn {
 } plens_expr_insn;
 
 /* ------------------------------------------------------------------- parameters */
-enum plens_precision { PLENS_PRECISION_FP64 = 0, PLENS_PRECISION_MIXED = 1 };
+/* FP64: every operation in FP64 (the reference's arithmetic).
+ * MIXED: the flux differencing, surface fluxes, subcell residual, viscous terms, indicator, CFL
+ *   estimate and network in FP32; the state, the three RK registers and their accumulation, the
+ *   metric terms and Jacobians (stored and read in FP64; FP32 arithmetic uses their rounding), the
+ *   1/det J scaling of the residual, the positivity decision and the conservative face fluxes'
+ *   sums in FP64.
+ * MIXED_R32: as MIXED, but the RK registers hold dt*R in FP32, combined in FP32, and the FP32
+ *   arithmetic reads FP32 images of the metric terms (made once at creation), scaling the residual
+ *   by 1/det J in FP32; only the final state update U + inc is FP64. Fewer bytes per DOF-stage. */
+enum plens_precision { PLENS_PRECISION_FP64 = 0, PLENS_PRECISION_MIXED = 1, PLENS_PRECISION_MIXED_R32 = 2 };
 enum plens_sensor { PLENS_SENSOR_MODAL = 0, PLENS_SENSOR_LEARNED = 1 };
 
 typedef struct plens_params {
@@ -184,7 +193,8 @@ typedef struct plens_ctx plens_ctx;
  * and the BC descriptors, allocates all device buffers. */
 int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* params, plens_ctx** out);
 int plens_gpu_destroy(plens_ctx* ctx);
-/* Message of the last failed call on this context (never NULL). */
+/* Message of the last failed call on this context (never NULL). With ctx = NULL: the message of
+ * the last failed context-free call (plens_gpu_time_step_noalloc) on the calling thread. */
 const char* plens_gpu_last_error(const plens_ctx* ctx);
 /* Number of CUDA kernels this library launched on the context so far. */
 int64_t plens_gpu_kernel_launches(const plens_ctx* ctx);
@@ -222,16 +232,22 @@ int plens_gpu_time_step(plens_ctx* ctx, double* dt_out);
 /* Stable time step of a caller-owned state, allocating nothing. No counterpart in the reference:
  * it is for callers that may not allocate device memory -- a framework that owns all GPU memory
  * through its own pool and forbids libraries from calling cudaMalloc, or a loop that must not
- * allocate while it runs. Same result as plens_gpu_time_step, but on device arrays the caller
- * passes: U [5][ndof], Jinv [9][ndof] and h_min [n_cells] in the layouts of plens_mesh_desc, the
+ * allocate while it runs. Same result as plens_gpu_time_step of an FP64 context (a mixed-precision
+ * context evaluates the step in FP32 and differs by about 1e-6 relative), but on device arrays
+ * the caller passes: U [5][ndof], Jinv [9][ndof] and h_min [n_cells] in the layouts of plens_mesh_desc, the
  * gas of `params`, the Courant number `courant` (capped to 0.9 when >= 1), and dt_out, one
  * double in device memory that receives the step (before any end-time clip). Runs on `stream`
  * (a cudaStream_t, may be NULL) and returns without synchronising.
  * Scratch: the per-cell steps go to a library-owned device array of PLENS_GPU_NOALLOC_MAX_CELLS
  * doubles (2 MiB) that every GPU using the library keeps until the process exits; larger meshes
  * return PLENS_GPU_E_INVALID. All calls share that array: calls that overlap on the GPU race.
- * The first call on each device looks the array up (cudaGetSymbolAddress); make that first call
- * before any stream capture. */
+ * The first call on each device looks the array up (cudaGetSymbolAddress) and keeps its address
+ * for the life of the process; make that first call before any stream capture, and do not call
+ * this entry point after a cudaDeviceReset of that device (the kept address would be stale).
+ * Errors: PLENS_GPU_E_INVALID for bad arguments or a mesh beyond the scratch array, and
+ * PLENS_GPU_E_CUDA for a failed launch or a CUDA error already pending from earlier work (which
+ * is reported, not cleared); plens_gpu_last_error(NULL) gives the message of the last failed
+ * call on the calling thread. */
 #define PLENS_GPU_NOALLOC_MAX_CELLS (1 << 18)
 int plens_gpu_time_step_noalloc(const double* U, const double* Jinv, const double* h_min, int64_t n_cells,
                                 int32_t degree, const plens_params* params, double courant, double* dt_out,
@@ -255,6 +271,13 @@ int plens_gpu_synchronize(plens_ctx* ctx);
  * QGauss(N+1) quadrature. Either output may be NULL; asking for a norm that was not requested at
  * setup gives PLENS_GPU_E_INVALID. Synchronising. */
 int plens_gpu_error_norms(plens_ctx* ctx, double* ss_error, double* conv_error);
+
+/* The compacted troubled-cell list of the last RHS (mixed forms with the Chandrashekhar volume
+ * flux at odd N, where the subcell residual runs over it): the cells with alpha > 0 in increasing
+ * index order -- the cells calc_cell_lo_inv_residual (dgsem/plens.cc:3469-3583) runs on -- built
+ * without atomics, so the same on every run. cells ([n_cells], may be NULL) receives the list,
+ * *count its length. PLENS_GPU_E_INVALID for a context without a list. Synchronising. */
+int plens_gpu_troubled_cells(plens_ctx* ctx, int32_t* cells, int64_t* count);
 
 /* Per-cell scalars of the last RHS: PLENS::gcrk_alpha, gcrk_alpha_d, loc_time_steps. */
 int plens_gpu_get_cell_scalars(plens_ctx* ctx, double* alpha, double* alpha_d, double* dt_cell);
@@ -296,7 +319,7 @@ int plens_gpu_set_sensor_weights(plens_ctx* ctx, const float* params /* [PLENS_M
  * indicator, summed over the judged steps (a cell whose alpha error exceeds the judge tolerance
  * keeps the plain indicator until the next judged step; a step redone after a positivity
  * failure counts every cell); the max per-cell alpha error seen; and the number of cells the
- * subcell kernel ran on in the last RHS. */
+ * subcell kernel ran on in the last RHS (the length of the compacted troubled-cell list). */
 int plens_gpu_sensor_stats(plens_ctx* ctx, int64_t* judged, int64_t* fallbacks,
                            double* max_alpha_err, int64_t* lo_cells_last);
 /* Training pairs of the current state: x [n_cells][64] FP32, the sensor input (nodal rho*p

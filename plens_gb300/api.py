@@ -10,6 +10,7 @@ library's message; a positivity failure raises ``PositivityError`` carrying the 
 from __future__ import annotations
 
 import ctypes as C
+import re
 from pathlib import Path
 
 import numpy as np
@@ -25,6 +26,8 @@ PLENS_GPU_E_TIMEOUT = 4
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+PRECISION_MIXED_R32 = 2
+PRECISIONS = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED, "mixed_r32": PRECISION_MIXED_R32}
 SENSOR_MODAL = 0
 SENSOR_LEARNED = 1
 MLP_N_PARAMS = 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1
@@ -89,6 +92,7 @@ class MeshDesc(C.Structure):
 
 _host = None
 _gpu = None
+_GEOMETRY_GPU = re.compile(r"^\s*set\s+geometry\s+setup\s*=\s*gpu\s*(#.*)?$", re.MULTILINE | re.IGNORECASE)
 
 
 def _load(name: str) -> C.CDLL:
@@ -165,6 +169,7 @@ def gpu_lib() -> C.CDLL:
         L.plens_gpu_get_cell_scalars.argtypes = [vp, vp, vp, vp]
         L.plens_gpu_error_norms.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.plens_gpu_get_avars.argtypes = [vp, vp]
+        L.plens_gpu_troubled_cells.argtypes = [vp, vp, C.POINTER(i64)]
         L.plens_gpu_first_bad_dof.argtypes = [vp, C.POINTER(i64)]
         L.plens_gpu_set_sensor_weights.argtypes = [vp, vp]
         L.plens_gpu_sensor_stats.argtypes = [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(dbl), C.POINTER(i64)]
@@ -198,7 +203,9 @@ class Case:
         L = host_lib()
         h = C.c_void_p()
         geometry = None
-        if (LIB_DIR / "libplens_gpu.so").exists():
+        # the CUDA library is loaded only when the prm asks for the GPU geometry job, so that a
+        # host-only setup (and a CPU-only process) never maps it
+        if _GEOMETRY_GPU.search(prm_text):
             geometry = C.cast(gpu_lib().plens_gpu_setup_geometry, C.c_void_p)
         rc = L.plens_case_create_ex(prm_text.encode(), str(base_dir).encode(), mapping_degree,
                                     fe_degree, geometry, C.byref(h))
@@ -420,6 +427,13 @@ class GpuSolver:
         dt = np.empty(self.n_cells)
         self._check(self.L.plens_gpu_get_cell_scalars(self.h, _ptr(a), _ptr(ad), _ptr(dt)), "cell_scalars")
         return a, ad, dt
+
+    def troubled_cells(self) -> np.ndarray:
+        """The compacted troubled-cell list of the last RHS (cells with alpha > 0, ascending)."""
+        cells = np.empty(self.n_cells, dtype=np.int32)
+        n = C.c_int64()
+        self._check(self.L.plens_gpu_troubled_cells(self.h, _ptr(cells), C.byref(n)), "troubled_cells")
+        return cells[:n.value].copy()
 
     def avars(self) -> np.ndarray:
         A = np.empty((9, self.n_dofs))

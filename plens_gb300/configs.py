@@ -128,9 +128,11 @@ end
 
 
 def dmr(nx: int = 240, ny: int = 60, precision="fp64", sensor="modal", end_time=0.2, noise=1e-6,
-        degree=3, z_bc="periodic"):
+        degree=3, z_bc="periodic", nz: int = 1, plens_2d: bool = False):
     """Double Mach reflection. z_bc: "periodic" (the benchmark configuration) or "symmetry" (the
-    z boundaries of the reference's own input, study1/dmr/scripts/base_input.prm:43-48)."""
+    z boundaries of the reference's own input, study1/dmr/scripts/base_input.prm:43-48); nz cells
+    of 0.0167 each across z; plens_2d: the reference's PLENS_2D switch (the z-momentum RHS set to
+    zero, dgsem/plens.cc:3772-3774), which keeps the flow two-dimensional."""
     if z_bc == "periodic":
         z_bcs = """    subsection bid5
         set type = periodic
@@ -160,8 +162,8 @@ subsection mesh
     subsection builtin
         set generator = box
         set lower corner = 0 0 0
-        set upper corner = 4 1 0.0167
-        set subdivisions = {nx} {ny} 1
+        set upper corner = 4 1 {0.0167 * nz!r}
+        set subdivisions = {nx} {ny} {nz}
         set boundary ids = 1 3 1 2 5 6
         set split -y side at x = 0.16666666666666666
         set split boundary id = 4
@@ -219,7 +221,7 @@ end
 subsection data output
     set write frequency = 1000000
 end
-""" + _gb300(precision, sensor)
+""" + _gb300(precision, sensor, "    set 2d = true\n" if plens_2d else "")
     return prm, {}, degree
 
 
@@ -236,7 +238,11 @@ def _local_stepping(local: dict | None) -> str:
 
 
 def cylinder(n_radial: int = 160, n_azimuthal: int = 128, precision="fp64", sensor="modal",
-             end_time=1e9, courant=0.3, mapping_degree_note=True, local: dict | None = None):
+             end_time=1e9, courant=0.3, mapping_degree_note=True, local: dict | None = None,
+             wall_bc="uniform temp wall", inflow_bc="uniform inflow", z_bc="periodic"):
+    """Laminar Mach-8 cylinder. The boundary types can be swapped for the BC parity cases:
+    wall_bc "uniform temp wall" | "insulated wall", inflow_bc "uniform inflow" | "ZPG inflow",
+    z_bc "periodic" | "symmetry" | "empty"."""
     gamma, Rgas, Tinf, Mach, Re, D = 1.4, 287.0, 200.0, 8.0, 1e5, 2.0
     pinf = 100.0
     rho = pinf / (Rgas * Tinf)
@@ -245,6 +251,28 @@ def cylinder(n_radial: int = 160, n_azimuthal: int = 128, precision="fp64", sens
     T0, S = 273.0, 111.0
     mu0 = mu_inf / ((Tinf / T0) ** 1.5 * (T0 + S) / (Tinf + S))
     MW = 8.314462618 / Rgas
+    if z_bc == "periodic":
+        z_bcs = """    subsection bid4
+        set type = periodic
+        set periodic direction = 2
+        set periodic orientation = left
+        set other surface boundary id = 5
+    end
+    subsection bid5
+        set type = periodic
+        set periodic direction = 2
+        set periodic orientation = right
+        set other surface boundary id = 4
+    end"""
+    elif z_bc in ("symmetry", "empty"):
+        z_bcs = f"""    subsection bid4
+        set type = {z_bc}
+    end
+    subsection bid5
+        set type = {z_bc}
+    end"""
+    else:
+        raise ValueError(z_bc)
     prm = f"""
 subsection mesh
     set type = curved
@@ -292,12 +320,12 @@ subsection IC
 end
 subsection BCs
     subsection bid1
-        set type = uniform temp wall
+        set type = {wall_bc}
         set prescribed T = 300
         set prescribed velocity = 0 0 0
     end
     subsection bid2
-        set type = uniform inflow
+        set type = {inflow_bc}
         set prescribed p = {pinf!r}
         set prescribed T = {Tinf!r}
         set prescribed velocity = {u!r} 0 0
@@ -306,18 +334,7 @@ subsection BCs
         set type = outflow
         set prescribed p = {pinf!r}
     end
-    subsection bid4
-        set type = periodic
-        set periodic direction = 2
-        set periodic orientation = left
-        set other surface boundary id = 5
-    end
-    subsection bid5
-        set type = periodic
-        set periodic direction = 2
-        set periodic orientation = right
-        set other surface boundary id = 4
-    end
+{z_bcs}
 end
 subsection blender parameters
     set variable = pxrho

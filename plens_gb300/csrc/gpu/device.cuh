@@ -90,10 +90,13 @@ struct Dev {
     int64_t nc, nd, ntask, nslot;
     // mesh
     const double *detJ, *Ja, *Jinv, *h_min, *center;
-    // mixed form: the FP32 rounding (f64_to_f32) of detJ, Ja and Jinv, made once on the device at
-    // context creation -- the value every FP32 consumer of the FP64 metric terms would compute
-    // (null in the FP64 form)
+    // MIXED_R32 form: the FP32 rounding (f64_to_f32) of detJ, Ja and Jinv, made once on the
+    // device at context creation -- the value every FP32 consumer of the FP64 metric terms would
+    // compute (null in the FP64 and MIXED forms, whose FP32 consumers round the FP64 arrays)
     const float *detJf, *Jaf, *Jinvf;
+    // MIXED form: 1/detJ in FP64 (made once at creation), by which the volume kernels scale the
+    // FP32 residual sums in FP64 (null otherwise)
+    const double* invJ;
     const int32_t *cell_nbr;
     const uint8_t *cell_wall;
     const int32_t *ft_cell, *ft_face, *ft_nbr_cell, *ft_nbr_face, *ft_bc, *ft_nbr_fdof;
@@ -124,8 +127,14 @@ struct Dev {
     double* tvstat;    // [3][nc] filter statistics of the modal indicator
     double *sf, *sf3;  // surface terms [5][nslot]
     double* avars;     // [9][nd]
-    int32_t* lo_list;  // compacted troubled-cell list
+    // compacted troubled-cell list of the mixed forms (ordered by cell index): lo_list[pos] =
+    // cell, lo_pos[cell] = pos or -1, *lo_count cells; lo_blk: troubled cells per smoothing block;
+    // lo_buf [5][nd]: the subcell residual sums of the listed cells at position * P^3 + node
+    int32_t* lo_list;
     int32_t* lo_count;
+    int32_t* lo_pos;
+    int32_t* lo_blk;
+    float* lo_buf;
     // local time stepping (null unless requested): per-cell stable step, and what multiplies
     // each cell's RHS (loc_time_steps)
     double *dt_cell, *dt_loc;
@@ -191,12 +200,14 @@ template <class T> __device__ __forceinline__ double to_f64(T x)
     if constexpr (sizeof(T) == 8) return x; else return f32_to_f64(x);
 }
 
-// A metric term in the arithmetic type: the FP64 array (plain form) or its FP32 rounding (mixed
-// form), which equals to_real<float> of the FP64 value bit for bit.
+// A metric term in the arithmetic type: the FP64 array (plain form), or its FP32 rounding --
+// read from the FP32 image where one exists (MIXED_R32), else rounded from the FP64 array on the
+// integer pipes (MIXED); the two are equal bit for bit.
 template <class T>
 __device__ __forceinline__ T metric(const double* f64, const float* f32, int64_t i)
 {
-    if constexpr (sizeof(T) == 8) return f64[i]; else return f32[i];
+    if constexpr (sizeof(T) == 8) return f64[i];
+    else return f32 ? f32[i] : f64_to_f32(f64[i]);
 }
 
 // One node's state in the arithmetic type: the FP64 state (plain form) or its FP32 image (mixed).
@@ -210,9 +221,9 @@ __device__ __forceinline__ void load_state(const Dev& dv, int64_t dof, T c[5])
     }
 }
 
-// The face-value and auxiliary-variable buffers are intermediates of one RHS, and the RK4
-// registers hold dt*R, an FP32 result in the mixed form: the mixed form stores all of them in
-// FP32 inside the FP64-sized allocations (exactly, for the registers).
+// The face-value and auxiliary-variable buffers are intermediates of one RHS: the mixed forms
+// store them in FP32 inside the FP64-sized allocations. The MIXED_R32 form stores its RK4
+// registers (dt*R, an FP32 result there) in FP32 the same way; the MIXED form keeps them in FP64.
 template <class T> __device__ __forceinline__ T* as_real(double* p) { return reinterpret_cast<T*>(p); }
 template <class T> __device__ __forceinline__ const T* as_real(const double* p) { return reinterpret_cast<const T*>(p); }
 

@@ -1,6 +1,7 @@
 // kernels.cuh -- the hot-path kernels, templated on P = N+1 and on the arithmetic type T
-// (double: plain path; float: mixed path, with state, metrics, registers and the RK update kept
-// in double). One block handles CellBlock<P>::CPB cells with one thread per GLL node.
+// (double: plain path; float: the mixed forms, whose state is FP64 and whose RK registers, metric
+// terms and register accumulation are FP64 in the MIXED form and FP32 in the MIXED_R32 form, see
+// plens_precision). One block handles CellBlock<P>::CPB cells with one thread per GLL node.
 #pragma once
 
 #include "device.cuh"
@@ -16,8 +17,8 @@ struct StageArgs {
     const double* R0;
     const double* R1;
     double c0, c1, c2;
-    float fc0, fc1, fc2;  // the same coefficients for the mixed form's FP32 register combination
-    int lo_from_list;  // 1: the subcell residual runs only on cells of the compacted list
+    float fc0, fc1, fc2;  // the same coefficients for the MIXED_R32 form's FP32 register combination
+    int reg64;  // mixed forms: 1 (MIXED) FP64 registers, FP64 1/detJ scaling and accumulation; 0 (MIXED_R32) FP32
 };
 
 // ------------------------------------------------------------------------ step bookkeeping
@@ -47,6 +48,13 @@ static __global__ void k_round_f32(const double* __restrict__ in, float* __restr
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = f64_to_f32(in[i]);
+}
+
+// FP64 reciprocal of an FP64 array (the MIXED form's 1/detJ)
+static __global__ void k_reciprocal(const double* __restrict__ in, double* __restrict__ out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = 1.0 / in[i];
 }
 
 // The state from (and to) a page-locked host buffer read through its device mapping: one pass
@@ -459,8 +467,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_blender(Dev dv, Ops o
     }
 }
 
-// the rest of the smoothing of one cell after the neighbour max: TV filter, alpha, alpha_d and the
-// troubled-cell list
+// the rest of the smoothing of one cell after the neighbour max: TV filter, alpha, alpha_d
 __device__ __forceinline__ void smooth_finish(const Dev& dv, const BlendP& bp, Scalars* s, int64_t c, double& a)
 {
     if (bp.do_filter && !(a > bp.amin)) {
@@ -470,30 +477,36 @@ __device__ __forceinline__ void smooth_finish(const Dev& dv, const BlendP& bp, S
     dv.alpha[c] = a;
     const double* x = dv.center + 3 * c;
     dv.alpha_d[c] = (eval_expr(dv, bp.expr_vis, x[0], x[1], x[2], s->time) > 0) ? ((1.0 < a / bp.amax) ? 1.0 : a / bp.amax) : 0.0;
-    if (dv.lo_list && a > 0) {  // compacted troubled-cell list (learned-sensor contexts)
-        const int k = atomicAdd(dv.lo_count, 1);
-        dv.lo_list[k] = (int32_t)c;
-    }
 }
 
+constexpr int kSmoothThreads = 128;  // cells per block of k_alpha_smooth and k_lo_list
+
 // neighbour smoothing over interior faces against the pre-smoothing values, optional TV filter
-// and alpha_d (dgsem/plens.cc:2926-2961, blender_calculator.cc:196-259)
-static __global__ void k_alpha_smooth(Dev dv, BlendP bp)
+// and alpha_d (dgsem/plens.cc:2926-2961, blender_calculator.cc:196-259); kSmoothThreads cells per
+// block. Mixed forms: each block also counts its troubled cells (alpha > 0) for the compacted list.
+static __global__ void __launch_bounds__(kSmoothThreads) k_alpha_smooth(Dev dv, BlendP bp)
 {
     Scalars* s = dv.sc;
     if (!s->active) return;
     if (bp.gate && !s->sensor_fallback) return;
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (c >= dv.nc) return;
-    double a = dv.alpha_raw[c];
+    bool troubled = false;
+    if (c < dv.nc) {
+        double a = dv.alpha_raw[c];
 #pragma unroll
-    for (int f = 0; f < 6; ++f) {
-        const int32_t nb = dv.cell_nbr[6 * c + f];
-        if (nb < 0) continue;
-        const double h = 0.5 * dv.alpha_raw[nb];
-        a = (h > a) ? h : a;
+        for (int f = 0; f < 6; ++f) {
+            const int32_t nb = dv.cell_nbr[6 * c + f];
+            if (nb < 0) continue;
+            const double h = 0.5 * dv.alpha_raw[nb];
+            a = (h > a) ? h : a;
+        }
+        smooth_finish(dv, bp, s, c, a);
+        troubled = a > 0;
     }
-    smooth_finish(dv, bp, s, c, a);
+    if (dv.lo_blk) {
+        const int n = __syncthreads_count(troubled ? 1 : 0);
+        if (threadIdx.x == 0) dv.lo_blk[blockIdx.x] = n;
+    }
 }
 
 // --------------------------------------------------------------------------- BC ghosts
@@ -1093,6 +1106,8 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
     // ---- phase B: HO inviscid = volume + surface, scaled by 1/(-detJ)
     const int ti[3] = {node % P, (node / P) % P, node / P2};
     const T detJt = valid ? metric<T>(dv.detJ, dv.detJf, dof) : T(1);
+    // MIXED form: the residual's parts stay unscaled FP32 sums, scaled by 1/detJ in FP64 below
+    const bool u64 = sizeof(T) == 4 && sa.reg64;
     T ho[5] = {0, 0, 0, 0, 0};
     if (valid) {
 #pragma unroll
@@ -1123,9 +1138,12 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                 }
             }
         }
-        const T js = fdiv(T(1), T(-1) * detJt);
+        // the MIXED form scales the FP32 sums by 1/detJ in FP64 in phase D
+        if (!u64) {
+            const T js = fdiv(T(1), T(-1) * detJt);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) ho[v] *= js;
+            for (int v = 0; v < 5; ++v) ho[v] *= js;
+        }
     }
 
     // ---- viscous HO residual: nodal viscous fluxes along each contravariant direction
@@ -1192,9 +1210,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                     }
                 }
             }
-            const T js = fdiv(T(1), T(1) * detJt);
+            if (!u64) {
+                const T js = fdiv(T(1), T(1) * detJt);
 #pragma unroll
-            for (int v = 0; v < 5; ++v) hd[v] *= js;
+                for (int v = 0; v < 5; ++v) hd[v] *= js;
+            }
         }
     }
 
@@ -1279,15 +1299,59 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
         __syncthreads();
         if (do_lo) {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) lo[v] = fdiv(Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node], -detJt);
+            for (int v = 0; v < 5; ++v) {
+                const T sum = Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node];
+                lo[v] = u64 ? sum : fdiv(sum, -detJt);
+            }
         }
     }
     if (!valid) return;
 
     // ---- phase D: blend, then either store the residual or advance the RK registers
     if constexpr (sizeof(T) == 4) {
-        // mixed form: blend and register combination in FP32 (the residual is an FP32 result,
-        // and so is dt*R, which the registers hold in FP32), the state accumulated in FP64
+        if (u64) {
+            // MIXED form: the blend of the unscaled FP32 sums, R = (-1/detJ) (alpha lo + (1 - alpha)
+            // ho - (1 - alpha_d) hd), scaled in FP64; dt*R, the registers and their combination
+            // (update_rk4, dgsem/plens.cc:4353-4400) in FP64
+            const double nij = -dv.invJ[dof];
+            const float ad = VISC ? f64_to_f32(dv.alpha_d[cell]) : 0.0f;
+            double Ru[5];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                float r = alpha_t * lo[v] + (1.0f - alpha_t) * ho[v];
+                if (VISC) r -= (1.0f - ad) * hd[v];
+                Ru[v] = f32_to_f64(r);
+            }
+            if (g.plens_2d) Ru[3] = 0.0;
+            if (sa.mode == 0) {
+#pragma unroll
+                for (int v = 0; v < 5; ++v) sa.Rout[v * dv.nd + dof] = Ru[v] * nij;
+                return;
+            }
+            const double sc = nij * rhs_step(dv, cell);  // -dt/detJ
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                const double Rs = Ru[v] * sc;
+                const int64_t k = v * dv.nd + dof;
+                const double u = dv.U[k];
+                double un;
+                if (sa.mode == 1) {
+                    un = __fma_rn(sa.c2, Rs, u);  // the chain of the TMA-staged kernel
+                    if (sa.stage >= 2) un = __fma_rn(sa.c1, sa.R1[k], un);
+                    if (sa.stage >= 3) un = __fma_rn(sa.c0, sa.R0[k], un);
+                    sa.Rw[k] = Rs;
+                } else {
+                    if (sa.stage == 1) un = u + Rs;
+                    else if (sa.stage == 2) un = 0.75 * dv.U0[k] + 0.25 * u + 0.25 * Rs;
+                    else un = 1.0 / 3 * dv.U0[k] + 2.0 / 3 * u + 2.0 / 3 * Rs;
+                }
+                dv.U[k] = un;
+                dv.Uf[k] = f64_to_f32(un);
+            }
+            return;
+        }
+        // MIXED_R32 form: blend and register combination in FP32 (the residual is an FP32
+        // result, and so is dt*R, which the registers hold in FP32), the state accumulated in FP64
         float R[5];
         const float ad = VISC ? f64_to_f32(dv.alpha_d[cell]) : 0.0f;
 #pragma unroll

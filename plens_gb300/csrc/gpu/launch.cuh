@@ -3,6 +3,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "subcell_mx.cuh"
 #include "surface_mx.cuh"
 #include "volume_mx.cuh"
 
@@ -16,6 +17,10 @@ struct LaunchTable {
     int (*aux)(const Dev&, const Ops&, const GasP&, cudaStream_t) = nullptr;
     int (*volume)(bool visc, const Dev&, const Ops&, const GasP&, const StageArgs&, cudaStream_t) = nullptr;
     int (*time_step)(const Dev&, const GasP&, double N15, int N, cudaStream_t) = nullptr;
+    // the subcell residual over the compacted troubled-cell list, where the volume kernel takes it
+    // from there (the TMA-staged mixed kernel); 0 launches otherwise
+    bool (*uses_lo_list)(const GasP&) = nullptr;
+    int (*subcell)(const Dev&, const Ops&, const GasP&, cudaStream_t) = nullptr;
 };
 
 LaunchTable table_fp64(int P);
@@ -72,17 +77,17 @@ struct Launch {
         k_aux<P, T><<<grid_cells(dv.nc), CB::THREADS, bytes, st>>>(dv, ops, g);
         return 1;
     }
-    template <bool VISC>
+    template <bool VISC, bool R64>
     static void volume_mx(const Dev& dv, const Ops& ops, const GasP& g, const StageArgs& sa, cudaStream_t st)
     {
         if constexpr (P % 2 == 0) {
-            const size_t bytes = MxSmem<P, VISC>::bytes;
+            const size_t bytes = MxSmem<P, VISC, R64>::bytes;
             static bool attr = false;
             if (!attr) {
-                cudaFuncSetAttribute(k_volume_mx<P, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+                cudaFuncSetAttribute(k_volume_mx<P, VISC, R64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
                 attr = true;
             }
-            k_volume_mx<P, VISC><<<grid_cells(dv.nc), CB::THREADS, bytes, st>>>(dv, ops, g, sa);
+            k_volume_mx<P, VISC, R64><<<grid_cells(dv.nc), CB::THREADS, bytes, st>>>(dv, ops, g, sa);
         }
     }
     static int volume(bool visc, const Dev& dv, const Ops& ops, const GasP& g, const StageArgs& sa, cudaStream_t st)
@@ -91,8 +96,13 @@ struct Launch {
         // TMA-staged kernel; the other volume fluxes take the generic kernel
         if constexpr (sizeof(T) == 4 && P % 2 == 0) {
             if (g.ivf == PLENS_IVF_CHANDRASHEKHAR) {
-                if (visc) volume_mx<true>(dv, ops, g, sa, st);
-                else volume_mx<false>(dv, ops, g, sa, st);
+                if (sa.reg64) {
+                    if (visc) volume_mx<true, true>(dv, ops, g, sa, st);
+                    else volume_mx<false, true>(dv, ops, g, sa, st);
+                } else {
+                    if (visc) volume_mx<true, false>(dv, ops, g, sa, st);
+                    else volume_mx<false, false>(dv, ops, g, sa, st);
+                }
                 return 1;
             }
         }
@@ -112,6 +122,26 @@ struct Launch {
             }
             k_volume<P, T, false><<<grid_cells(dv.nc), CB::THREADS, bytes, st>>>(dv, ops, g, sa);
         }
+        return 1;
+    }
+    static bool uses_lo_list(const GasP& g)
+    {
+        return sizeof(T) == 4 && P % 2 == 0 && g.ivf == PLENS_IVF_CHANDRASHEKHAR;
+    }
+    static int subcell(const Dev& dv, const Ops& ops, const GasP& g, cudaStream_t st)
+    {
+        if (!uses_lo_list(g)) return 0;
+        // persistent grid: the resident blocks take the listed cells in groups
+        static int blocks = 0;
+        if (!blocks) {
+            int dev = 0, nsm = 0, occ = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_subcell_lo<P>, CB::THREADS, 0);
+            blocks = (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
+        }
+        const int64_t need = (dv.nc + CB::CPB - 1) / CB::CPB;
+        k_subcell_lo<P><<<(int)(need < blocks ? need : blocks), CB::THREADS, 0, st>>>(dv, ops, g);
         return 1;
     }
     static int time_step(const Dev& dv, const GasP& g, double N15, int N, cudaStream_t st)
@@ -134,6 +164,8 @@ struct Launch {
         t.aux = &aux;
         t.volume = &volume;
         t.time_step = &time_step;
+        t.uses_lo_list = &uses_lo_list;
+        t.subcell = &subcell;
         return t;
     }
 };

@@ -346,7 +346,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, (P <= 4 ? 3 : 1)) k_senso
     float* sh = sx + 64 * G;  // [64][G]
     Scalars* s = dv.sc;
     if (!s->active) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *dv.lo_count = 0;  // this stage's troubled-cell list
     if (gated && s->sensor_fallback) return;
     {
         const float4* src = reinterpret_cast<const float4*>(Wt);
@@ -430,7 +429,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, (P <= 4 ? 3 : 1))
     float* sx = st + SC::V;
     Scalars* s = dv.sc;
     if (!s->active) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *dv.lo_count = 0;  // this stage's troubled-cell list
     if (gated && s->sensor_fallback) return;
     const float gm = f64_to_f32(g.gamma);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -740,7 +738,7 @@ int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, con
         b1.mask = nullptr;
         n += launch_blender<P>(dv, ops, g, b1, st, 152 * 2);
     }
-    k_alpha_smooth<<<(unsigned)((dv.nc + 127) / 128), 128, 0, st>>>(dv, b0);
+    k_alpha_smooth<<<(unsigned)((dv.nc + kSmoothThreads - 1) / kSmoothThreads), kSmoothThreads, 0, st>>>(dv, b0);
     return n + 1;
 }
 

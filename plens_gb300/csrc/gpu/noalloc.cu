@@ -15,6 +15,7 @@
 
 #include <cmath>
 #include <mutex>
+#include <string>
 
 #include "device.cuh"
 #include "flux.cuh"
@@ -29,6 +30,15 @@ static __device__ __align__(256) double g_noalloc_cell_dt[PLENS_GPU_NOALLOC_MAX_
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 double* g_scratch[kMaxDevices] = {};
+
+// Message of the last failed call on this thread, read through plens_gpu_last_error(NULL).
+thread_local std::string g_noalloc_err = "no error";
+
+int noalloc_fail(int code, const std::string& msg)
+{
+    g_noalloc_err = "plens_gpu_time_step_noalloc: " + msg;
+    return code;
+}
 
 // Device address of the scratch array on the current device. Host code must not pass
 // g_noalloc_cell_dt itself to a kernel: on the host that name is only a stand-in.
@@ -132,11 +142,19 @@ extern "C" int plens_gpu_time_step_noalloc(const double* U, const double* Jinv, 
                                            int32_t degree, const plens_params* params, double courant, double* dt_out,
                                            void* stream)
 {
-    if (!U || !Jinv || !h_min || !params || !dt_out) return PLENS_GPU_E_INVALID;
-    if (degree < 1 || degree > 5 || n_cells <= 0) return PLENS_GPU_E_INVALID;
-    if (n_cells > PLENS_GPU_NOALLOC_MAX_CELLS) return PLENS_GPU_E_INVALID;  // beyond the scratch array
+    if (!U || !Jinv || !h_min || !params || !dt_out) return noalloc_fail(PLENS_GPU_E_INVALID, "null pointer argument");
+    if (degree < 1 || degree > 5) return noalloc_fail(PLENS_GPU_E_INVALID, "degree must lie in [1,5]");
+    if (n_cells <= 0) return noalloc_fail(PLENS_GPU_E_INVALID, "n_cells must be positive");
+    if (n_cells > PLENS_GPU_NOALLOC_MAX_CELLS)
+        return noalloc_fail(PLENS_GPU_E_INVALID, "n_cells = " + std::to_string(n_cells) + " exceeds the scratch array (" +
+                                                     std::to_string(PLENS_GPU_NOALLOC_MAX_CELLS) + " cells)");
+    // an error left by earlier work is reported as it is (not cleared), so that the launch check
+    // below sees only this call's launches
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+        return noalloc_fail(PLENS_GPU_E_CUDA, std::string("a CUDA error is pending from earlier work: ") + cudaGetErrorString(pending));
     double* scratch = nullptr;
-    if (int r = scratch_on_current_device(&scratch)) return r;
+    if (scratch_on_current_device(&scratch)) return noalloc_fail(PLENS_GPU_E_CUDA, "scratch array address lookup failed");
     NoallocGas g;
     g.gamma = params->gamma;
     g.R = params->R;
@@ -154,5 +172,13 @@ extern "C" int plens_gpu_time_step_noalloc(const double* U, const double* Jinv, 
     const int64_t blocks = (n_cells + cpb - 1) / cpb;
     k_cell_dt_noalloc<<<(unsigned)blocks, 256, 0, st>>>(U, Jinv, h_min, n_cells, g, co, scratch);
     k_global_dt_noalloc<<<1, 1024, 0, st>>>(scratch, n_cells, dt_out);
-    return cudaGetLastError() == cudaSuccess ? PLENS_GPU_OK : PLENS_GPU_E_CUDA;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return noalloc_fail(PLENS_GPU_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return PLENS_GPU_OK;
+}
+
+// plens_gpu_last_error(NULL): the message of the last failed context-free call on this thread
+extern "C" __attribute__((visibility("hidden"))) const char* plens_gpu_noalloc_last_error_message()
+{
+    return g_noalloc_err.c_str();
 }

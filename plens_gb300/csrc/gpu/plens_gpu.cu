@@ -143,6 +143,7 @@ struct plens_ctx {
     int P = 0, N = 0;
     int64_t nc = 0, nd = 0, ntask = 0, nslot = 0;
     bool viscous = false, mixed = false, learned = false;
+    bool reg64 = false;  // MIXED form: FP64 RK registers, metric terms read in FP64
     plens_params prm{};
     Dev dv{};
     Ops ops{};
@@ -285,7 +286,11 @@ int launch_rhs(plens_ctx* c, const StageArgs& sa)
         c->launches += mlp_sensor_launch(c->mlp, c->dv, c->ops, c->gas, c->bp, c->P, c->side);
     } else {
         c->launches += c->tab.blender(c->dv, c->ops, c->gas, c->bp, c->side);
-        k_alpha_smooth<<<(unsigned)((c->nc + 127) / 128), 128, 0, c->side>>>(c->dv, c->bp);
+        k_alpha_smooth<<<(unsigned)((c->nc + kSmoothThreads - 1) / kSmoothThreads), kSmoothThreads, 0, c->side>>>(c->dv, c->bp);
+        ++c->launches;
+    }
+    if (c->dv.lo_blk) {  // the compacted troubled-cell list from the smoothing's block counts
+        k_lo_list<<<(unsigned)((c->nc + kSmoothThreads - 1) / kSmoothThreads), kSmoothThreads, 0, c->side>>>(c->dv);
         ++c->launches;
     }
     e = cudaEventRecord(c->ev_join, c->side);
@@ -305,6 +310,9 @@ int launch_rhs(plens_ctx* c, const StageArgs& sa)
     if (e != cudaSuccess) return cuda_fail(c, e, "indicator join");
     c->step_join_pending = false;
     if (blended) c->launches += c->tab.surface(2, c->dv, c->gas, c->dv.sf, st);
+    // the subcell residual of the listed troubled cells (needs alpha, the list and the stage-2
+    // face fluxes), read by the volume kernel
+    if (c->dv.lo_blk) c->launches += c->tab.subcell(c->dv, c->ops, c->gas, st);
     if (c->timing) {
         if (c->ev_used == c->ev_pool.size()) {
             cudaEvent_t a, b;
@@ -396,6 +404,7 @@ int launch_step(plens_ctx* c, double end_time, bool judge = true)
             sa.fc0 = (float)sa.c0;
             sa.fc1 = (float)sa.c1;
             sa.fc2 = (float)sa.c2;
+            sa.reg64 = c->reg64 ? 1 : 0;
             if (int r = launch_rhs(c, sa)) return r;
             r0 = r1;
             r1 = w;
@@ -408,6 +417,7 @@ int launch_step(plens_ctx* c, double end_time, bool judge = true)
             StageArgs sa{};
             sa.mode = 2;
             sa.stage = s;
+            sa.reg64 = c->reg64 ? 1 : 0;
             if (int r = launch_rhs(c, sa)) return r;
         }
     }
@@ -474,7 +484,11 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
     c->nslot = c->nc * 6 * P2;
     c->prm = *prm;
     c->viscous = !(prm->mu0 < 1e-16);
-    c->mixed = prm->precision == PLENS_PRECISION_MIXED;
+    if (prm->precision != PLENS_PRECISION_FP64 && prm->precision != PLENS_PRECISION_MIXED &&
+        prm->precision != PLENS_PRECISION_MIXED_R32)
+        return fail(c, PLENS_GPU_E_INVALID, "bad precision");
+    c->mixed = prm->precision != PLENS_PRECISION_FP64;
+    c->reg64 = prm->precision == PLENS_PRECISION_MIXED;
     c->learned = prm->sensor == PLENS_SENSOR_LEARNED;
     c->tab = pick_table(c->P, c->mixed);
     if (!c->tab.volume) return fail(c, PLENS_GPU_E_INVALID, "no kernels for this degree");
@@ -613,9 +627,18 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         if ((r = dupload(c, &d.cell_wall, wall.data(), nc))) return r;
     }
     if (c->mixed && (r = dalloc(c, &d.Uf, 5 * nd))) return r;
-    if (c->mixed) {
-        // the FP32 rounding of the metric terms, once (every FP32 consumer reads these instead of
-        // rounding the FP64 arrays itself: the same values)
+    if (c->reg64) {
+        // MIXED form: 1/detJ in FP64, by which the volume kernels scale the FP32 residual sums
+        double* invJ = nullptr;
+        if ((r = dalloc(c, &invJ, nd))) return r;
+        CK(cudaDeviceSynchronize());  // the uploads above ran on the legacy stream
+        k_reciprocal<<<(unsigned)std::min<int64_t>((nd + 255) / 256, 152 * 16), 256, 0, c->stream>>>(d.detJ, invJ, nd);
+        c->launches += 1;
+        if ((r = check_launch(c, "1/detJ"))) return r;
+        d.invJ = invJ;
+    } else if (c->mixed) {
+        // MIXED_R32 form: the FP32 rounding of the metric terms, once (every FP32 consumer reads
+        // these instead of rounding the FP64 arrays itself: the same values)
         float *detJf = nullptr, *Jaf = nullptr, *Jinvf = nullptr;
         if ((r = dalloc(c, &detJf, nd)) || (r = dalloc(c, &Jaf, 9 * nd)) || (r = dalloc(c, &Jinvf, 9 * nd))) return r;
         // the uploads above ran on the legacy stream, which this non-blocking stream does not
@@ -664,8 +687,16 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         if ((r = dalloc(c, &d.dt_cell, nc)) || (r = dalloc(c, &d.dt_loc, nc))) return r;
         CK(cudaMemset(d.dt_loc, 0, sizeof(double) * nc));
     }
+    if (c->mixed && c->tab.uses_lo_list(c->gas)) {
+        // the compacted troubled-cell list and the subcell sums of the listed cells
+        const int64_t nblk = (nc + kSmoothThreads - 1) / kSmoothThreads;
+        if ((r = dalloc(c, &d.lo_list, nc)) || (r = dalloc(c, &d.lo_count, 1)) || (r = dalloc(c, &d.lo_pos, nc)) ||
+            (r = dalloc(c, &d.lo_blk, nblk)) || (r = dalloc(c, &d.lo_buf, 5 * nd)))
+            return r;
+        CK(cudaMemset(d.lo_count, 0, sizeof(int32_t)));
+        CK(cudaMemset(d.lo_pos, 0xff, sizeof(int32_t) * nc));
+    }
     if (c->learned) {
-        if ((r = dalloc(c, &d.lo_list, nc)) || (r = dalloc(c, &d.lo_count, 1))) return r;
         if ((r = mlp_create(c->mlp, nc, c->allocs))) return fail(c, PLENS_GPU_E_CUDA, "mlp buffers");
         c->mlp.tol = prm->judge_alpha_tol;
     }
@@ -730,7 +761,8 @@ int plens_gpu_destroy(plens_ctx* c)
     return 0;
 }
 
-const char* plens_gpu_last_error(const plens_ctx* c) { return c ? c->err.c_str() : "null context"; }
+__attribute__((visibility("hidden"))) const char* plens_gpu_noalloc_last_error_message();  // noalloc.cu
+const char* plens_gpu_last_error(const plens_ctx* c) { return c ? c->err.c_str() : plens_gpu_noalloc_last_error_message(); }
 int64_t plens_gpu_kernel_launches(const plens_ctx* c) { return c ? c->launches : 0; }
 void* plens_gpu_stream(const plens_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
@@ -803,6 +835,7 @@ int plens_gpu_rhs(plens_ctx* c, double* R_out)
     StageArgs sa{};
     sa.mode = 0;
     sa.Rout = c->Rout;
+    sa.reg64 = c->reg64 ? 1 : 0;
     if (int r = launch_rhs(c, sa)) return r;
     if (int r = sync_and_check(c)) return r;
     if (R_out) CK(cudaMemcpy(R_out, c->Rout, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToHost));
@@ -985,6 +1018,18 @@ int plens_gpu_get_cell_scalars(plens_ctx* c, double* alpha, double* alpha_d, dou
         CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
         for (int64_t i = 0; i < c->nc; ++i) dt_cell[i] = h.dt_update;
     }
+    return 0;
+}
+
+int plens_gpu_troubled_cells(plens_ctx* c, int32_t* cells, int64_t* count)
+{
+    if (!c || !count) return PLENS_GPU_E_INVALID;
+    if (!c->dv.lo_pos) return fail(c, PLENS_GPU_E_INVALID, "this context has no compacted troubled-cell list");
+    CK(cudaStreamSynchronize(c->stream));
+    int32_t n = 0;
+    CK(cudaMemcpy(&n, c->dv.lo_count, sizeof(n), cudaMemcpyDeviceToHost));
+    *count = n;
+    if (cells && n > 0) CK(cudaMemcpy(cells, c->dv.lo_list, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
     return 0;
 }
 

@@ -1,0 +1,172 @@
+// subcell_mx.cuh -- the mixed forms' first-order subcell residual over the compacted troubled-cell
+// list: calc_cell_lo_inv_residual (dgsem/plens.cc:3469-3583) for the cells with alpha > 0 only,
+// in a kernel of its own between the inviscid face fluxes and the volume kernel.
+//
+// The list is ordered by cell index and built without atomics: the smoothing kernel counts each
+// block's troubled cells (k_alpha_smooth, 128 cells per block), k_lo_list gives every block its
+// offset (the sum of the counts of the blocks before it) and every troubled cell its rank within
+// the block (warp ballots), so the list and each cell's position lo_pos are the same on every run.
+// k_subcell_lo then runs one thread per GLL node of a listed cell and writes the cell's unscaled
+// subcell sums (the three directions' contributions, before the 1/(-detJ) scaling) to
+// lo_buf[var][position * P^3 + node], which the volume kernel blends in.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace plens_gpu {
+
+// positions of the troubled cells: lo_list[pos] = cell, lo_pos[cell] = pos (-1 if alpha = 0),
+// *lo_count = number of troubled cells
+static __global__ void __launch_bounds__(kSmoothThreads) k_lo_list(Dev dv)
+{
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    __shared__ int s_part[kSmoothThreads / 32];
+    __shared__ int s_off;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int b = blockIdx.x;
+    // offset of this block: the troubled cells of the blocks before it
+    int part = 0;
+    for (int j = tid; j < b; j += kSmoothThreads) part += dv.lo_blk[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) s_part[warp] = part;
+    __syncthreads();
+    if (tid == 0) {
+        int t = 0;
+        for (int w = 0; w < kSmoothThreads / 32; ++w) t += s_part[w];
+        s_off = t;
+    }
+    __syncthreads();
+    const int64_t c = (int64_t)b * kSmoothThreads + tid;
+    // the smoothing kernel's predicate on the stored value (alpha > 0)
+    const bool flag = c < dv.nc && dv.alpha[c] > 0;
+    const unsigned m = __ballot_sync(0xffffffffu, flag);
+    const int rank = __popc(m & ((1u << lane) - 1u));
+    __syncthreads();  // s_part is reused for the warp counts
+    if (lane == 0) s_part[warp] = __popc(m);
+    __syncthreads();
+    int wofs = 0;
+    for (int w = 0; w < warp; ++w) wofs += s_part[w];
+    const int pos = s_off + wofs + rank;
+    if (c < dv.nc) {
+        dv.lo_pos[c] = flag ? pos : -1;
+        if (flag) dv.lo_list[pos] = (int32_t)c;
+    }
+    if (b == (int)gridDim.x - 1 && tid == 0) {
+        int t = s_off;
+        for (int w = 0; w < kSmoothThreads / 32; ++w) t += s_part[w];
+        *dv.lo_count = t;
+    }
+}
+
+// Subcell residual sums of the listed cells, CPB cells per block, one thread per GLL node; line
+// tasks numbered flat over the block's cells (3 P^2 per cell), each running the subcell
+// interfaces of one line. The grid is persistent: blocks take groups of CPB listed cells with a
+// stride, up to the count the list kernel wrote.
+template <int P>
+__global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Ops ops, GasP g)
+{
+    using CB = CellBlock<P>;
+    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1, NB = CPB * P3, NF = CPB * 6 * P2;
+    constexpr int TPC = 3 * P2;
+    __shared__ float sC[5][NB];   // FP32 state image
+    __shared__ float sJ[9][NB];   // FP32 rounding of Ja
+    __shared__ float sSf[5][NF];  // stage-2 face fluxes
+    __shared__ float sAcc[CPB][15][P3];
+    __shared__ float sAl[CPB];
+    __shared__ int32_t sCell[CPB];
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    const int n = *dv.lo_count;
+    const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
+    const float gm = f64_to_f32(g.gamma);
+    for (int grp = blockIdx.x; grp * CPB < n; grp += gridDim.x) {
+        const int p0 = grp * CPB;
+        const int ncb = (n - p0 < CPB) ? n - p0 : CPB;
+        if (tid < CPB) {
+            sCell[tid] = (tid < ncb) ? dv.lo_list[p0 + tid] : -1;
+            sAl[tid] = (tid < ncb) ? f64_to_f32(dv.alpha[dv.lo_list[p0 + tid]]) : 0.0f;
+        }
+        __syncthreads();
+        if (cl < ncb) {
+            const int64_t cell = sCell[cl];
+            const int64_t dof = cell * P3 + node;
+#pragma unroll
+            for (int v = 0; v < 5; ++v) sC[v][cl * P3 + node] = dv.Uf[v * dv.nd + dof];
+#pragma unroll
+            for (int m = 0; m < 9; ++m) sJ[m][cl * P3 + node] = metric<float>(dv.Ja, dv.Jaf, m * dv.nd + dof);
+            for (int sl = node; sl < 6 * P2; sl += P3)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) sSf[v][cl * 6 * P2 + sl] = as_real<float>(dv.sf)[v * dv.nslot + cell * 6 * P2 + sl];
+        }
+        __syncthreads();
+        for (int ft = tid; ft < ncb * TPC; ft += CB::THREADS) {
+            const int tc = ft / TPC, task = ft - tc * TPC;
+            const float at = sAl[tc];
+            const float fb = (at <= 0.0f) ? 0.0f : (at <= 1.0f ? at : 1.0f);  // the cell's alpha as flux blender (plens.cc:3492)
+            const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
+            const int base = tc * P3;
+            float acc[P][5];
+#pragma unroll
+            for (int i = 0; i < P; ++i)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) acc[i][v] = 0.0f;
+            // running subcell normal n_(i-1,i) = Ja_0 + sum_{l<i} sum_m Q_lm Ja_m (metric_terms.cc:106-141)
+            const int n0 = base + line_node<P>(dir, la, lb, 0);
+            float sn[3] = {sJ[dir * 3][n0], sJ[dir * 3 + 1][n0], sJ[dir * 3 + 2][n0]};
+#pragma unroll
+            for (int id = 1; id < P; ++id) {
+#pragma unroll
+                for (int m = 0; m < P; ++m) {
+                    const int nm = base + line_node<P>(dir, la, lb, m);
+                    const float qlm = opQ<float>(ops, (id - 1) * P + m);
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) sn[d] += qlm * sJ[dir * 3 + d][nm];
+                }
+                const int nl = base + line_node<P>(dir, la, lb, id - 1), nr = base + line_node<P>(dir, la, lb, id);
+                const float nn = sqrtf(sn[0] * sn[0] + sn[1] * sn[1] + sn[2] * sn[2]);
+                const float dn[3] = {__fdividef(sn[0], nn), __fdividef(sn[1], nn), __fdividef(sn[2], nn)};
+                const float cL[5] = {sC[0][nl], sC[1][nl], sC[2][nl], sC[3][nl], sC[4][nl]};
+                const float cR[5] = {sC[0][nr], sC[1][nr], sC[2][nr], sC[3][nr], sC[4][nr]};
+                float F[5];
+                inv_surf_flux_mx(cL, cR, dn, gm, g.isf, fb, F);
+                const float wl = __fdividef(nn, opW<float>(ops, id - 1)), wr = __fdividef(nn, opW<float>(ops, id));
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    acc[id - 1][v] += F[v] * wl;
+                    acc[id][v] -= F[v] * wr;
+                }
+            }
+            // cell-face terms at both ends of the line: the stage-2 face flux x |Ja| / w
+            // (contribution sign x flux sign = +1, plens.cc:3544-3575)
+#pragma unroll
+            for (int lr = 0; lr < 2; ++lr) {
+                const int i = lr ? N : 0;
+                const int ni = base + line_node<P>(dir, la, lb, i);
+                const int f = 2 * dir + lr;
+                const int q = la + P * lb;
+                const float j0 = sJ[dir * 3][ni], j1 = sJ[dir * 3 + 1][ni], j2 = sJ[dir * 3 + 2][ni];
+                const float nn = sqrtf(j0 * j0 + j1 * j1 + j2 * j2);
+                const float sw = __fdividef(nn, opW<float>(ops, lr * N));
+#pragma unroll
+                for (int v = 0; v < 5; ++v) acc[i][v] += sSf[v][tc * 6 * P2 + f * P2 + q] * sw;
+            }
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int ni = line_node<P>(dir, la, lb, i);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) sAcc[tc][dir * 5 + v][ni] = acc[i][v];
+            }
+        }
+        __syncthreads();
+        if (cl < ncb) {
+            const int64_t o = (int64_t)(p0 + cl) * P3 + node;
+#pragma unroll
+            for (int v = 0; v < 5; ++v) dv.lo_buf[v * dv.nd + o] = sAcc[cl][v][node] + sAcc[cl][5 + v][node] + sAcc[cl][10 + v][node];
+        }
+        __syncthreads();  // shared arrays are reused by the next group
+    }
+}
+
+}  // namespace plens_gpu

@@ -5,9 +5,20 @@
 // every per-block input staged in shared memory by TMA bulk copies. For even P each cell's P^3
 // values of a variable are a multiple of 16 bytes, so a block's CPB cells are one contiguous,
 // 16-byte aligned chunk per variable: one thread issues the copies, two mbarriers signal them --
-// the FP32 state image and metric images that the flux phase needs first, then the FP64 state,
-// the face values and the RK registers, which arrive while the fluxes are computed.
+// the FP32 state image (and, in the MIXED_R32 form, the FP32 metric images) that the flux phase
+// needs first, then the FP64 state, the face values and the RK registers (and, in the MIXED form,
+// 1/detJ in FP64), which arrive while the fluxes are computed. The subcell residual of the
+// troubled cells comes from k_subcell_lo (subcell_mx.cuh), which runs before this kernel on the
+// compacted troubled-cell list.
+//
+// R64 selects the MIXED form: the metric terms are read in FP64 (each thread rounds its node's
+// nine Ja components for the FP32 fluxes), the residual's FP32 sums are scaled by -dt/detJ in
+// FP64, and the three FP64 RK registers are combined in FP64 (update_rk4, dgsem/plens.cc:
+// 4353-4400). Without R64 (MIXED_R32) the registers hold dt*R in FP32 and the metric terms are
+// read from their FP32 images.
 #pragma once
+
+#include <type_traits>
 
 #include "async.cuh"
 #include "kernels.cuh"
@@ -15,20 +26,28 @@
 namespace plens_gpu {
 
 // Shared-memory layout of one block (bytes), all regions 16-byte aligned.
-template <int P, bool VISC>
+template <int P, bool VISC, bool R64>
 struct MxSmem {
     static constexpr int P2 = P * P, P3 = P2 * P, CPB = CellBlock<P>::CPB, NB = CPB * P3, NF = CPB * 6 * P2;
     static constexpr int NQ = 10;  // rho, 1/rho, v0, v1, v2, p, beta, ln rho, ln beta, |v|^2
+    // the warps past the line tasks (phase A) and whether the MIXED form gives them the FP64
+    // pre-update, which reads the two older registers from global memory (not staged)
+    static constexpr int TPC = 3 * P2;
+    static constexpr int TF = ((CPB * TPC + 31) / 32) * 32 < CellBlock<P>::THREADS ? ((CPB * TPC + 31) / 32) * 32
+                                                                                    : CellBlock<P>::THREADS;
+    static constexpr bool PRE = R64 && TF < CellBlock<P>::THREADS;
+    static constexpr size_t RB = PRE ? 0 : (R64 ? 8 : 4);  // bytes of a staged register value
     static constexpr size_t up16(size_t x) { return (x + 15) / 16 * 16; }
-    // staged inputs: the FP64 state (for the update), its FP32 image (for the fluxes), the FP32
-    // metric images, the FP32 RK registers, FP32 face values and auxiliary variables
+    // staged inputs: the FP64 state (for the update), its FP32 image (for the fluxes), detJ (FP32
+    // image; R64: 1/detJ in FP64), the FP32 metric terms (R64: rounded by the threads from FP64),
+    // the RK registers, FP32 face values and auxiliary variables
     static constexpr size_t oU = 0;                                   // double [5][NB]
     static constexpr size_t oUf = oU + up16(8 * 5 * NB);              // float [5][NB]
-    static constexpr size_t oDet = oUf + up16(4 * 5 * NB);            // float [NB]
-    static constexpr size_t oJ = oDet + up16(4 * NB);                 // float [9][NB]
-    static constexpr size_t oR0 = oJ + up16(4 * 9 * NB);              // float [5][NB]
-    static constexpr size_t oR1 = oR0 + up16(4 * 5 * NB);             // float [5][NB]
-    static constexpr size_t oSf = oR1 + up16(4 * 5 * NB);             // float [5][NF]
+    static constexpr size_t oDet = oUf + up16(4 * 5 * NB);            // float [NB] (R64: double [NB])
+    static constexpr size_t oJ = oDet + up16(RB * NB);                // float [9][NB]
+    static constexpr size_t oR0 = oJ + up16(4 * 9 * NB);              // RB [5][NB]
+    static constexpr size_t oR1 = oR0 + up16(RB * 5 * NB);            // RB [5][NB]
+    static constexpr size_t oSf = oR1 + up16(RB * 5 * NB);            // float [5][NF]
     static constexpr size_t oSf3 = oSf + up16(4 * 5 * NF);            // float [5][NF] (viscous)
     static constexpr size_t oAv = oSf3 + (VISC ? up16(4 * 5 * NF) : 0);  // float [9][NB] (viscous)
     static constexpr size_t oAcc = oAv + (VISC ? up16(4 * 9 * NB) : 0);  // float [CPB][15][P3]
@@ -37,25 +56,27 @@ struct MxSmem {
 };
 
 // Resident blocks per SM the register allocation is sized for: six 128-thread blocks at P = 2, 4
-// (80 registers, the shared-memory limit is also six); two 224-thread blocks at P = 6.
-template <int P>
+// (80 registers; the shared-memory limit is six or more), two 224-thread blocks at P = 6.
+template <int P, bool R64>
 constexpr int vol_mx_min_blocks() { return P == 6 ? 2 : 6; }
 
-template <int P, bool VISC>
-__global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>()) k_volume_mx(Dev dv, Ops ops, GasP g, StageArgs sa)
+template <int P, bool VISC, bool R64>
+__global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R64>()) k_volume_mx(Dev dv, Ops ops, GasP g, StageArgs sa)
 {
     static_assert(P % 2 == 0, "bulk staging needs 16-byte aligned per-cell chunks (even P)");
     using CB = CellBlock<P>;
-    using L = MxSmem<P, VISC>;
+    using L = MxSmem<P, VISC, R64>;
+    using RT = typename std::conditional<R64, double, float>::type;  // register storage type
     constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1, NQ = L::NQ, NB = L::NB, NF = L::NF;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bars[2];
     double* stU = reinterpret_cast<double*>(smem_raw + L::oU);
     float* stUf = reinterpret_cast<float*>(smem_raw + L::oUf);
     float* stDet = reinterpret_cast<float*>(smem_raw + L::oDet);
+    double* stInv = reinterpret_cast<double*>(smem_raw + L::oDet);  // R64: 1/detJ
     float* stJ = reinterpret_cast<float*>(smem_raw + L::oJ);
-    float* stR0 = reinterpret_cast<float*>(smem_raw + L::oR0);
-    float* stR1 = reinterpret_cast<float*>(smem_raw + L::oR1);
+    RT* stR0 = reinterpret_cast<RT*>(smem_raw + L::oR0);
+    RT* stR1 = reinterpret_cast<RT*>(smem_raw + L::oR1);
     float* stSf = reinterpret_cast<float*>(smem_raw + L::oSf);
     float* stSf3 = reinterpret_cast<float*>(smem_raw + L::oSf3);
     float* stAv = reinterpret_cast<float*>(smem_raw + L::oAv);
@@ -77,31 +98,48 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>())
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         const uint32_t bd = (uint32_t)(8 * ncb * P3), bf = (uint32_t)(4 * ncb * 6 * P2), bv = (uint32_t)(4 * ncb * P3);
+        const uint32_t br = R64 ? bd : bv;  // one variable's chunk of a register
         const int64_t d0 = cell0 * P3, f0 = cell0 * 6 * P2;
-        mbar_arrive_expect_tx(&bars[0], bv * (5 + 9 + 1));
+        mbar_arrive_expect_tx(&bars[0], R64 ? bv * 5 : bv * (5 + 9 + 1));
 #pragma unroll
         for (int v = 0; v < 5; ++v) tma_load_1d(stUf + v * NB, dv.Uf + v * dv.nd + d0, bv, &bars[0]);
+        if (!R64) {
 #pragma unroll
-        for (int m = 0; m < 9; ++m) tma_load_1d(stJ + m * NB, dv.Jaf + m * dv.nd + d0, bv, &bars[0]);
-        tma_load_1d(stDet, dv.detJf + d0, bv, &bars[0]);
-        uint32_t late = bd * 5 + bf * 5 + (need_r0 ? bv * 5 : 0) + (need_r1 ? bv * 5 : 0) + (VISC ? bf * 5 + bv * 9 : 0);
+            for (int m = 0; m < 9; ++m) tma_load_1d(stJ + m * NB, dv.Jaf + m * dv.nd + d0, bv, &bars[0]);
+            tma_load_1d(stDet, dv.detJf + d0, bv, &bars[0]);
+        }
+        // (with the FP64 pre-update the idle warp reads the registers itself)
+        const bool st_r0 = need_r0 && !L::PRE, st_r1 = need_r1 && !L::PRE;
+        uint32_t late = bd * 5 + bf * 5 + (st_r0 ? br * 5 : 0) + (st_r1 ? br * 5 : 0) + (VISC ? bf * 5 + bv * 9 : 0) +
+                        (R64 ? bd : 0);
         mbar_arrive_expect_tx(&bars[1], late);
 #pragma unroll
         for (int v = 0; v < 5; ++v) tma_load_1d(stU + v * NB, dv.U + v * dv.nd + d0, bd, &bars[1]);
 #pragma unroll
         for (int v = 0; v < 5; ++v) tma_load_1d(stSf + v * NF, as_real<float>(dv.sf) + v * dv.nslot + f0, bf, &bars[1]);
-        if (need_r0)
+        if (R64) tma_load_1d(stInv, dv.invJ + d0, bd, &bars[1]);
+        if (st_r0)
 #pragma unroll
-            for (int v = 0; v < 5; ++v) tma_load_1d(stR0 + v * NB, as_real<float>(sa.R0) + v * dv.nd + d0, bv, &bars[1]);
-        if (need_r1)
+            for (int v = 0; v < 5; ++v) tma_load_1d(stR0 + v * NB, as_real<RT>(sa.R0) + v * dv.nd + d0, br, &bars[1]);
+        if (st_r1)
 #pragma unroll
-            for (int v = 0; v < 5; ++v) tma_load_1d(stR1 + v * NB, as_real<float>(sa.R1) + v * dv.nd + d0, bv, &bars[1]);
+            for (int v = 0; v < 5; ++v) tma_load_1d(stR1 + v * NB, as_real<RT>(sa.R1) + v * dv.nd + d0, br, &bars[1]);
         if (VISC) {
 #pragma unroll
             for (int v = 0; v < 5; ++v) tma_load_1d(stSf3 + v * NF, as_real<float>(dv.sf3) + v * dv.nslot + f0, bf, &bars[1]);
 #pragma unroll
             for (int m = 0; m < 9; ++m) tma_load_1d(stAv + m * NB, as_real<float>(dv.avars) + m * dv.nd + d0, bv, &bars[1]);
         }
+    }
+    if (R64 && valid) {
+        // the FP32 rounding of this node's FP64 metric terms, for the FP32 fluxes (the loads are in
+        // flight while the first copy group lands; the __syncthreads below publishes them)
+        const int64_t dn = cell * P3 + node;
+        double ja[9];
+#pragma unroll
+        for (int m = 0; m < 9; ++m) ja[m] = dv.Ja[m * dv.nd + dn];
+#pragma unroll
+        for (int m = 0; m < 9; ++m) stJ[m * NB + cl * P3 + node] = f64_to_f32(ja[m]);
     }
     __syncthreads();  // barrier initialisation visible to every thread
     // the block takes one decision: a wait that ran out anywhere ends the block (error status set,
@@ -144,12 +182,35 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>())
 
     bool late_waited = false, late_ok = true;
     // ---- phase A: two-point volume fluxes per line. The block's line tasks are numbered flat,
-    // cell after cell, so the threads past the last task -- whole warps at P = 4 -- issue nothing
-    // here and leave their issue slots to the other blocks.
+    // cell after cell, over the first TF threads (whole warps); the warps past them -- one at
+    // P = 4 -- have no line task. In the MIXED form (an RK4 stage) those warps take the part of the
+    // FP64 register update that does not depend on this stage's residual while the others compute
+    // the fluxes: W = U + c1 R1 + c0 R0 and the node factor -dt/detJ, written over the staged U
+    // and 1/detJ. GB300 issues FP64 at a small fraction of its FP32 rate; done here, that work
+    // overlaps the FP32 flux phase instead of lengthening the update at the end.
+    constexpr int TPC = L::TPC, TF = L::TF;  // line tasks per cell, threads running them
+    const bool pre = L::PRE && sa.mode == 1;
+    if (pre && tid >= TF) {
+        late_ok = mbar_wait0(&bars[1]);
+        late_waited = true;
+        if (late_ok) {
+            const double* R0g = sa.R0 + cell0 * P3;
+            const double* R1g = sa.R1 + cell0 * P3;
+            for (int i = tid - TF; i < ncb * P3; i += CB::THREADS - TF) {
+                stInv[i] = -stInv[i] * rhs_step(dv, cell0 + i / P3);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) {
+                    double w = stU[v * NB + i];
+                    if (sa.stage >= 3) w = __fma_rn(sa.c0, R0g[v * dv.nd + i], w);
+                    if (sa.stage >= 2) w = __fma_rn(sa.c1, R1g[v * dv.nd + i], w);
+                    stU[v * NB + i] = w;
+                }
+            }
+        }
+    }
     {
-        constexpr int TPC = 3 * P2;  // line tasks per cell
         const float hg = __fdividef(0.5f, gm - 1.0f), gf = __fdividef(gm, gm - 1.0f);
-        for (int ft = tid; ft < ncb * TPC; ft += CB::THREADS) {
+        for (int ft = tid; ft < ncb * TPC && tid < TF; ft += TF) {
             const int tc = ft / TPC, task = ft - tc * TPC;
             const float* Qa = sQ + tc * NQ * P3;
             const float* Ca = stUf + tc * P3;
@@ -247,10 +308,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>())
     // ---- phase B: HO inviscid = volume + surface (summed per direction in phase A), scaled by
     // 1/(-detJ)
     const int ti[3] = {node % P, (node / P) % P, node / P2};
-    const float detJ = valid ? stDet[bn] : 1.0f;
+    // R64: the parts of the residual stay unscaled FP32 sums, scaled by -dt/detJ in FP64 in phase D
+    const float detJ = (valid && !R64) ? stDet[bn] : 1.0f;
     float ho[5] = {0, 0, 0, 0, 0};
     if (valid) {
-        const float js = __fdividef(-1.0f, detJ);
+        const float js = R64 ? 1.0f : __fdividef(-1.0f, detJ);
 #pragma unroll
         for (int v = 0; v < 5; ++v) ho[v] = (Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node]) * js;
     }
@@ -306,99 +368,80 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>())
                     }
                 }
             }
-            const float js = __fdividef(1.0f, detJ);
+            if (!R64) {
+                const float js = __fdividef(1.0f, detJ);
 #pragma unroll
-            for (int v = 0; v < 5; ++v) hd[v] *= js;
+                for (int v = 0; v < 5; ++v) hd[v] *= js;
+            }
         }
     }
 
-    // ---- phase C: first-order subcell residual, only where alpha > 0
+    // ---- phase C: first-order subcell residual, only where alpha > 0: the sums k_subcell_lo
+    // wrote for this cell's place in the compacted troubled-cell list
     float lo[5] = {0, 0, 0, 0, 0};
-    bool any_lo = false;
+    if (valid && stored_gt0<float>(alpha)) {
+        const int32_t pos = dv.lo_pos[cell];
+        if (pos >= 0) {
+            const float js = R64 ? 1.0f : __fdividef(-1.0f, detJ);
+            const int64_t o = (int64_t)pos * P3 + node;
 #pragma unroll
-    for (int k = 0; k < CPB; ++k)
-        if (k < ncb && stored_gt0<float>(dv.alpha[cell0 + k])) any_lo = true;
-    if (any_lo) {
-        __syncthreads();
-        const bool do_lo = valid && stored_gt0<float>(alpha);
-        {
-            // line tasks numbered flat over the block's cells, as in phase A
-            constexpr int TPC = 3 * P2;
-            for (int ft = tid; ft < ncb * TPC; ft += CB::THREADS) {
-                const int tc = ft / TPC, task = ft - tc * TPC;
-                const double a_t = dv.alpha[cell0 + tc];
-                if (!stored_gt0<float>(a_t)) continue;
-                const float at = f64_to_f32(a_t);
-                const float fb = (at <= 0.0f) ? 0.0f : (at <= 1.0f ? at : 1.0f);
-                const float* Ca = stUf + tc * P3;
-                const float* Jt = stJ + tc * P3;
-                float* At = sAcc + tc * 15 * P3;
-                const float* sfa = stSf + tc * 6 * P2;
-                const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
-                float acc[P][5];
-#pragma unroll
-                for (int i = 0; i < P; ++i)
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) acc[i][v] = 0.0f;
-                // running subcell normal n_(i-1,i) = Ja_0 + sum_{l<i} sum_m Q_lm Ja_m
-                // (metric_terms.cc:106-141)
-                const int n0 = line_node<P>(dir, la, lb, 0);
-                float sn[3] = {Jt[(dir * 3) * NB + n0], Jt[(dir * 3 + 1) * NB + n0], Jt[(dir * 3 + 2) * NB + n0]};
-#pragma unroll
-                for (int id = 1; id < P; ++id) {
-#pragma unroll
-                    for (int m = 0; m < P; ++m) {
-                        const int nm = line_node<P>(dir, la, lb, m);
-                        const float qlm = opQ<float>(ops, (id - 1) * P + m);
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) sn[d] += qlm * Jt[(dir * 3 + d) * NB + nm];
-                    }
-                    const int nl = line_node<P>(dir, la, lb, id - 1), nr = line_node<P>(dir, la, lb, id);
-                    const float nn = sqrtf(sn[0] * sn[0] + sn[1] * sn[1] + sn[2] * sn[2]);
-                    const float dn[3] = {__fdividef(sn[0], nn), __fdividef(sn[1], nn), __fdividef(sn[2], nn)};
-                    const float cL[5] = {Ca[nl], Ca[NB + nl], Ca[2 * NB + nl], Ca[3 * NB + nl], Ca[4 * NB + nl]};
-                    const float cR[5] = {Ca[nr], Ca[NB + nr], Ca[2 * NB + nr], Ca[3 * NB + nr], Ca[4 * NB + nr]};
-                    float F[5];
-                    inv_surf_flux_mx(cL, cR, dn, gm, g.isf, fb, F);
-                    const float wl = __fdividef(nn, opW<float>(ops, id - 1)), wr = __fdividef(nn, opW<float>(ops, id));
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) {
-                        acc[id - 1][v] += F[v] * wl;
-                        acc[id][v] -= F[v] * wr;
-                    }
-                }
-                // cell-face terms at both ends of the line
-#pragma unroll
-                for (int lr = 0; lr < 2; ++lr) {
-                    const int i = lr ? N : 0;
-                    const int ni = line_node<P>(dir, la, lb, i);
-                    const int f = 2 * dir + lr;
-                    const int q = la + P * lb;
-                    const float j0 = Jt[(dir * 3) * NB + ni], j1 = Jt[(dir * 3 + 1) * NB + ni], j2 = Jt[(dir * 3 + 2) * NB + ni];
-                    const float nn = sqrtf(j0 * j0 + j1 * j1 + j2 * j2);
-                    const float sw = __fdividef(nn, opW<float>(ops, lr * N));  // contrib_sign * flux_sign = +1
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) acc[i][v] += sfa[v * NF + f * P2 + q] * sw;
-                }
-#pragma unroll
-                for (int i = 0; i < P; ++i) {
-                    const int ni = line_node<P>(dir, la, lb, i);
-#pragma unroll
-                    for (int v = 0; v < 5; ++v) At[(dir * 5 + v) * P3 + ni] = acc[i][v];
-                }
-            }
-        }
-        __syncthreads();
-        if (do_lo) {
-            const float js = __fdividef(-1.0f, detJ);
-#pragma unroll
-            for (int v = 0; v < 5; ++v) lo[v] = (Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node]) * js;
+            for (int v = 0; v < 5; ++v) lo[v] = dv.lo_buf[v * dv.nd + o] * js;
         }
     }
     if (!valid) return;
 
-    // ---- phase D: blend and register combination in FP32 (the residual is an FP32 result, and
-    // so is dt*R, which the registers hold in FP32); the state accumulated in FP64
+    if constexpr (R64) {
+        // ---- phase D (MIXED): blend of the unscaled FP32 sums,
+        // R = (-1/detJ) (alpha lo + (1 - alpha) ho - (1 - alpha_d) hd), scaled in FP64; dt*R, the
+        // three registers and their combination in FP64
+        const float ad = VISC ? f64_to_f32(dv.alpha_d[cell]) : 0.0f;
+        double Ru[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            float r = alpha_t * lo[v] + (1.0f - alpha_t) * ho[v];
+            if (VISC) r -= (1.0f - ad) * hd[v];
+            Ru[v] = f32_to_f64(r);
+        }
+        if (g.plens_2d) Ru[3] = 0.0;
+        if (sa.mode == 0) {
+            const double nij = -stInv[bn];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) sa.Rout[v * dv.nd + dof] = Ru[v] * nij;
+            return;
+        }
+        // -dt/detJ: made by the idle warp during phase A when it exists
+        const double sc = pre ? stInv[bn] : -stInv[bn] * rhs_step(dv, cell);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+            const double Rs = Ru[v] * sc;
+            const int64_t k = v * dv.nd + dof;
+            const double u = stU[v * NB + bn];
+            double un;
+            if (sa.mode == 1) {
+                // U + c0 R0 + c1 R1 + c2 Rs as a chain of FP64 multiply-adds (one rounding each);
+                // with the idle warp, stU already holds W = U + c0 R0 + c1 R1
+                if (pre) {
+                    un = __fma_rn(sa.c2, Rs, u);
+                } else {
+                    un = u;
+                    if (sa.stage >= 3) un = __fma_rn(sa.c0, stR0[v * NB + bn], un);
+                    if (sa.stage >= 2) un = __fma_rn(sa.c1, stR1[v * NB + bn], un);
+                    un = __fma_rn(sa.c2, Rs, un);
+                }
+                sa.Rw[k] = Rs;
+            } else {
+                if (sa.stage == 1) un = u + Rs;
+                else if (sa.stage == 2) un = 0.75 * dv.U0[k] + 0.25 * u + 0.25 * Rs;
+                else un = 1.0 / 3 * dv.U0[k] + 2.0 / 3 * u + 2.0 / 3 * Rs;
+            }
+            dv.U[k] = un;
+            dv.Uf[k] = f64_to_f32(un);
+        }
+        return;
+    }
+
+    // ---- phase D (MIXED_R32): blend and register combination in FP32 (the residual is an FP32
+    // result, and so is dt*R, which the registers hold in FP32); the state accumulated in FP64
     float R[5];
     const float ad = VISC ? f64_to_f32(dv.alpha_d[cell]) : 0.0f;
 #pragma unroll
@@ -421,8 +464,8 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P>())
         if (sa.mode == 1) {
             float inc;
             if (sa.stage == 1) inc = sa.fc2 * Rs;
-            else if (sa.stage == 2) inc = sa.fc1 * stR1[v * NB + bn] + sa.fc2 * Rs;
-            else inc = sa.fc0 * stR0[v * NB + bn] + sa.fc1 * stR1[v * NB + bn] + sa.fc2 * Rs;
+            else if (sa.stage == 2) inc = sa.fc1 * (float)stR1[v * NB + bn] + sa.fc2 * Rs;
+            else inc = sa.fc0 * (float)stR0[v * NB + bn] + sa.fc1 * (float)stR1[v * NB + bn] + sa.fc2 * Rs;
             as_real<float>(sa.Rw)[k] = Rs;
             const double un = u + f32_to_f64(inc);
             dv.U[k] = un;

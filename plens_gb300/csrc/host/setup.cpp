@@ -457,7 +457,7 @@ void declare_parameters(ParameterHandler& prm)
     prm.declare_entry("data output/convergence/exact solution", "1");
     // this build: the compile-time switches of the reference as run-time options, precision
     // and the learned sensor
-    prm.declare_entry("GB300/precision", "fp64", "fp64|mixed");
+    prm.declare_entry("GB300/precision", "fp64", "fp64|mixed|mixed_r32");
     prm.declare_entry("GB300/sensor", "modal", "modal|learned");
     prm.declare_entry("GB300/sensor weights file", "");
     prm.declare_entry("GB300/judge every", "25");
@@ -857,8 +857,9 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
         C.output_dir = prm.get("data output/directory");
         C.base_file_name = prm.get("data output/base file name");
         const std::string prec = prm.get("GB300/precision");
-        pr.precision = (prec == "mixed") ? PLENS_PRECISION_MIXED : PLENS_PRECISION_FP64;
-        if (prec != "mixed" && prec != "fp64") throw std::runtime_error("GB300/precision must be fp64|mixed");
+        pr.precision = (prec == "mixed") ? PLENS_PRECISION_MIXED : (prec == "mixed_r32") ? PLENS_PRECISION_MIXED_R32 : PLENS_PRECISION_FP64;
+        if (prec != "mixed" && prec != "mixed_r32" && prec != "fp64")
+            throw std::runtime_error("GB300/precision must be fp64|mixed|mixed_r32");
         const std::string sens = prm.get("GB300/sensor");
         pr.sensor = (sens == "learned") ? PLENS_SENSOR_LEARNED : PLENS_SENSOR_MODAL;
         pr.judge_every = static_cast<int32_t>(prm.get_integer("GB300/judge every"));

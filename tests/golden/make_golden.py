@@ -7,10 +7,14 @@
 - oracle_sod_rhs.npz: a small oracle regression vector (40-cell Sod workload: the state after 15
   RK steps and its RHS), used to check that the oracle computes the same numbers on every host.
 
-Run from the repository root: python tests/golden/make_golden.py
+Run from the repository root:
+    python tests/golden/make_golden.py --reference <path of the reference checkout>
+(or with the PLENS_REFERENCE environment variable naming that path).
 """
+import argparse
 import contextlib
 import io
+import os
 import sys
 from pathlib import Path
 
@@ -18,11 +22,10 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
-REF = Path("/root/reference/utilities")
 
 
-def sod_exact():
-    sys.path.insert(0, str(REF))
+def sod_exact(reference: Path):
+    sys.path.insert(0, str(reference / "utilities"))
     from shockTubeSoln import shockTubeSoln  # noqa: E402  (the reference's utility)
     R = 287.0
     x = np.linspace(0.0, 1.0, 401)
@@ -32,7 +35,13 @@ def sod_exact():
 
 
 def main():
-    x, out = sod_exact()
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--reference", default=os.environ.get("PLENS_REFERENCE"),
+                    help="root of the reference checkout (holds utilities/shockTubeSoln.py)")
+    args = ap.parse_args()
+    if not args.reference:
+        ap.error("give --reference or set PLENS_REFERENCE")
+    x, out = sod_exact(Path(args.reference))
     out = np.asarray(out, dtype=float)  # columns: x, T, p, u, rho
     p, u, rho = out[:, 2], out[:, 3], out[:, 4]
     np.savez(Path(__file__).parent / "sod_exact_t0.2.npz", x=x, rho=rho, u=u, p=p)

@@ -1,7 +1,8 @@
-"""The mixed form (FP32 flux differencing, FP64 state, metrics and RK registers) against the FP64
-oracle, over the kernels it dispatches to: the TMA-staged volume kernel (even P: N = 1, 3, 5;
-inviscid and viscous), the generic one (odd P), every surface and volume flux scheme, RK3 and the
-positivity check.
+"""The mixed forms against the FP64 oracle, over the kernels they dispatch to: the TMA-staged
+volume kernel (even P: N = 1, 3, 5; inviscid and viscous), the generic one (odd P), every surface
+and volume flux scheme, RK3 and the positivity check. "mixed": FP32 flux differencing with the
+state, the metric terms, the 1/det J scaling, the RK registers and their accumulation in FP64;
+"mixed_r32": the same flux arithmetic with FP32 registers and FP32 metric images.
 
 Tolerances: one RHS, max over equations of max|R_mixed - R_oracle| / max|R_oracle| <= 2e-4 (2e-3
 on the 1e-3-clustered curved O-mesh, where the wall-cell residual is a small difference of large
@@ -19,6 +20,7 @@ pytestmark = pytest.mark.gpu
 
 RHS_TOL = 2e-4
 STEPS_TOL = 1e-4
+PRECS = ["mixed", "mixed_r32"]
 
 
 def _state(case64, steps):
@@ -52,20 +54,22 @@ def _steps_err(spec64, specmx, steps=20):
     return rel_l1(g.get_state(), o.get_state()[0])
 
 
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("degree", [1, 2, 3, 4, 5])
-def test_mixed_dmr_degrees(degree):
-    e = _rhs_err(configs.dmr(nx=12, ny=4, degree=degree), configs.dmr(nx=12, ny=4, degree=degree, precision="mixed"))
+def test_mixed_dmr_degrees(degree, prec):
+    e = _rhs_err(configs.dmr(nx=12, ny=4, degree=degree), configs.dmr(nx=12, ny=4, degree=degree, precision=prec))
     print(f"N={degree} rhs err {e:.3e}")
     assert e <= RHS_TOL
-    s = _steps_err(configs.dmr(nx=12, ny=4, degree=degree), configs.dmr(nx=12, ny=4, degree=degree, precision="mixed"))
+    s = _steps_err(configs.dmr(nx=12, ny=4, degree=degree), configs.dmr(nx=12, ny=4, degree=degree, precision=prec))
     print(f"N={degree} 20-step rel L1 {s}")
     assert s.max() <= STEPS_TOL
 
 
-def test_mixed_sod():
-    e = _rhs_err(configs.sod(n=40), configs.sod(n=40, precision="mixed"), steps=10)
+@pytest.mark.parametrize("prec", PRECS)
+def test_mixed_sod(prec):
+    e = _rhs_err(configs.sod(n=40), configs.sod(n=40, precision=prec), steps=10)
     assert e <= RHS_TOL
-    assert _steps_err(configs.sod(n=40), configs.sod(n=40, precision="mixed"), 100).max() <= STEPS_TOL
+    assert _steps_err(configs.sod(n=40), configs.sod(n=40, precision=prec), 100).max() <= STEPS_TOL
 
 
 @pytest.mark.parametrize("scheme", ["Rusanov", "AUSM+-up", "Rusanov-HLLC", "Chandrashekhar"])
@@ -88,9 +92,10 @@ def test_mixed_volume_schemes(scheme):
     assert e <= RHS_TOL
 
 
-def test_mixed_viscous_cylinder():
+@pytest.mark.parametrize("prec", PRECS)
+def test_mixed_viscous_cylinder(prec):
     c64 = make(configs.cylinder(n_radial=6, n_azimuthal=12))
-    cmx = make(configs.cylinder(n_radial=6, n_azimuthal=12, precision="mixed"))
+    cmx = make(configs.cylinder(n_radial=6, n_azimuthal=12, precision=prec))
     U, t = _state(c64, 2)
     o = Oracle(c64)
     o.set_state(U, t)
@@ -104,24 +109,26 @@ def test_mixed_viscous_cylinder():
     print(f"cylinder rhs err {e:.3e} (worst var {worst[0]} cell {worst[1] // 64}); per-var rel L1 "
           f"{d.sum(axis=1) / np.abs(Ro).sum(axis=1)}")
     assert e <= 2e-3
-    s = _steps_err(configs.cylinder(n_radial=6, n_azimuthal=12), configs.cylinder(n_radial=6, n_azimuthal=12, precision="mixed"))
+    s = _steps_err(configs.cylinder(n_radial=6, n_azimuthal=12), configs.cylinder(n_radial=6, n_azimuthal=12, precision=prec))
     print(f"cylinder 20-step rel L1 {s}")
     assert s.max() <= STEPS_TOL
 
 
-def test_mixed_viscous_shock_vortex():
-    e = _rhs_err(configs.shock_vortex(n=3, modes=2), configs.shock_vortex(n=3, modes=2, precision="mixed"), steps=1)
+@pytest.mark.parametrize("prec", PRECS)
+def test_mixed_viscous_shock_vortex(prec):
+    e = _rhs_err(configs.shock_vortex(n=3, modes=2), configs.shock_vortex(n=3, modes=2, precision=prec), steps=1)
     print(f"shock-vortex rhs err {e:.3e}")
     assert e <= RHS_TOL
-    s = _steps_err(configs.shock_vortex(n=3, modes=2), configs.shock_vortex(n=3, modes=2, precision="mixed"), 5)
+    s = _steps_err(configs.shock_vortex(n=3, modes=2), configs.shock_vortex(n=3, modes=2, precision=prec), 5)
     assert s.max() <= STEPS_TOL
 
 
-def test_mixed_rk3():
-    def spec(prec):
-        prm, files, deg = configs.dmr(nx=12, ny=4, precision=prec)
+@pytest.mark.parametrize("prec", PRECS)
+def test_mixed_rk3(prec):
+    def spec(p):
+        prm, files, deg = configs.dmr(nx=12, ny=4, precision=p)
         return prm.replace("set RK order = 4", "set RK order = 3"), files, deg
-    assert _steps_err(spec("fp64"), spec("mixed")).max() <= STEPS_TOL
+    assert _steps_err(spec("fp64"), spec(prec)).max() <= STEPS_TOL
 
 
 def test_mixed_positivity_failure_reports_first_bad_dof():

@@ -34,11 +34,17 @@ def test_mlp_gradient_matches_oracle():
     x, y = _data(517, seed=2)
     loss_g, g_gpu = mlp_loss_grad(x, y, p)
     loss_r, g_ref = mlp_oracle.loss_grad(p, x, y)
-    assert abs(loss_g - loss_r) <= 1e-4 * abs(loss_r)
-    scale = np.abs(g_ref).max()
-    assert np.abs(g_gpu - g_ref).max() <= 1e-3 * scale
-    # per block: W1, W2, w3 are all exercised
-    assert np.abs(g_ref[:4096]).max() > 0 and np.abs(g_ref[4160:8256]).max() > 0
+    assert abs(loss_g - loss_r) <= 1e-5 * abs(loss_r)
+    # per parameter block (W1, b1, W2, b2, w3, b3), against the block's largest gradient: FP32
+    # kernels with fixed-order reductions against the FP64 oracle
+    bounds = np.cumsum([0, 64 * 64, 64, 64 * 64, 64, 64, 1])
+    errs = []
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        scale = np.abs(g_ref[a:b]).max()
+        assert scale > 0
+        errs.append(np.abs(g_gpu[a:b] - g_ref[a:b]).max() / scale)
+    print("per-block relative gradient errors (W1, b1, W2, b2, w3, b3):", ["%.2e" % e for e in errs])
+    assert max(errs) <= 1e-4
 
 
 def test_mlp_training_reduces_loss():

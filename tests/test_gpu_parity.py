@@ -194,10 +194,12 @@ def test_positivity_failure_reports_first_bad_dof():
     g.rhs()
 
 
-def test_mixed_precision_dmr_error_bound():
-    """FP32 flux differencing with FP64 registers: rho relative L1 vs the FP64 oracle <= 1e-4."""
+@pytest.mark.parametrize("prec", ["mixed", "mixed_r32"])
+def test_mixed_precision_dmr_error_bound(prec):
+    """FP32 flux differencing (with FP64 registers and metric terms in "mixed", FP32 registers and
+    metric images in "mixed_r32"): rho relative L1 vs the FP64 oracle <= 1e-4."""
     spec_fp64 = configs.dmr(nx=24, ny=6)
-    spec_mixed = configs.dmr(nx=24, ny=6, precision="mixed")
+    spec_mixed = configs.dmr(nx=24, ny=6, precision=prec)
     c64 = make(spec_fp64)
     cmx = make(spec_mixed)
     o = Oracle(c64)
