@@ -76,6 +76,17 @@ static __global__ void k_state_out(Dev dv, double* __restrict__ dst)
         dst[i] = dv.U[i];
 }
 
+// the clock of the next state of a sequence (plens_gpu_advance_states), on the stream: what
+// plens_gpu_set_time writes from the host
+static __global__ void k_set_clock(Dev dv, double t, long long n_steps)
+{
+    Scalars* s = dv.sc;
+    s->time = t;
+    s->n_steps = n_steps;
+    s->err = 0;
+    s->bad_dof = INT64_MAX;
+}
+
 // mixed form: the FP32 image of the state after the host or a restore changed U
 static __global__ void k_state_image(Dev dv)
 {
@@ -1336,9 +1347,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                 const double u = dv.U[k];
                 double un;
                 if (sa.mode == 1) {
-                    un = __fma_rn(sa.c2, Rs, u);  // the chain of the TMA-staged kernel
-                    if (sa.stage >= 2) un = __fma_rn(sa.c1, sa.R1[k], un);
+                    // U + c0 R0 + c1 R1 + c2 Rs, the chain of the TMA-staged kernel
+                    un = u;
                     if (sa.stage >= 3) un = __fma_rn(sa.c0, sa.R0[k], un);
+                    if (sa.stage >= 2) un = __fma_rn(sa.c1, sa.R1[k], un);
+                    un = __fma_rn(sa.c2, Rs, un);
                     sa.Rw[k] = Rs;
                 } else {
                     if (sa.stage == 1) un = u + Rs;

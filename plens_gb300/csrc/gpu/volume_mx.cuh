@@ -44,7 +44,7 @@ struct MxSmem {
     static constexpr size_t oU = 0;                                   // double [5][NB]
     static constexpr size_t oUf = oU + up16(8 * 5 * NB);              // float [5][NB]
     static constexpr size_t oDet = oUf + up16(4 * 5 * NB);            // float [NB] (R64: double [NB])
-    static constexpr size_t oJ = oDet + up16(RB * NB);                // float [9][NB]
+    static constexpr size_t oJ = oDet + up16((R64 ? 8 : 4) * NB);     // float [9][NB]
     static constexpr size_t oR0 = oJ + up16(4 * 9 * NB);              // RB [5][NB]
     static constexpr size_t oR1 = oR0 + up16(RB * 5 * NB);            // RB [5][NB]
     static constexpr size_t oSf = oR1 + up16(RB * 5 * NB);            // float [5][NF]
