@@ -296,24 +296,33 @@ def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_in
         g.close()
         return {"case": case, "ms": ms, "launches": launches, "vol_ms": vol_ms, "vol_n": vol_n,
                 "clocks": cs.summary(), "stats": stats, "U": Ug}
-    # end to end through the C ABI with pinned host buffers: per step the state goes host ->
-    # device, one step runs, the new state comes back
+    # end to end through the C ABI with pinned host buffers: per step a state goes host -> device,
+    # one step runs, the new state comes back. (1) plens_gpu_advance_states: a sequence of states,
+    # the transfers on copy streams beside the steps; (2) the serial loop set_state -> advance(1)
+    # -> get_state, each call synchronous.
     pin_in = torch.empty((5, case.n_dofs), dtype=torch.float64).pin_memory()
     pin_in.numpy()[:] = Ug
     pin_out = torch.empty((5, case.n_dofs), dtype=torch.float64).pin_memory()
-    e2e_steps = max(3, min(steps, 20))
+    t_state = g.get_time()[0]
+    e2e_steps = max(3, steps)
+    g.advance_states([pin_in.numpy()], [pin_out.numpy()], t_state, 1)  # copy streams and buffers made
     barrier()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    g.advance_states([pin_in.numpy()] * e2e_steps, [pin_out.numpy()] * e2e_steps, t_state, 1)
+    t_e2e = time.perf_counter() - t0
+    serial_steps = max(3, min(steps, 20))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(serial_steps):
         g.set_state(pin_in.numpy())
         g.advance(1)
         g.get_state(pin_out.numpy())
-    t_e2e = time.perf_counter() - t0
+    t_serial = time.perf_counter() - t0
     g.close()
     return {
         "case": case, "ms": ms, "launches": launches, "vol_ms": vol_ms, "vol_n": vol_n,
         "clocks": cs.summary(), "stats": stats, "U": Ug, "e2e_s": t_e2e, "e2e_steps": e2e_steps,
-        "bytes_state": 5 * case.n_dofs * 8,
+        "serial_s": t_serial, "serial_steps": serial_steps, "bytes_state": 5 * case.n_dofs * 8,
     }
 
 
@@ -479,6 +488,64 @@ def run_workload_report(args):
     print(json.dumps(out), flush=True)
 
 
+# z boundaries and z resolution of the double Mach reflection: the variants of the horizon study
+HORIZON_VARIANTS = {
+    "periodic": dict(z_bc="periodic"),                  # the configuration: one periodic cell across z
+    "periodic_no_noise": dict(z_bc="periodic", noise=0.0),  # the same without the seeded density noise
+    "symmetry": dict(z_bc="symmetry"),                  # the reference's own z boundaries
+    "periodic_2_cells": dict(z_bc="periodic", nz=2),    # two periodic cells across z
+    "plens_2d": dict(z_bc="periodic", plens_2d=True),   # the reference's PLENS_2D switch
+}
+
+
+def run_horizon(args):
+    """How far the double Mach reflection gets towards t = 0.2 with each z treatment, and how the
+    flow's z-dependence grows on the way: every 100 steps the max |rho w| over max |rho u|, and the
+    largest spread of rho and of rho E across the P z-layers of a cell (relative to their maxima).
+    One JSON line per variant; on a positivity failure, the first failing dof with its cell, node,
+    z-layer and location."""
+    import torch
+
+    from plens_gb300 import configs
+    from plens_gb300.api import GpuSolver, PositivityError
+
+    torch.cuda.set_device(0)
+    prec = args.horizon_precision
+    for name in args.horizon.split(","):
+        case = configs.make_case(configs.dmr(precision=prec, **HORIZON_VARIANTS[name]))
+        P = case.degree + 1
+        P2, P3 = P * P, P ** 3
+
+        def zstats(U):
+            Ur = U.reshape(5, case.n_cells, P, P2)
+            spread = lambda a: float((a.max(axis=1) - a.min(axis=1)).max() / np.abs(a).max())  # noqa: E731
+            return {"w_rel": float(np.abs(U[3]).max() / np.abs(U[1:4]).max()), "rho_z_spread": spread(Ur[0]),
+                    "rhoE_z_spread": spread(Ur[4])}
+
+        g = GpuSolver(case)
+        g.set_state(case.initial_state(), 0.0)
+        t0 = time.perf_counter()
+        hist, out = [], {"variant": name, "precision": prec, "end_time": 0.2}
+        while True:
+            try:
+                g.advance(100, 0.2)
+            except PositivityError as e:
+                t, n, _ = g.get_time()
+                xyz = case.dof_xyz()[:, e.dof]
+                out["failed"] = {"t": t, "steps": n, "dof": e.dof, "cell": e.dof // P3, "node": e.dof % P3,
+                                 "z_layer": (e.dof % P3) // P2, "xyz": [float(v) for v in xyz]}
+                break
+            t, n, _ = g.get_time()
+            hist.append(dict(t=t, steps=n, **zstats(g.get_state())))
+            if t >= 0.2 or time.perf_counter() - t0 > 300:
+                out["reached"] = t >= 0.2
+                break
+        out["seconds"] = time.perf_counter() - t0
+        out["history"] = hist
+        g.close()
+        print(json.dumps(out), flush=True)
+
+
 FORMS = {"plain": ("fp64", "modal"), "modal": ("mixed", "modal"), "learned": ("mixed", "learned"),
          "modal_r32": ("mixed_r32", "modal"), "learned_r32": ("mixed_r32", "learned")}
 
@@ -513,6 +580,8 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=0, help="override the accuracy window (steps)")
     ap.add_argument("--sensor-tensor-cores", action="store_true",
                     help="the learned sensor's hidden layers on the tensor cores (tcgen05, 3xTF32)")
+    ap.add_argument("--horizon", default="", help="comma-separated DMR z variants: " + ",".join(HORIZON_VARIANTS))
+    ap.add_argument("--horizon-precision", default="mixed", choices=["fp64", "mixed", "mixed_r32"])
     ap.add_argument("--form", default="", choices=["", "plain", "modal", "learned", "modal_r32", "learned_r32"],
                     help="time one form only and print its numbers (a short run for profiling) instead of "
                          "the benchmark line")
@@ -520,6 +589,9 @@ def main():
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.horizon:
+        run_horizon(args)
         return
     if args.workload:
         run_workload_report(args)
@@ -566,8 +638,10 @@ def main():
             continue
         t = max_over_ranks(r["ms"] / 1e3, device)
         te = max_over_ranks(r["e2e_s"], device)
+        ts = max_over_ranks(r["serial_s"], device)
         job[k] = {"value": nd * 5 * args.steps * ws / t, "ms_per_step": 1e3 * t / args.steps,
                   "e2e": nd * 5 * r["e2e_steps"] * ws / te,
+                  "e2e_serial_calls": nd * 5 * r["serial_steps"] * ws / ts,
                   "volume_kernel_ms": r["vol_ms"] / max(r["vol_n"], 1),
                   "bytes_per_dof_stage": BYTES_PER_DOF_STAGE[k],
                   "achieved_gbs": BYTES_PER_DOF_STAGE[k] * nd / (r["vol_ms"] / max(r["vol_n"], 1) / 1e3) / 1e9}
@@ -619,7 +693,11 @@ def main():
                     "profiles/k_volume_mx_dmr.md",
         },
         "e2e": {"value": hd["e2e"], "unit": UNIT, "h2d_bytes_per_step": fast["bytes_state"],
-                "d2h_bytes_per_step": fast["bytes_state"]},
+                "d2h_bytes_per_step": fast["bytes_state"],
+                "how": "plens_gpu_advance_states over a sequence of one-step members from page-locked host "
+                       "buffers (host -> device copy, one step, device -> host copy per member; the copies run "
+                       "on copy streams beside the steps)",
+                "serial_calls": hd["e2e_serial_calls"]},
         "gpu_launches": fast["launches"],
         "clocks": fast["clocks"],
     }

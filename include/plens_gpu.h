@@ -263,6 +263,25 @@ int plens_gpu_advance(plens_ctx* ctx, int64_t n_steps, double end_time);
 int plens_gpu_advance_async(plens_ctx* ctx, int64_t n_steps, double end_time);
 int plens_gpu_synchronize(plens_ctx* ctx);
 
+/* A sequence of independent states on this context's mesh and parameters (ensemble members,
+ * the cases of a parameter study, restarts), each made the current state at time t0 with the step
+ * counter at 0, advanced by n_steps steps as plens_gpu_advance advances it (stopping at end_time),
+ * and handed back. The reference advances one state per run, `while (cur_time < end_time)
+ * update();` (PLENS::run, dgsem/plens.cc:1509-1550); a host loop of plens_gpu_set_state,
+ * plens_gpu_advance and plens_gpu_get_state does the same per member with the transfers in series.
+ * Here the transfers run on two copy streams beside the steps: member j+1 is copied in and member
+ * j-1 copied out while member j is advanced.
+ *  - U_in[j], U_out[j]: host [5][ndof] buffers. Page-locked ones (cudaHostAlloc,
+ *    cudaHostRegister) give the overlap; pageable ones give the same results in series.
+ *    U_out[j] must not overlap any U_in[k], k > j.
+ *  - t_out: NULL or count doubles, member j's clock after its steps.
+ *  - On an error the call stops at the failing member (named in plens_gpu_last_error); the
+ *    outputs of the members before it are complete. No copy to or from the caller's buffers
+ *    outlives the call. The context then holds the state and clock of the last member it
+ *    advanced. Device buffers for the two staged states are made on the first call. */
+int plens_gpu_advance_states(plens_ctx* ctx, int64_t count, const double* const* U_in, double* const* U_out,
+                             double t0, int64_t n_steps, double end_time, double* t_out);
+
 /* Error norms of the current state as PLENS::write logs them (dgsem/plens.cc:4234-4243), i.e.
  * at stage 1 of the next step, after its time step: the steady-state error
  * ||(rhoE - rhoE_old) / loc_dt|| / ||rhoE|| (calc_ss_error, 3985-4035; rhoE_old = rho E at the

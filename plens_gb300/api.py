@@ -166,6 +166,7 @@ def gpu_lib() -> C.CDLL:
         L.plens_gpu_advance.argtypes = [vp, i64, dbl]
         L.plens_gpu_advance_async.argtypes = [vp, i64, dbl]
         L.plens_gpu_synchronize.argtypes = [vp]
+        L.plens_gpu_advance_states.argtypes = [vp, i64, vp, vp, dbl, i64, dbl, vp]
         L.plens_gpu_get_cell_scalars.argtypes = [vp, vp, vp, vp]
         L.plens_gpu_error_norms.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.plens_gpu_get_avars.argtypes = [vp, vp]
@@ -411,6 +412,22 @@ class GpuSolver:
 
     def synchronize(self):
         self._check(self.L.plens_gpu_synchronize(self.h), "synchronize")
+
+    def advance_states(self, U_in, U_out, t0: float, n_steps: int, end_time: float = 1e300) -> np.ndarray:
+        """Advance each state of the sequence U_in ([5][ndof] FP64 host arrays) from time t0 by
+        n_steps steps into the matching array of U_out, with the host transfers overlapping the
+        steps (plens_gpu_advance_states; page-locked arrays give the overlap). Returns each
+        member's clock."""
+        n = len(U_in)
+        assert len(U_out) == n
+        for U in list(U_in) + list(U_out):
+            assert U.dtype == np.float64 and U.shape == (5, self.n_dofs) and U.flags.c_contiguous
+        pin = (C.c_void_p * max(n, 1))(*[_ptr(U) for U in U_in])
+        pout = (C.c_void_p * max(n, 1))(*[_ptr(U) for U in U_out])
+        t = np.empty(max(n, 1))
+        self._check(self.L.plens_gpu_advance_states(self.h, n, pin, pout, t0, n_steps, end_time, _ptr(t)),
+                    "advance_states")
+        return t[:n]
 
     def error_norms(self):
         """(steady-state error, convergence error) of the current state, as PLENS::write logs

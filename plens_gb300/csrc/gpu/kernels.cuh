@@ -932,7 +932,9 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
     T* sNorm = sAv + (VISC ? CPB * 9 * P3 : 0);  // [CPB][P3] scratch
     (void)sNorm;
     Scalars* s = dv.sc;
-    if (!s->active) return;
+    // a positivity failure earlier in this step stops the updates: the state stays that of the
+    // RHS that failed, as the reference exits there (assert_positivity, dgsem/plens.cc:2531-2546)
+    if (!s->active || s->err) return;
     const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
     const int64_t cell = (int64_t)blockIdx.x * CPB + cl;
     const bool valid = (cl < CPB) && (cell < dv.nc);

@@ -157,6 +157,9 @@ struct plens_ctx {
     // kernels, which do not read alpha unless the surface flux blends with it
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // mixed forms with the compacted troubled-cell list: the interior subcell sums of the listed
+    // cells follow alpha and the list on the side stream; the volume kernel joins them
+    cudaEvent_t ev_join_lo = nullptr;
     // the start of a step (stable time step, rho E and state snapshots) runs on a third stream
     // beside stage 1's indicator and face kernels; stage 1's volume kernel, the first to need dt
     // or to write the state, joins it
@@ -191,6 +194,12 @@ struct plens_ctx {
     unsigned char* snap_host = nullptr;
     size_t snap_bytes = 0;
     bool snap_pending = false;
+    // sequences of states (plens_gpu_advance_states): the next member's state copied in on one
+    // stream, the last member's state copied out on another, each through a device buffer of its
+    // own; made on the first call
+    cudaStream_t seq_in = nullptr, seq_out = nullptr;
+    cudaEvent_t seq_in_ready = nullptr, seq_in_free = nullptr, seq_out_ready = nullptr, seq_out_free = nullptr;
+    double *seq_in_buf = nullptr, *seq_out_buf = nullptr;
     // error norms of the output steps: rho E of the previous step's start, the quadrature data,
     // per-cell and total sums
     double* rhoE_old = nullptr;
@@ -295,6 +304,13 @@ int launch_rhs(plens_ctx* c, const StageArgs& sa)
     }
     e = cudaEventRecord(c->ev_join, c->side);
     if (e != cudaSuccess) return cuda_fail(c, e, "indicator join");
+    if (c->dv.lo_blk) {
+        // the interior subcell sums of the listed troubled cells (need alpha and the list only;
+        // the volume kernel adds their cell-face terms), still beside the face kernels
+        c->launches += c->tab.subcell(c->dv, c->ops, c->gas, c->side);
+        e = cudaEventRecord(c->ev_join_lo, c->side);
+        if (e != cudaSuccess) return cuda_fail(c, e, "subcell join");
+    }
     if (c->viscous) {
         c->launches += c->tab.surface(1, c->dv, c->gas, c->dv.sf, st);
         c->launches += c->tab.aux(c->dv, c->ops, c->gas, st);
@@ -310,9 +326,10 @@ int launch_rhs(plens_ctx* c, const StageArgs& sa)
     if (e != cudaSuccess) return cuda_fail(c, e, "indicator join");
     c->step_join_pending = false;
     if (blended) c->launches += c->tab.surface(2, c->dv, c->gas, c->dv.sf, st);
-    // the subcell residual of the listed troubled cells (needs alpha, the list and the stage-2
-    // face fluxes), read by the volume kernel
-    if (c->dv.lo_blk) c->launches += c->tab.subcell(c->dv, c->ops, c->gas, st);
+    if (c->dv.lo_blk) {
+        e = cudaStreamWaitEvent(st, c->ev_join_lo, 0);
+        if (e != cudaSuccess) return cuda_fail(c, e, "subcell join");
+    }
     if (c->timing) {
         if (c->ev_used == c->ev_pool.size()) {
             cudaEvent_t a, b;
@@ -511,6 +528,7 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
     CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_join_lo, cudaEventDisableTiming));
     CK(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->ev_step_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_step_join, cudaEventDisableTiming));
@@ -633,9 +651,16 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         if ((r = dalloc(c, &invJ, nd))) return r;
         CK(cudaDeviceSynchronize());  // the uploads above ran on the legacy stream
         k_reciprocal<<<(unsigned)std::min<int64_t>((nd + 255) / 256, 152 * 16), 256, 0, c->stream>>>(d.detJ, invJ, nd);
-        c->launches += 1;
-        if ((r = check_launch(c, "1/detJ"))) return r;
+        // the time step is an FP32 estimate from the FP32 rounding of J^-1: read from an image
+        // made once (the same values; half the bytes of rounding the FP64 array every step)
+        float* Jinvf = nullptr;
+        if ((r = dalloc(c, &Jinvf, 9 * nd))) return r;
+        k_round_f32<<<(unsigned)std::min<int64_t>((9 * nd + 255) / 256, 152 * 16), 256, 0, c->stream>>>(d.Jinv, Jinvf,
+                                                                                                    9 * nd);
+        c->launches += 2;
+        if ((r = check_launch(c, "1/detJ, J^-1 image"))) return r;
         d.invJ = invJ;
+        d.Jinvf = Jinvf;
     } else if (c->mixed) {
         // MIXED_R32 form: the FP32 rounding of the metric terms, once (every FP32 consumer reads
         // these instead of rounding the FP64 arrays itself: the same values)
@@ -747,11 +772,19 @@ int plens_gpu_destroy(plens_ctx* c)
     if (c->snap_ready) cudaEventDestroy(c->snap_ready);
     if (c->snap_done) cudaEventDestroy(c->snap_done);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    for (cudaStream_t s : {c->seq_in, c->seq_out})
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    for (cudaEvent_t e : {c->seq_in_ready, c->seq_in_free, c->seq_out_ready, c->seq_out_free})
+        if (e) cudaEventDestroy(e);
     if (c->side) cudaStreamSynchronize(c->side);
     if (c->aux) cudaStreamSynchronize(c->aux);
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_join_lo) cudaEventDestroy(c->ev_join_lo);
     if (c->ev_step_fork) cudaEventDestroy(c->ev_step_fork);
     if (c->ev_step_join) cudaEventDestroy(c->ev_step_join);
     if (c->side) cudaStreamDestroy(c->side);
@@ -972,6 +1005,93 @@ int plens_gpu_advance(plens_ctx* c, int64_t n_steps, double end_time)
     }
     if (int r = plens_gpu_advance_async(c, n_steps, end_time)) return r;
     return sync_and_check(c);
+}
+
+namespace {
+
+// the copy streams, events and device buffers of plens_gpu_advance_states, once per context
+int sequence_setup(plens_ctx* c)
+{
+    if (c->seq_in_buf) return 0;
+    CK(cudaStreamCreateWithFlags(&c->seq_in, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->seq_out, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&c->seq_in_ready, &c->seq_in_free, &c->seq_out_ready, &c->seq_out_free})
+        CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    double *a = nullptr, *b = nullptr;
+    if (int r = dalloc(c, &a, 5 * c->nd)) return r;
+    if (int r = dalloc(c, &b, 5 * c->nd)) return r;
+    c->seq_in_buf = a;
+    c->seq_out_buf = b;
+    return 0;
+}
+
+// one member of a sequence: its state (staged in seq_in_buf) made current at time t0, its steps,
+// its state copied to seq_out_buf and from there to the host on seq_out; the next member's copy
+// into seq_in_buf is issued as soon as this member's state has left that buffer
+int sequence_member(plens_ctx* c, int64_t j, int64_t count, const double* const* U_in, double* const* U_out,
+                    double t0, int64_t n_steps, double end_time, double* t_out)
+{
+    const size_t bytes = sizeof(double) * 5 * c->nd;
+    const unsigned grid = (unsigned)std::min<int64_t>((5 * c->nd + 255) / 256, 152 * 16);
+    CK(cudaStreamWaitEvent(c->stream, c->seq_in_ready, 0));
+    k_state_in<<<grid, 256, 0, c->stream>>>(c->dv, c->seq_in_buf);  // U and the FP32 image
+    k_set_clock<<<1, 1, 0, c->stream>>>(c->dv, t0, 0);
+    c->launches += 2;
+    if (int r = check_launch(c, "state in")) return r;
+    CK(cudaEventRecord(c->seq_in_free, c->stream));
+    if (j + 1 < count) {
+        CK(cudaStreamWaitEvent(c->seq_in, c->seq_in_free, 0));
+        CK(cudaMemcpyAsync(c->seq_in_buf, U_in[j + 1], bytes, cudaMemcpyHostToDevice, c->seq_in));
+        CK(cudaEventRecord(c->seq_in_ready, c->seq_in));
+    }
+    if (int r = plens_gpu_advance(c, n_steps, end_time)) return r;
+    if (t_out) CK(cudaMemcpy(&t_out[j], &c->sc->time, sizeof(double), cudaMemcpyDeviceToHost));
+    // the previous member's copy out must have left seq_out_buf
+    CK(cudaStreamWaitEvent(c->stream, c->seq_out_free, 0));
+    CK(cudaMemcpyAsync(c->seq_out_buf, c->dv.U, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaEventRecord(c->seq_out_ready, c->stream));
+    CK(cudaStreamWaitEvent(c->seq_out, c->seq_out_ready, 0));
+    CK(cudaMemcpyAsync(U_out[j], c->seq_out_buf, bytes, cudaMemcpyDeviceToHost, c->seq_out));
+    CK(cudaEventRecord(c->seq_out_free, c->seq_out));
+    return 0;
+}
+
+}  // namespace
+
+int plens_gpu_advance_states(plens_ctx* c, int64_t count, const double* const* U_in, double* const* U_out,
+                             double t0, int64_t n_steps, double end_time, double* t_out)
+{
+    if (!c || !c->dv.U) return PLENS_GPU_E_INVALID;
+    if (count < 0 || n_steps < 0) return fail(c, PLENS_GPU_E_INVALID, "advance_states: negative count or step number");
+    if (count == 0) return 0;
+    if (!U_in || !U_out) return fail(c, PLENS_GPU_E_INVALID, "advance_states: null state array");
+    for (int64_t j = 0; j < count; ++j)
+        if (!U_in[j] || !U_out[j])
+            return fail(c, PLENS_GPU_E_INVALID, "advance_states: null state buffer of member " + std::to_string(j));
+    if (c->learned && !c->mlp.weights_set) return fail(c, PLENS_GPU_E_INVALID, "learned sensor: weights not set");
+    if (int r = sequence_setup(c)) return r;
+    int r = 0;
+    {
+        const cudaError_t e = cudaMemcpyAsync(c->seq_in_buf, U_in[0], sizeof(double) * 5 * c->nd,
+                                              cudaMemcpyHostToDevice, c->seq_in);
+        r = (e == cudaSuccess) ? 0 : cuda_fail(c, e, "advance_states: copy in");
+        if (!r) {
+            const cudaError_t e2 = cudaEventRecord(c->seq_in_ready, c->seq_in);
+            if (e2 != cudaSuccess) r = cuda_fail(c, e2, "advance_states: event");
+        }
+    }
+    int64_t j = 0;
+    for (; j < count && !r; ++j) r = sequence_member(c, j, count, U_in, U_out, t0, n_steps, end_time, t_out);
+    // no copy into or out of the caller's buffers outlives the call
+    const cudaError_t ei = cudaStreamSynchronize(c->seq_in);
+    const cudaError_t eo = cudaStreamSynchronize(c->seq_out);
+    if (r) {
+        c->err = "advance_states: member " + std::to_string(j - 1) + ": " + c->err;
+        return r;
+    }
+    if (ei != cudaSuccess) return cuda_fail(c, ei, "advance_states: copy in");
+    if (eo != cudaSuccess) return cuda_fail(c, eo, "advance_states: copy out");
+    return 0;
 }
 
 int plens_gpu_error_norms(plens_ctx* c, double* ss_error, double* conv_error)

@@ -1,14 +1,17 @@
 // subcell_mx.cuh -- the mixed forms' first-order subcell residual over the compacted troubled-cell
 // list: calc_cell_lo_inv_residual (dgsem/plens.cc:3469-3583) for the cells with alpha > 0 only,
-// in a kernel of its own between the inviscid face fluxes and the volume kernel.
+// in a kernel of its own on the indicator stream, beside the face kernels.
 //
 // The list is ordered by cell index and built without atomics: the smoothing kernel counts each
 // block's troubled cells (k_alpha_smooth, 128 cells per block), k_lo_list gives every block its
 // offset (the sum of the counts of the blocks before it) and every troubled cell its rank within
 // the block (warp ballots), so the list and each cell's position lo_pos are the same on every run.
-// k_subcell_lo then runs one thread per GLL node of a listed cell and writes the cell's unscaled
-// subcell sums (the three directions' contributions, before the 1/(-detJ) scaling) to
-// lo_buf[var][position * P^3 + node], which the volume kernel blends in.
+// k_subcell_lo then runs the subcell interfaces inside each listed cell (the line tasks' P - 1
+// interior fluxes) and writes the cell's unscaled sums of the three directions to
+// lo_buf[var][position * P^3 + node]. It needs the state, the metric terms and alpha only; the
+// cell-face terms of the first-order residual (the inviscid face flux x |Ja| / w at the nodes on
+// the cell's faces, plens.cc:3544-3575) need this stage's face fluxes and are added by the volume
+// kernel, which has them staged.
 #pragma once
 
 #include "kernels.cuh"
@@ -60,19 +63,18 @@ static __global__ void __launch_bounds__(kSmoothThreads) k_lo_list(Dev dv)
     }
 }
 
-// Subcell residual sums of the listed cells, CPB cells per block, one thread per GLL node; line
-// tasks numbered flat over the block's cells (3 P^2 per cell), each running the subcell
+// Interior subcell sums of the listed cells, CPB cells per block, one thread per GLL node; line
+// tasks numbered flat over the block's cells (3 P^2 per cell), each running the P - 1 subcell
 // interfaces of one line. The grid is persistent: blocks take groups of CPB listed cells with a
 // stride, up to the count the list kernel wrote.
 template <int P>
 __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Ops ops, GasP g)
 {
     using CB = CellBlock<P>;
-    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1, NB = CPB * P3, NF = CPB * 6 * P2;
+    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, NB = CPB * P3;
     constexpr int TPC = 3 * P2;
     __shared__ float sC[5][NB];   // FP32 state image
     __shared__ float sJ[9][NB];   // FP32 rounding of Ja
-    __shared__ float sSf[5][NF];  // stage-2 face fluxes
     __shared__ float sAcc[CPB][15][P3];
     __shared__ float sAl[CPB];
     __shared__ int32_t sCell[CPB];
@@ -96,9 +98,6 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
             for (int v = 0; v < 5; ++v) sC[v][cl * P3 + node] = dv.Uf[v * dv.nd + dof];
 #pragma unroll
             for (int m = 0; m < 9; ++m) sJ[m][cl * P3 + node] = metric<float>(dv.Ja, dv.Jaf, m * dv.nd + dof);
-            for (int sl = node; sl < 6 * P2; sl += P3)
-#pragma unroll
-                for (int v = 0; v < 5; ++v) sSf[v][cl * 6 * P2 + sl] = as_real<float>(dv.sf)[v * dv.nslot + cell * 6 * P2 + sl];
         }
         __syncthreads();
         for (int ft = tid; ft < ncb * TPC; ft += CB::THREADS) {
@@ -137,20 +136,6 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
                     acc[id - 1][v] += F[v] * wl;
                     acc[id][v] -= F[v] * wr;
                 }
-            }
-            // cell-face terms at both ends of the line: the stage-2 face flux x |Ja| / w
-            // (contribution sign x flux sign = +1, plens.cc:3544-3575)
-#pragma unroll
-            for (int lr = 0; lr < 2; ++lr) {
-                const int i = lr ? N : 0;
-                const int ni = base + line_node<P>(dir, la, lb, i);
-                const int f = 2 * dir + lr;
-                const int q = la + P * lb;
-                const float j0 = sJ[dir * 3][ni], j1 = sJ[dir * 3 + 1][ni], j2 = sJ[dir * 3 + 2][ni];
-                const float nn = sqrtf(j0 * j0 + j1 * j1 + j2 * j2);
-                const float sw = __fdividef(nn, opW<float>(ops, lr * N));
-#pragma unroll
-                for (int v = 0; v < 5; ++v) acc[i][v] += sSf[v][tc * 6 * P2 + f * P2 + q] * sw;
             }
 #pragma unroll
             for (int i = 0; i < P; ++i) {

@@ -7,9 +7,10 @@
 // 16-byte aligned chunk per variable: one thread issues the copies, two mbarriers signal them --
 // the FP32 state image (and, in the MIXED_R32 form, the FP32 metric images) that the flux phase
 // needs first, then the FP64 state, the face values and the RK registers (and, in the MIXED form,
-// 1/detJ in FP64), which arrive while the fluxes are computed. The subcell residual of the
-// troubled cells comes from k_subcell_lo (subcell_mx.cuh), which runs before this kernel on the
-// compacted troubled-cell list.
+// 1/detJ in FP64), which arrive while the fluxes are computed. The first-order subcell residual
+// of the troubled cells is the interior sums k_subcell_lo (subcell_mx.cuh) makes over the
+// compacted troubled-cell list beside the face kernels, plus the cell-face terms, which this
+// kernel adds from its staged face values.
 //
 // R64 selects the MIXED form: the metric terms are read in FP64 (each thread rounds its node's
 // nine Ja components for the FP32 fluxes), the residual's FP32 sums are scaled by -dt/detJ in
@@ -55,10 +56,11 @@ struct MxSmem {
     static constexpr size_t bytes = oQ + up16(4 * NQ * NB);
 };
 
-// Resident blocks per SM the register allocation is sized for: six 128-thread blocks at P = 2, 4
-// (80 registers; the shared-memory limit is six or more), two 224-thread blocks at P = 6.
+// Resident blocks per SM the register allocation is sized for: 128-thread blocks at P = 2, 4 --
+// six in the MIXED_R32 form (80 registers), seven in the MIXED form (72 registers, no spills;
+// its 30 KB of shared memory allow seven) -- and two 224-thread blocks at P = 6.
 template <int P, bool R64>
-constexpr int vol_mx_min_blocks() { return P == 6 ? 2 : 6; }
+constexpr int vol_mx_min_blocks() { return P == 6 ? 2 : (R64 ? 7 : 6); }
 
 template <int P, bool VISC, bool R64>
 __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R64>()) k_volume_mx(Dev dv, Ops ops, GasP g, StageArgs sa)
@@ -84,7 +86,9 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
     float* sQ = reinterpret_cast<float*>(smem_raw + L::oQ);
 
     Scalars* s = dv.sc;
-    if (!s->active) return;
+    // no update after a positivity failure earlier in the step (the state stays that of the RHS
+    // that failed, where the reference exits)
+    if (!s->active || s->err) return;
     const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
     const int64_t cell0 = (int64_t)blockIdx.x * CPB;
     const int ncb = (int)((dv.nc - cell0 < CPB) ? dv.nc - cell0 : CPB);  // cells of this block
@@ -376,16 +380,34 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
         }
     }
 
-    // ---- phase C: first-order subcell residual, only where alpha > 0: the sums k_subcell_lo
-    // wrote for this cell's place in the compacted troubled-cell list
+    // ---- phase C: first-order subcell residual, only where alpha > 0: the interior sums
+    // k_subcell_lo wrote for this cell's place in the compacted troubled-cell list, plus the
+    // cell-face terms at the nodes on the cell's faces: this stage's face flux x |Ja| / w
+    // (contribution sign x flux sign = +1, calc_cell_lo_inv_residual, dgsem/plens.cc:3544-3575)
     float lo[5] = {0, 0, 0, 0, 0};
     if (valid && stored_gt0<float>(alpha)) {
         const int32_t pos = dv.lo_pos[cell];
         if (pos >= 0) {
-            const float js = R64 ? 1.0f : __fdividef(-1.0f, detJ);
             const int64_t o = (int64_t)pos * P3 + node;
 #pragma unroll
-            for (int v = 0; v < 5; ++v) lo[v] = dv.lo_buf[v * dv.nd + o] * js;
+            for (int v = 0; v < 5; ++v) lo[v] = dv.lo_buf[v * dv.nd + o];
+            const float* sfa = stSf + cl * 6 * P2;
+#pragma unroll
+            for (int sd = 0; sd < 3; ++sd) {
+#pragma unroll
+                for (int lr = 0; lr < 2; ++lr) {
+                    if (ti[sd] != (lr ? N : 0)) continue;
+                    const int f = 2 * sd + lr;
+                    const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
+                    const float j0 = J[(sd * 3) * NB + node], j1 = J[(sd * 3 + 1) * NB + node], j2 = J[(sd * 3 + 2) * NB + node];
+                    const float sw = __fdividef(sqrtf(j0 * j0 + j1 * j1 + j2 * j2), opW<float>(ops, lr * N));
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) lo[v] += sfa[v * NF + f * P2 + q] * sw;
+                }
+            }
+            const float js = R64 ? 1.0f : __fdividef(-1.0f, detJ);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) lo[v] *= js;
         }
     }
     if (!valid) return;
