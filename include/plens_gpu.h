@@ -275,10 +275,15 @@ int plens_gpu_synchronize(plens_ctx* ctx);
  *    cudaHostRegister) give the overlap; pageable ones give the same results in series.
  *    U_out[j] must not overlap any U_in[k], k > j.
  *  - t_out: NULL or count doubles, member j's clock after its steps.
- *  - On an error the call stops at the failing member (named in plens_gpu_last_error); the
- *    outputs of the members before it are complete. No copy to or from the caller's buffers
- *    outlives the call. The context then holds the state and clock of the last member it
- *    advanced. Device buffers for the two staged states are made on the first call. */
+ *  - Errors: the call returns the status of the first member that failed, named in
+ *    plens_gpu_last_error (positivity: plens_gpu_first_bad_dof gives its dof); the outputs of
+ *    the members before it are complete. With the learned sensor the call stops there (its
+ *    fallback redoes failed steps from the host, so its members run one after the other);
+ *    otherwise every member is advanced (each starts with a clear error state) and the later
+ *    members' outputs are complete as well. No copy to or from the caller's buffers outlives
+ *    the call. The context then holds the state and clock of the last member it advanced.
+ *  - Device buffers for the two staged states and a page-locked status array are made on the
+ *    first call (the array grows with count). */
 int plens_gpu_advance_states(plens_ctx* ctx, int64_t count, const double* const* U_in, double* const* U_out,
                              double t0, int64_t n_steps, double end_time, double* t_out);
 

@@ -76,6 +76,33 @@ static __global__ void k_state_out(Dev dv, double* __restrict__ dst)
         dst[i] = dv.U[i];
 }
 
+// the device scalars into a page-locked, device-mapped host mirror, read by the host once the
+// stream has synchronised: no copy engine is involved, so the read never waits behind bulk
+// host <-> device copies in flight on other streams
+static __global__ void k_scalars_out(Dev dv, Scalars* __restrict__ dst)
+{
+    *dst = *dv.sc;
+    __threadfence_system();
+}
+
+// the outcome of one member of a sequence of states (plens_gpu_advance_states)
+struct MemberStatus {
+    double time;
+    long long n_steps, bad_dof;
+    int err, pad;
+};
+
+// a member's outcome into a page-locked, device-mapped host array (no copy engine involved)
+static __global__ void k_member_status(Dev dv, MemberStatus* __restrict__ dst)
+{
+    const Scalars* s = dv.sc;
+    dst->time = s->time;
+    dst->n_steps = s->n_steps;
+    dst->bad_dof = s->bad_dof;
+    dst->err = s->err;
+    __threadfence_system();
+}
+
 // the clock of the next state of a sequence (plens_gpu_advance_states), on the stream: what
 // plens_gpu_set_time writes from the host
 static __global__ void k_set_clock(Dev dv, double t, long long n_steps)

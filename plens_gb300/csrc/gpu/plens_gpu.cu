@@ -172,6 +172,9 @@ struct plens_ctx {
     double* R[3] = {nullptr, nullptr, nullptr};
     double* Rout = nullptr;
     Scalars* sc = nullptr;
+    // page-locked, device-mapped mirror of the device scalars (k_scalars_out writes it)
+    Scalars* sc_host = nullptr;
+    Scalars* sc_mirror = nullptr;  // its device address
     MlpDevice mlp{};
     int64_t bad_dof_host = -1;
     // volume-kernel timing
@@ -200,6 +203,10 @@ struct plens_ctx {
     cudaStream_t seq_in = nullptr, seq_out = nullptr;
     cudaEvent_t seq_in_ready = nullptr, seq_in_free = nullptr, seq_out_ready = nullptr, seq_out_free = nullptr;
     double *seq_in_buf = nullptr, *seq_out_buf = nullptr;
+    // each member's outcome, in page-locked, device-mapped host memory (grown as needed)
+    MemberStatus* seq_status_host = nullptr;
+    MemberStatus* seq_status_dev = nullptr;
+    int64_t seq_status_cap = 0;
     // error norms of the output steps: rho E of the previous step's start, the quadrature data,
     // per-cell and total sums
     double* rhoE_old = nullptr;
@@ -444,9 +451,24 @@ int launch_step(plens_ctx* c, double end_time, bool judge = true)
     return check_launch(c, "step kernels");
 }
 
+// the device scalars as the stream's work so far leaves them (synchronises the stream)
+int read_scalars(plens_ctx* c, Scalars* h)
+{
+    k_scalars_out<<<1, 1, 0, c->stream>>>(c->dv, c->sc_mirror);
+    c->launches += 1;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "read scalars");
+    *h = *c->sc_host;
+    return 0;
+}
+
 int sync_and_check(plens_ctx* c)
 {
-    cudaError_t e = cudaStreamSynchronize(c->stream);
+    k_scalars_out<<<1, 1, 0, c->stream>>>(c->dv, c->sc_mirror);
+    c->launches += 1;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamSynchronize");
     for (size_t i = 0; i < c->ev_used; ++i) {
         float ms = 0;
@@ -455,9 +477,7 @@ int sync_and_check(plens_ctx* c)
         ++c->vol_n;
     }
     c->ev_used = 0;
-    Scalars h;
-    e = cudaMemcpy(&h, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(c, e, "read scalars");
+    const Scalars h = *c->sc_host;
     if (h.err == PLENS_GPU_E_POSITIVITY) {
         c->bad_dof_host = h.bad_dof;
         char buf[160];
@@ -726,6 +746,8 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         c->mlp.tol = prm->judge_alpha_tol;
     }
     d.sc = c->sc;
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&c->sc_host), sizeof(Scalars), cudaHostAllocMapped));
+    CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&c->sc_mirror), c->sc_host, 0));
     CK(cudaMemset(d.alpha, 0, sizeof(double) * nc));
     CK(cudaMemset(d.alpha_raw, 0, sizeof(double) * nc));
     CK(cudaMemset(d.alpha_d, 0, sizeof(double) * nc));
@@ -768,6 +790,8 @@ int plens_gpu_destroy(plens_ctx* c)
         if (gx) cudaGraphExecDestroy(gx);
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     if (c->snap_host) cudaFreeHost(c->snap_host);
+    if (c->sc_host) cudaFreeHost(c->sc_host);
+    if (c->seq_status_host) cudaFreeHost(c->seq_status_host);
     if (c->snap_dev) cudaFree(c->snap_dev);
     if (c->snap_ready) cudaEventDestroy(c->snap_ready);
     if (c->snap_done) cudaEventDestroy(c->snap_done);
@@ -835,9 +859,8 @@ int plens_gpu_get_state(plens_ctx* c, double* U)
 int plens_gpu_set_time(plens_ctx* c, double t, int64_t n_steps)
 {
     if (!c || !c->sc) return PLENS_GPU_E_INVALID;
-    CK(cudaStreamSynchronize(c->stream));
     Scalars h;
-    CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+    if (int r = read_scalars(c, &h)) return r;
     h.time = t;
     h.n_steps = n_steps;
     h.err = 0;
@@ -849,9 +872,8 @@ int plens_gpu_set_time(plens_ctx* c, double t, int64_t n_steps)
 int plens_gpu_get_time(plens_ctx* c, double* t, int64_t* n_steps, double* last_dt)
 {
     if (!c || !c->sc) return PLENS_GPU_E_INVALID;
-    CK(cudaStreamSynchronize(c->stream));
     Scalars h;
-    CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+    if (int r = read_scalars(c, &h)) return r;
     if (t) *t = h.time;
     if (n_steps) *n_steps = h.n_steps;
     if (last_dt) *last_dt = h.dt;
@@ -882,9 +904,7 @@ int plens_gpu_time_step(plens_ctx* c, double* dt_out)
     c->launches += 1;
     if (int r = launch_time_step(c)) return r;
     if (int r = sync_and_check(c)) return r;
-    Scalars h;
-    CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
-    if (dt_out) *dt_out = h.dt_update;
+    if (dt_out) *dt_out = c->sc_host->dt_update;  // the mirror sync_and_check read
     return 0;
 }
 
@@ -956,52 +976,68 @@ int plens_gpu_synchronize(plens_ctx* c)
     return sync_and_check(c);
 }
 
+}  // extern "C"
+
+namespace {
+
+// The learned sensor's advance: steps are launched in batches; each step first snapshots its
+// start state and clock on the device. A positivity failure deactivates the rest of the batch
+// (k_step_begin), and the failed step is redone from its snapshot with the plain modal indicator
+// on the whole domain (the fallback lasts until the next judged step). `start`: the clock at the
+// call (time and step count) when the caller knows it, which saves reading the device scalars.
+int advance_learned(plens_ctx* c, int64_t n_steps, double end_time, const Scalars* start)
+{
+    constexpr int64_t kBatch = 64;
+    int64_t done = 0;
+    while (done < n_steps) {
+        Scalars h0;
+        if (start && done == 0) {
+            h0 = *start;
+        } else if (int r = read_scalars(c, &h0)) {
+            return r;
+        }
+        if (!(h0.time < end_time)) break;
+        const int64_t nb = std::min<int64_t>(kBatch, n_steps - done);
+        const int counter0 = c->mlp.step_counter;
+        for (int64_t k = 0; k < nb; ++k)
+            if (int r = run_step(c, end_time)) return r;
+        const int r = sync_and_check(c);
+        if (r != PLENS_GPU_E_POSITIVITY) {
+            if (r) return r;
+            done += nb;
+            continue;
+        }
+        Scalars h = *c->sc_host;  // the mirror sync_and_check read
+        if (h.sensor_fallback) return r;  // the plain indicator was in use: report it
+        const int64_t ok_steps = h.n_steps0 - h0.n_steps;  // steps of the batch before the failed one
+        CK(cudaMemcpyAsync(c->dv.U, c->dv.U0, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToDevice, c->stream));
+        if (int r2 = refresh_image(c)) return r2;
+        h.time = h.time0;
+        h.n_steps = h.n_steps0;
+        h.sensor_fallback = 1;
+        h.fallbacks += c->nc;  // every cell handed back for this step
+        h.err = 0;
+        h.bad_dof = INT64_MAX;
+        CK(cudaMemcpy(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice));
+        c->mlp.step_counter = counter0 + (int)ok_steps + 1;
+        c->mlp.judge_this_step = false;
+        if (int r2 = launch_step(c, end_time, false)) return r2;
+        if (int r2 = sync_and_check(c)) return r2;
+        done += ok_steps + 1;
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
 int plens_gpu_advance(plens_ctx* c, int64_t n_steps, double end_time)
 {
     if (c && c->learned) {
-        // Learned sensor: steps are launched in batches; each step first snapshots its start
-        // state and clock on the device. A positivity failure deactivates the rest of the batch
-        // (k_step_begin), and the failed step is redone from its snapshot with the plain modal
-        // indicator on the whole domain (the fallback lasts until the next judged step).
         if (!c->dv.U || n_steps < 0) return PLENS_GPU_E_INVALID;
         if (!c->mlp.weights_set) return fail(c, PLENS_GPU_E_INVALID, "learned sensor: weights not set");
-        constexpr int64_t kBatch = 64;
-        int64_t done = 0;
-        while (done < n_steps) {
-            Scalars h0;
-            CK(cudaStreamSynchronize(c->stream));
-            CK(cudaMemcpy(&h0, c->sc, sizeof(h0), cudaMemcpyDeviceToHost));
-            if (!(h0.time < end_time)) break;
-            const int64_t nb = std::min<int64_t>(kBatch, n_steps - done);
-            const int counter0 = c->mlp.step_counter;
-            for (int64_t k = 0; k < nb; ++k)
-                if (int r = run_step(c, end_time)) return r;
-            const int r = sync_and_check(c);
-            if (r != PLENS_GPU_E_POSITIVITY) {
-                if (r) return r;
-                done += nb;
-                continue;
-            }
-            Scalars h;
-            CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
-            if (h.sensor_fallback) return r;  // the plain indicator was in use: report it
-            const int64_t ok_steps = h.n_steps0 - h0.n_steps;  // steps of the batch before the failed one
-            CK(cudaMemcpyAsync(c->dv.U, c->dv.U0, sizeof(double) * 5 * c->nd, cudaMemcpyDeviceToDevice, c->stream));
-            if (int r2 = refresh_image(c)) return r2;
-            h.time = h.time0;
-            h.n_steps = h.n_steps0;
-            h.sensor_fallback = 1;
-            h.fallbacks += c->nc;  // every cell handed back for this step
-            h.err = 0;
-            h.bad_dof = INT64_MAX;
-            CK(cudaMemcpy(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice));
-            c->mlp.step_counter = counter0 + (int)ok_steps + 1;
-            c->mlp.judge_this_step = false;
-            if (int r2 = launch_step(c, end_time, false)) return r2;
-            if (int r2 = sync_and_check(c)) return r2;
-            done += ok_steps + 1;
-        }
-        return 0;
+        return advance_learned(c, n_steps, end_time, nullptr);
     }
     if (int r = plens_gpu_advance_async(c, n_steps, end_time)) return r;
     return sync_and_check(c);
@@ -1025,11 +1061,27 @@ int sequence_setup(plens_ctx* c)
     return 0;
 }
 
+// room for `count` member outcomes
+int sequence_status(plens_ctx* c, int64_t count)
+{
+    if (count <= c->seq_status_cap) return 0;
+    if (c->seq_status_host) cudaFreeHost(c->seq_status_host);
+    c->seq_status_host = nullptr;
+    c->seq_status_cap = 0;
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&c->seq_status_host), sizeof(MemberStatus) * count, cudaHostAllocMapped));
+    CK(cudaHostGetDevicePointer(reinterpret_cast<void**>(&c->seq_status_dev), c->seq_status_host, 0));
+    c->seq_status_cap = count;
+    return 0;
+}
+
 // one member of a sequence: its state (staged in seq_in_buf) made current at time t0, its steps,
 // its state copied to seq_out_buf and from there to the host on seq_out; the next member's copy
-// into seq_in_buf is issued as soon as this member's state has left that buffer
+// into seq_in_buf is issued as soon as this member's state has left that buffer. Without the
+// learned sensor nothing here waits for the GPU: the member's outcome goes to the mapped status
+// array and the host goes on to enqueue the next member. The learned sensor's positivity
+// fallback redoes a failed step from the host, so its members run one after the other.
 int sequence_member(plens_ctx* c, int64_t j, int64_t count, const double* const* U_in, double* const* U_out,
-                    double t0, int64_t n_steps, double end_time, double* t_out)
+                    double t0, int64_t n_steps, double end_time)
 {
     const size_t bytes = sizeof(double) * 5 * c->nd;
     const unsigned grid = (unsigned)std::min<int64_t>((5 * c->nd + 255) / 256, 152 * 16);
@@ -1044,8 +1096,19 @@ int sequence_member(plens_ctx* c, int64_t j, int64_t count, const double* const*
         CK(cudaMemcpyAsync(c->seq_in_buf, U_in[j + 1], bytes, cudaMemcpyHostToDevice, c->seq_in));
         CK(cudaEventRecord(c->seq_in_ready, c->seq_in));
     }
-    if (int r = plens_gpu_advance(c, n_steps, end_time)) return r;
-    if (t_out) CK(cudaMemcpy(&t_out[j], &c->sc->time, sizeof(double), cudaMemcpyDeviceToHost));
+    if (c->learned) {
+        Scalars s0{};
+        s0.time = t0;
+        s0.n_steps = 0;
+        if (int r = advance_learned(c, n_steps, end_time, &s0)) return r;
+        const Scalars& h = *c->sc_host;  // synchronised: the mirror holds this member's clock
+        c->seq_status_host[j] = MemberStatus{h.time, h.n_steps, h.bad_dof, 0, 0};
+    } else {
+        if (int r = plens_gpu_advance_async(c, n_steps, end_time)) return r;
+        k_member_status<<<1, 1, 0, c->stream>>>(c->dv, c->seq_status_dev + j);
+        c->launches += 1;
+        if (int r = check_launch(c, "member status")) return r;
+    }
     // the previous member's copy out must have left seq_out_buf
     CK(cudaStreamWaitEvent(c->stream, c->seq_out_free, 0));
     CK(cudaMemcpyAsync(c->seq_out_buf, c->dv.U, bytes, cudaMemcpyDeviceToDevice, c->stream));
@@ -1070,6 +1133,7 @@ int plens_gpu_advance_states(plens_ctx* c, int64_t count, const double* const* U
             return fail(c, PLENS_GPU_E_INVALID, "advance_states: null state buffer of member " + std::to_string(j));
     if (c->learned && !c->mlp.weights_set) return fail(c, PLENS_GPU_E_INVALID, "learned sensor: weights not set");
     if (int r = sequence_setup(c)) return r;
+    if (int r = sequence_status(c, count)) return r;
     int r = 0;
     {
         const cudaError_t e = cudaMemcpyAsync(c->seq_in_buf, U_in[0], sizeof(double) * 5 * c->nd,
@@ -1081,16 +1145,29 @@ int plens_gpu_advance_states(plens_ctx* c, int64_t count, const double* const* U
         }
     }
     int64_t j = 0;
-    for (; j < count && !r; ++j) r = sequence_member(c, j, count, U_in, U_out, t0, n_steps, end_time, t_out);
+    for (; j < count && !r; ++j) r = sequence_member(c, j, count, U_in, U_out, t0, n_steps, end_time);
     // no copy into or out of the caller's buffers outlives the call
+    const cudaError_t es = cudaStreamSynchronize(c->stream);
     const cudaError_t ei = cudaStreamSynchronize(c->seq_in);
     const cudaError_t eo = cudaStreamSynchronize(c->seq_out);
     if (r) {
         c->err = "advance_states: member " + std::to_string(j - 1) + ": " + c->err;
         return r;
     }
+    if (es != cudaSuccess) return cuda_fail(c, es, "advance_states: steps");
     if (ei != cudaSuccess) return cuda_fail(c, ei, "advance_states: copy in");
     if (eo != cudaSuccess) return cuda_fail(c, eo, "advance_states: copy out");
+    for (int64_t k = 0; k < count; ++k) {
+        const MemberStatus m = c->seq_status_host[k];
+        if (m.err == PLENS_GPU_E_POSITIVITY) {
+            c->bad_dof_host = m.bad_dof;
+            return fail(c, PLENS_GPU_E_POSITIVITY, "advance_states: member " + std::to_string(k) +
+                                                       ": Positivity assertion failed at dof " + std::to_string(m.bad_dof));
+        }
+        if (m.err) return fail(c, m.err, "advance_states: member " + std::to_string(k) + ": device error " + std::to_string(m.err));
+    }
+    if (t_out)
+        for (int64_t k = 0; k < count; ++k) t_out[k] = c->seq_status_host[k].time;
     return 0;
 }
 
@@ -1135,7 +1212,7 @@ int plens_gpu_get_cell_scalars(plens_ctx* c, double* alpha, double* alpha_d, dou
         CK(cudaMemcpy(dt_cell, c->dv.dt_loc, sizeof(double) * c->nc, cudaMemcpyDeviceToHost));
     } else if (dt_cell) {
         Scalars h;
-        CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+        if (int r = read_scalars(c, &h)) return r;
         for (int64_t i = 0; i < c->nc; ++i) dt_cell[i] = h.dt_update;
     }
     return 0;
@@ -1318,9 +1395,8 @@ int plens_gpu_set_sensor_weights(plens_ctx* c, const float* params)
 int plens_gpu_sensor_stats(plens_ctx* c, int64_t* judged, int64_t* fallbacks, double* max_alpha_err, int64_t* lo_cells)
 {
     if (!c) return PLENS_GPU_E_INVALID;
-    CK(cudaStreamSynchronize(c->stream));
     Scalars h;
-    CK(cudaMemcpy(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost));
+    if (int r = read_scalars(c, &h)) return r;
     if (judged) *judged = h.judged;
     if (fallbacks) *fallbacks = h.fallbacks;
     if (max_alpha_err) *max_alpha_err = h.max_alpha_err;

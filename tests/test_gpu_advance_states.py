@@ -87,18 +87,29 @@ def test_sequence_matches_the_serial_loop(prec, sensor, pinned):
     assert list(t2) == ref_t[:2]
 
 
-def test_failing_member_is_named_and_earlier_outputs_are_complete():
-    case = make(configs.dmr(nx=24, ny=6))
+@pytest.mark.parametrize("sensor", ["modal", "learned"])
+def test_failing_member_is_named_and_earlier_outputs_are_complete(sensor):
+    """Member 1 has a negative density: the call reports member 1 and its dof (the first stage's
+    positivity assertion; no later stage moves the state on). Member 0 is complete; without the
+    learned sensor every member is advanced, so member 2 is complete too, while the learned
+    sensor's sequence stops at the failure."""
+    case = make(configs.dmr(nx=24, ny=6, precision="mixed", sensor=sensor))
+    weights = _weights() if sensor == "learned" else None
     members = _members(case, 3)
     bad = members[1].copy()
-    bad[0, 77] = -1.0  # negative density: the positivity assertion of the first stage
+    bad[0, 77] = -1.0
     members[1] = bad
-    ref, _ = _serial(case, members[:1], 2)
+    ref, _ = _serial(case, [members[0], members[2]], 2, weights)
     U_out = [np.full_like(m, np.nan) for m in members]
     g = GpuSolver(case)
+    if weights is not None:
+        g.set_sensor_weights(weights)
     with pytest.raises(PositivityError) as ei:
         g.advance_states(members, U_out, T0, 2)
     assert "member 1" in str(ei.value)
     assert ei.value.dof == 77
     assert np.array_equal(U_out[0], ref[0])
-    assert np.isnan(U_out[2]).all()
+    if sensor == "learned":
+        assert np.isnan(U_out[2]).all()
+    else:
+        assert np.array_equal(U_out[2], ref[1])
