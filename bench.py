@@ -253,7 +253,8 @@ def _form_case(workload: str, precision: str, sensor: str, cache: dict | None = 
 
 
 def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_index: int, weights=None,
-                 workload: str = "dmr", cache: dict | None = None, tensor_cores: bool = False, e2e: bool = True):
+                 workload: str = "dmr", cache: dict | None = None, tensor_cores: bool = False, e2e: bool = True,
+                 indicator_tc: bool | None = None):
     import torch
 
     from plens_gb300.api import GpuSolver
@@ -264,6 +265,8 @@ def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_in
     if sensor == "learned":
         g.set_sensor_weights(weights)
         g.set_sensor_tensor_cores(tensor_cores)
+    elif indicator_tc is not None:
+        g.set_indicator_tensor_cores(indicator_tc)
     g.set_state(U0, 0.0)
     g.advance(warmup)
     stream = torch.cuda.ExternalStream(g.stream, device=torch.device("cuda", device_index))
@@ -558,10 +561,12 @@ def run_single_form(args):
     torch.cuda.set_device(0)
     prec, sensor = FORMS[args.form]
     r = measure_form(prec, sensor, args.steps, args.warmup, 0, _sensor_weights() if sensor == "learned" else None,
-                     tensor_cores=args.sensor_tensor_cores, e2e=False)
+                     tensor_cores=args.sensor_tensor_cores, e2e=False,
+                     indicator_tc=False if args.indicator_cuda_cores else None)
     nd = r["case"].n_dofs
     vol = r["vol_ms"] / max(r["vol_n"], 1)
     print(json.dumps({"form": args.form, "precision": prec, "sensor": sensor, "steps": args.steps,
+                      "indicator_cuda_cores": args.indicator_cuda_cores,
                       "ms_per_step": r["ms"] / args.steps, "dof_stage_per_s": nd * 5 * args.steps / (r["ms"] / 1e3),
                       "volume_kernel_ms": vol, "gpu_launches": r["launches"], "clocks": r["clocks"],
                       "sensor_stats": r["stats"]}), flush=True)
@@ -580,6 +585,9 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=0, help="override the accuracy window (steps)")
     ap.add_argument("--sensor-tensor-cores", action="store_true",
                     help="the learned sensor's hidden layers on the tensor cores (tcgen05, 3xTF32)")
+    ap.add_argument("--indicator-cuda-cores", action="store_true",
+                    help="the modal indicator's change of basis on the CUDA cores (mixed forms, degree 3; "
+                         "the default there is the tensor-core form)")
     ap.add_argument("--horizon", default="", help="comma-separated DMR z variants: " + ",".join(HORIZON_VARIANTS))
     ap.add_argument("--horizon-precision", default="mixed", choices=["fp64", "mixed", "mixed_r32"])
     ap.add_argument("--form", default="", choices=["", "plain", "modal", "learned", "modal_r32", "learned_r32"],

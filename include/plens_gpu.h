@@ -311,6 +311,12 @@ int plens_gpu_get_avars(plens_ctx* ctx, double* avars);
  * or on the CUDA cores (enable = 0, the default: faster on the measured workloads). No reference
  * counterpart. */
 int plens_gpu_set_sensor_tensor_cores(plens_ctx* ctx, int enable);
+/* Modal indicator of a mixed-precision context of degree 3 (the blender's change of basis,
+ * dgsem/blender_calculator.cc:123-177 with dgsem/change_of_basis_matrix.h:74-98): the 64 x 64
+ * change of basis of 128 cells at a time on the tensor cores (tcgen05, 3xTF32) when enable != 0
+ * -- the default, measured faster -- else the separable transform on the CUDA cores.
+ * PLENS_GPU_E_INVALID for other contexts. */
+int plens_gpu_set_indicator_tensor_cores(plens_ctx* ctx, int enable);
 /* Asynchronous snapshot for data output (replaces the host reads of PLENS::write,
  * dgsem/plens.cc:4170-4322): _begin copies U, alpha, alpha_d, the auxiliary variables (viscous)
  * and the clock on the context's stream into a device buffer, then to library-owned pinned host

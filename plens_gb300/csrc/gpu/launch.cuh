@@ -2,6 +2,7 @@
 // (P, arithmetic type) so the context can dispatch on the run-time degree and precision.
 #pragma once
 
+#include "blender_tc.cuh"
 #include "kernels.cuh"
 #include "subcell_mx.cuh"
 #include "surface_mx.cuh"
@@ -13,6 +14,9 @@ struct LaunchTable {
     int P = 0;
     // each returns the number of kernels it launched
     int (*blender)(const Dev&, const Ops&, const GasP&, const BlendP&, cudaStream_t) = nullptr;
+    // the mixed forms' modal indicator with the change of basis on the tensor cores (N = 3 only;
+    // blender_tc.cuh), given its B operand
+    int (*blender_tc)(const Dev&, const Ops&, const GasP&, const BlendP&, const float*, cudaStream_t) = nullptr;
     int (*surface)(int stage, const Dev&, const GasP&, double* out, cudaStream_t) = nullptr;
     int (*aux)(const Dev&, const Ops&, const GasP&, cudaStream_t) = nullptr;
     int (*volume)(bool visc, const Dev&, const Ops&, const GasP&, const StageArgs&, cudaStream_t) = nullptr;
@@ -34,6 +38,20 @@ struct Launch {
     static int blender(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, cudaStream_t st)
     {
         k_blender<P, T><<<grid_cells(dv.nc), CB::THREADS, 0, st>>>(dv, ops, g, bp);
+        return 1;
+    }
+    static int blender_tc(const Dev& dv, const Ops& ops, const GasP& g, const BlendP& bp, const float* Btc, cudaStream_t st)
+    {
+        static int nsm = 0;
+        if (!nsm) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            cudaFuncSetAttribute(k_blender_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BtcSmem::bytes);
+            if (nsm < 1) nsm = 1;
+        }
+        const int64_t tiles = (dv.nc + tc::kRows - 1) / tc::kRows;
+        k_blender_tc<P><<<(unsigned)(tiles < nsm ? tiles : nsm), kBtcThreads, BtcSmem::bytes, st>>>(dv, Btc, g, bp, ops);
         return 1;
     }
     template <bool HLLC>
@@ -128,20 +146,26 @@ struct Launch {
     {
         return sizeof(T) == 4 && P % 2 == 0 && g.ivf == PLENS_IVF_CHANDRASHEKHAR;
     }
-    static int subcell(const Dev& dv, const Ops& ops, const GasP& g, cudaStream_t st)
+    template <bool HLLC>
+    static void subcell_launch(const Dev& dv, const Ops& ops, const GasP& g, cudaStream_t st)
     {
-        if (!uses_lo_list(g)) return 0;
-        // persistent grid: the resident blocks take the listed cells in groups
+        // persistent grid, at most two blocks per SM: the blocks take the listed cells in groups
         static int blocks = 0;
         if (!blocks) {
             int dev = 0, nsm = 0, occ = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_subcell_lo<P>, CB::THREADS, 0);
-            blocks = (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_subcell_lo<P, HLLC>, CB::THREADS, 0);
+            blocks = (occ > 2 ? 2 : (occ > 0 ? occ : 1)) * (nsm > 0 ? nsm : 1);
         }
         const int64_t need = (dv.nc + CB::CPB - 1) / CB::CPB;
-        k_subcell_lo<P><<<(int)(need < blocks ? need : blocks), CB::THREADS, 0, st>>>(dv, ops, g);
+        k_subcell_lo<P, HLLC><<<(int)(need < blocks ? need : blocks), CB::THREADS, 0, st>>>(dv, ops, g);
+    }
+    static int subcell(const Dev& dv, const Ops& ops, const GasP& g, cudaStream_t st)
+    {
+        if (!uses_lo_list(g)) return 0;
+        if (g.isf == PLENS_ISF_HLLC) subcell_launch<true>(dv, ops, g, st);
+        else subcell_launch<false>(dv, ops, g, st);
         return 1;
     }
     static int time_step(const Dev& dv, const GasP& g, double N15, int N, cudaStream_t st)
@@ -160,6 +184,7 @@ struct Launch {
         LaunchTable t;
         t.P = P;
         t.blender = &blender;
+        if constexpr (sizeof(T) == 4 && P == 4) t.blender_tc = &blender_tc;
         t.surface = &surface;
         t.aux = &aux;
         t.volume = &volume;

@@ -144,6 +144,10 @@ struct plens_ctx {
     int64_t nc = 0, nd = 0, ntask = 0, nslot = 0;
     bool viscous = false, mixed = false, learned = false;
     bool reg64 = false;  // MIXED form: FP64 RK registers, metric terms read in FP64
+    // mixed forms at N = 3: the modal indicator's change of basis on the tensor cores (the B
+    // operand, made at creation) while indicator_tc is set (the default with the modal sensor)
+    float* cbm_tc = nullptr;
+    bool indicator_tc = false;
     plens_params prm{};
     Dev dv{};
     Ops ops{};
@@ -301,7 +305,8 @@ int launch_rhs(plens_ctx* c, const StageArgs& sa)
     if (c->learned) {
         c->launches += mlp_sensor_launch(c->mlp, c->dv, c->ops, c->gas, c->bp, c->P, c->side);
     } else {
-        c->launches += c->tab.blender(c->dv, c->ops, c->gas, c->bp, c->side);
+        if (c->indicator_tc) c->launches += c->tab.blender_tc(c->dv, c->ops, c->gas, c->bp, c->cbm_tc, c->side);
+        else c->launches += c->tab.blender(c->dv, c->ops, c->gas, c->bp, c->side);
         k_alpha_smooth<<<(unsigned)((c->nc + kSmoothThreads - 1) / kSmoothThreads), kSmoothThreads, 0, c->side>>>(c->dv, c->bp);
         ++c->launches;
     }
@@ -698,6 +703,15 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         d.detJf = detJf;
         d.Jaf = Jaf;
         d.Jinvf = Jinvf;
+    }
+    if (c->tab.blender_tc) {
+        // the B operand of the tensor-core modal indicator (64 x 64 change of basis, TF32 hi/lo)
+        std::vector<float> op(2 * 64 * 64);
+        blender_tc_operand(c->ops.C1, op.data());
+        if ((r = dalloc(c, &c->cbm_tc, op.size()))) return r;
+        CK(cudaMemcpy(c->cbm_tc, op.data(), sizeof(float) * op.size(), cudaMemcpyHostToDevice));
+        // the default where it applies: measured faster than the separable CUDA-core transform
+        c->indicator_tc = !c->learned;
     }
     if ((r = dalloc(c, &d.U, 5 * nd)) || (r = dalloc(c, &d.alpha_raw, nc)) || (r = dalloc(c, &d.alpha, nc)) ||
         (r = dalloc(c, &d.alpha_d, nc)) || (r = dalloc(c, &d.sf, 5 * c->nslot)) || (r = dalloc(c, &c->sc, 1)) ||
@@ -1313,6 +1327,21 @@ int plens_gpu_set_sensor_tensor_cores(plens_ctx* c, int enable)
     if (!c->learned) return fail(c, PLENS_GPU_E_INVALID, "context was created without the learned sensor");
     if (int r = sync_and_check(c)) return r;
     c->mlp.use_tc = enable != 0;
+    for (auto& gx : c->step_graph)  // the step's launch sequence changed
+        if (gx) {
+            cudaGraphExecDestroy(gx);
+            gx = nullptr;
+        }
+    return 0;
+}
+
+int plens_gpu_set_indicator_tensor_cores(plens_ctx* c, int enable)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    if (!c->cbm_tc) return fail(c, PLENS_GPU_E_INVALID, "the tensor-core modal indicator needs a mixed-precision context of degree 3");
+    if (c->learned) return fail(c, PLENS_GPU_E_INVALID, "context uses the learned sensor, not the modal indicator");
+    if (int r = sync_and_check(c)) return r;
+    c->indicator_tc = enable != 0;
     for (auto& gx : c->step_graph)  // the step's launch sequence changed
         if (gx) {
             cudaGraphExecDestroy(gx);

@@ -66,8 +66,13 @@ static __global__ void __launch_bounds__(kSmoothThreads) k_lo_list(Dev dv)
 // Interior subcell sums of the listed cells, CPB cells per block, one thread per GLL node; line
 // tasks numbered flat over the block's cells (3 P^2 per cell), each running the P - 1 subcell
 // interfaces of one line. The grid is persistent: blocks take groups of CPB listed cells with a
-// stride, up to the count the list kernel wrote.
-template <int P>
+// stride, up to the count the list kernel wrote. The kernel is latency-bound (a few hundred
+// listed cells, one chain of dependent loads per group): the count and the group's list entries
+// are loaded together (entries past the count are not used), HLLC -- whose subcell flux does not
+// read alpha -- has an instantiation of its own without the alpha load or the scheme switch (a
+// smaller code path to fetch), and the launcher caps the grid at two blocks per SM so that blocks
+// take several groups with their code already fetched.
+template <int P, bool HLLC>
 __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Ops ops, GasP g)
 {
     using CB = CellBlock<P>;
@@ -80,17 +85,23 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
     __shared__ int32_t sCell[CPB];
     Scalars* s = dv.sc;
     if (!s->active) return;
-    const int n = *dv.lo_count;
     const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
     const float gm = f64_to_f32(g.gamma);
-    for (int grp = blockIdx.x; grp * CPB < n; grp += gridDim.x) {
+    for (int grp = blockIdx.x;; grp += gridDim.x) {
         const int p0 = grp * CPB;
-        const int ncb = (n - p0 < CPB) ? n - p0 : CPB;
         if (tid < CPB) {
-            sCell[tid] = (tid < ncb) ? dv.lo_list[p0 + tid] : -1;
-            sAl[tid] = (tid < ncb) ? f64_to_f32(dv.alpha[dv.lo_list[p0 + tid]]) : 0.0f;
+            const int n = *dv.lo_count;
+            const int32_t c = (p0 + tid < dv.nc) ? dv.lo_list[p0 + tid] : -1;  // loaded beside the count
+            sCell[tid] = (p0 + tid < n) ? c : -1;
+            if (!HLLC) sAl[tid] = (p0 + tid < n) ? f64_to_f32(dv.alpha[c]) : 0.0f;
         }
         __syncthreads();
+        if (sCell[0] < 0) break;  // the list ends before this group (the same for the whole block)
+        const int ncb = (CPB == 1 || sCell[CPB - 1] >= 0) ? CPB : [&] {
+            int k = 1;
+            while (k < CPB && sCell[k] >= 0) ++k;
+            return k;
+        }();
         if (cl < ncb) {
             const int64_t cell = sCell[cl];
             const int64_t dof = cell * P3 + node;
@@ -102,8 +113,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
         __syncthreads();
         for (int ft = tid; ft < ncb * TPC; ft += CB::THREADS) {
             const int tc = ft / TPC, task = ft - tc * TPC;
-            const float at = sAl[tc];
-            const float fb = (at <= 0.0f) ? 0.0f : (at <= 1.0f ? at : 1.0f);  // the cell's alpha as flux blender (plens.cc:3492)
+            float fb = 0.0f;
+            if (!HLLC) {
+                const float at = sAl[tc];
+                fb = (at <= 0.0f) ? 0.0f : (at <= 1.0f ? at : 1.0f);  // the cell's alpha as flux blender (plens.cc:3492)
+            }
             const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
             const int base = tc * P3;
             float acc[P][5];
@@ -129,7 +143,8 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
                 const float cL[5] = {sC[0][nl], sC[1][nl], sC[2][nl], sC[3][nl], sC[4][nl]};
                 const float cR[5] = {sC[0][nr], sC[1][nr], sC[2][nr], sC[3][nr], sC[4][nr]};
                 float F[5];
-                inv_surf_flux_mx(cL, cR, dn, gm, g.isf, fb, F);
+                if (HLLC) hllc_n_f32(cL, cR, dn, gm, F);
+                else inv_surf_flux_mx(cL, cR, dn, gm, g.isf, fb, F);
                 const float wl = __fdividef(nn, opW<float>(ops, id - 1)), wr = __fdividef(nn, opW<float>(ops, id));
 #pragma unroll
                 for (int v = 0; v < 5; ++v) {
