@@ -253,7 +253,7 @@ def _form_case(workload: str, precision: str, sensor: str, cache: dict | None = 
 
 
 def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_index: int, weights=None,
-                 workload: str = "dmr", cache: dict | None = None, tensor_cores: bool = False, e2e: bool = True,
+                 workload: str = "dmr", cache: dict | None = None, tensor_cores: bool | None = None, e2e: bool = True,
                  indicator_tc: bool | None = None):
     import torch
 
@@ -264,7 +264,8 @@ def measure_form(precision: str, sensor: str, steps: int, warmup: int, device_in
     g = GpuSolver(case)
     if sensor == "learned":
         g.set_sensor_weights(weights)
-        g.set_sensor_tensor_cores(tensor_cores)
+        if tensor_cores is not None:
+            g.set_sensor_tensor_cores(tensor_cores)
     elif indicator_tc is not None:
         g.set_indicator_tensor_cores(indicator_tc)
     g.set_state(U0, 0.0)
@@ -561,7 +562,7 @@ def run_single_form(args):
     torch.cuda.set_device(0)
     prec, sensor = FORMS[args.form]
     r = measure_form(prec, sensor, args.steps, args.warmup, 0, _sensor_weights() if sensor == "learned" else None,
-                     tensor_cores=args.sensor_tensor_cores, e2e=False,
+                     tensor_cores=False if args.sensor_cuda_cores else None, e2e=False,
                      indicator_tc=False if args.indicator_cuda_cores else None)
     nd = r["case"].n_dofs
     vol = r["vol_ms"] / max(r["vol_n"], 1)
@@ -583,8 +584,9 @@ def main():
                     help="per-configuration report (throughput of every form, accuracy after --accuracy-steps) "
                          "instead of the benchmark line")
     ap.add_argument("--accuracy-steps", type=int, default=0, help="override the accuracy window (steps)")
-    ap.add_argument("--sensor-tensor-cores", action="store_true",
-                    help="the learned sensor's hidden layers on the tensor cores (tcgen05, 3xTF32)")
+    ap.add_argument("--sensor-cuda-cores", action="store_true",
+                    help="the learned sensor's network on the CUDA cores (the default at degree 3 is the fused "
+                         "tensor-core kernel)")
     ap.add_argument("--indicator-cuda-cores", action="store_true",
                     help="the modal indicator's change of basis on the CUDA cores (mixed forms, degree 3; "
                          "the default there is the tensor-core form)")
@@ -630,10 +632,10 @@ def main():
     plain = measure_form("fp64", "modal", args.steps, args.warmup, device.index, cache=cache)
     modal = measure_form("mixed", "modal", args.steps, args.warmup, device.index, cache=cache)
     learned = (measure_form("mixed", "learned", args.steps, args.warmup, device.index, weights, cache=cache,
-                            tensor_cores=args.sensor_tensor_cores)
+                            tensor_cores=False if args.sensor_cuda_cores else None)
                if weights is not None else None)
     learned_r32 = (measure_form("mixed_r32", "learned", args.steps, args.warmup, device.index, weights, cache=cache,
-                                tensor_cores=args.sensor_tensor_cores)
+                                tensor_cores=False if args.sensor_cuda_cores else None)
                    if weights is not None else None)
     fast = learned if learned is not None else modal
     fast_sensor = "learned" if learned is not None else "modal"
@@ -680,7 +682,8 @@ def main():
                  "RK registers and their accumulation",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": f"mixed FP32 + {fast_sensor} sensor"
-                   + (" (network on tensor cores)" if args.sensor_tensor_cores and learned is not None else ""),
+                   + (" (network on the CUDA cores)" if args.sensor_cuda_cores and learned is not None else
+                      " (fused tensor-core sensor and modal indicator)"),
                    "l2": "working set per step > L2 (state, 3 registers, metrics, face buffers ~ 0.5 GB)",
                    "parallelism": f"replicas x{ws}"},
         "forms": {

@@ -308,8 +308,10 @@ int plens_gpu_get_cell_scalars(plens_ctx* ctx, double* alpha, double* alpha_d, d
 /* Auxiliary variables of the last viscous RHS ([9][ndof]): PLENS::gcrk_avars. */
 int plens_gpu_get_avars(plens_ctx* ctx, double* avars);
 /* Learned sensor: evaluate the network's two hidden layers on the tensor cores (tcgen05, 3xTF32)
- * or on the CUDA cores (enable = 0, the default: faster on the measured workloads). No reference
- * counterpart. */
+ * or on the CUDA cores (enable = 0). At degree 3 the tensor-core form is one fused kernel (the
+ * features, both layers and the judge's plain indicator for handed-back cells) and the default,
+ * measured faster; at other degrees it is a two-kernel form and the CUDA cores are the default.
+ * No reference counterpart. */
 int plens_gpu_set_sensor_tensor_cores(plens_ctx* ctx, int enable);
 /* Modal indicator of a mixed-precision context of degree 3 (the blender's change of basis,
  * dgsem/blender_calculator.cc:123-177 with dgsem/change_of_basis_matrix.h:74-98): the 64 x 64

@@ -248,11 +248,13 @@ __global__ void __launch_bounds__(kBtcThreads, 1) k_blender_tc(Dev dv, const flo
 
 // The B operand of k_blender_tc on the host: C[mode][node] = C1[mi][ni] C1[mj][nj] C1[mk][nk]
 // (mode = mi + 4 mj + 16 mk, node likewise) in FP64, rounded to FP32 and split into TF32 hi/lo,
-// in the canonical K-major layout.
+// in the canonical K-major layout; then C's row sums (the modal coefficients of the constant 1),
+// 2 x 64 x 64 + 64 floats in all.
 inline void blender_tc_operand(const double* C1, float* out)
 {
     constexpr int P = 4;
-    for (int n = 0; n < 64; ++n)
+    for (int n = 0; n < 64; ++n) {
+        double rs = 0;
         for (int k = 0; k < 64; ++k) {
             const int mi = n % P, mj = (n / P) % P, mk = n / (P * P);
             const int ni = k % P, nj = (k / P) % P, nk = k / (P * P);
@@ -260,7 +262,10 @@ inline void blender_tc_operand(const double* C1, float* out)
             const float hi = tc::tf32_hi(x);
             out[tc::core_off(n, k)] = hi;
             out[64 * 64 + tc::core_off(n, k)] = x - hi;
+            rs += x;
         }
+        out[2 * 64 * 64 + n] = (float)rs;
+    }
 }
 
 }  // namespace plens_gpu

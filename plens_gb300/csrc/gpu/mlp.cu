@@ -8,6 +8,7 @@
 #include <random>
 #include <vector>
 
+#include "blender_tc.cuh"
 #include "kernels.cuh"
 #include "mlp.cuh"
 #include "mlp_tc.cuh"
@@ -647,6 +648,288 @@ __global__ void k_features(Dev dv, GasP g, Interp ip, float* x)
     }
 }
 
+// The learned sensor at N = 3 in one kernel with the network and the judge's plain indicator on
+// the tensor cores: one 128-cell tile per SM, 16 warps.
+//  - The tile's FP32 state is staged in two halves of 64 cells (five bulk copies each); thread t
+//    takes node t % 64 of cells 8 i + t / 64, forms rho*p with the positivity assertion, and the
+//    cell's 64 values are normalised by their mean (the features of interp_normalise at P = 4,
+//    where the interpolation to the 4^3 nodes is the identity).
+//  - The features, split into TF32 hi/lo parts, are the A operand (K-major, K stride padded to 144
+//    bytes: no bank conflicts); tcgen05.mma in 3xTF32 form computes layer 1 (B = W1) and, for the
+//    cells the judge handed back, the change of basis of the features (B = C1 (x) C1 (x) C1; the
+//    modal coefficients of rho*p are the mean times those plus C's row sums, and the indicator's
+//    energy ratios do not depend on the mean).
+//  - Warp w reads rows 32 (w % 4) .. + 31 and 16 columns 16 (w / 4) .. + 15 of each accumulator:
+//    bias + GELU become layer 2's A operand, the modal energies are summed per cell; after layer 2
+//    (B = W2) the warps sum their columns' share of the output layer; the first 128 threads
+//    finish their cell: sigmoid x alpha_max, the cut, the plain indicator where the judge handed
+//    the cell back, the wall override.
+struct SensorTcSmem {
+    static constexpr int kW = kTcParams;                        // W1 hi/lo, W2 hi/lo, b1, b2, w3, b3
+    static constexpr int kC = 2 * 64 * 64 + 64;                 // C hi/lo and C's row sums
+    static constexpr int kHalf = 5 * 64 * 64;                   // staged state of 64 cells (floats)
+    static constexpr size_t oW = 0, oC = (kW + 31) / 32 * 32, oS = oC + (kC + 31) / 32 * 32;
+    static constexpr int kOp = 2 * BtcSmem::kA;                 // an operand pair (hi, lo), padded layout
+    static constexpr int kS = (kHalf > kOp ? kHalf : kOp);      // staging, then A, then H
+    static constexpr size_t bytes = sizeof(float) * (oS + kS);
+};
+
+template <int P>
+__global__ void __launch_bounds__(kBtcThreads, 1) k_sensor_tc(Dev dv, const float* __restrict__ Wtc,
+                                                              const float* __restrict__ Ctc, BlendP bp, GasP g,
+                                                              double* out, int gated, const uint8_t* mask)
+{
+    static_assert(P == 4, "the fused tensor-core sensor takes the 4^3 nodes of degree 3 as its inputs");
+    constexpr int N = 3, P3 = 64, R = tc::kRows;
+    extern __shared__ __align__(128) float smem_stc[];
+    __shared__ __align__(8) uint64_t bar_ld, bar_mma;
+    __shared__ uint32_t tmem_base;
+    __shared__ float s_half[R][2], s_mean[R];
+    __shared__ float s_e[4][3][R], s_z[4][R];
+    float* sW = smem_stc + SensorTcSmem::oW;
+    const float* W1hi = sW;
+    const float* W1lo = sW + 4096;
+    const float* W2hi = sW + 2 * 4096;
+    const float* W2lo = sW + 3 * 4096;
+    const float* b1 = sW + 4 * 4096;
+    const float* b2 = b1 + 64;
+    const float* w3 = b2 + 64;
+    float* sC = smem_stc + SensorTcSmem::oC;
+    const float* Chi = sC;
+    const float* Clo = sC + 4096;
+    const float* Crow = sC + 8192;
+    float* sS = smem_stc + SensorTcSmem::oS;  // [5][64][64] staging, then A hi/lo, then H hi/lo
+    float* sOhi = sS;
+    float* sOlo = sS + BtcSmem::kA;
+    Scalars* s = dv.sc;
+    if (!s->active) return;
+    if (gated && s->sensor_fallback) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t ntiles = (dv.nc + R - 1) / R;
+    const float gm = f64_to_f32(g.gamma);
+    const float cut = fmaxf(f64_to_f32(bp.amin), kLearnedCut), amax = f64_to_f32(bp.amax);
+    constexpr uint32_t kCols = 256;  // three 64-column accumulators
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::s_addr(&tmem_base)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(&bar_ld, 1);
+        mbar_init(&bar_mma, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_base;
+    uint32_t ph_ld = 0, ph_mma = 0;
+    bool ok = true, first = true, mma_out = false;
+    auto wait = [&](uint64_t* bar, uint32_t& ph) {
+        bool done = false;
+        for (int it = 0; it < (1 << 22) && !done; ++it) done = mbar_try_wait(bar, ph);
+        ok = __syncthreads_and(done ? 1 : 0) != 0;
+        if (ok) ph ^= 1;
+    };
+    const int node = tid & 63, q = warp & 3, cg = warp >> 2;
+    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int64_t c0 = tile * R;
+        const int ncell = (int)((dv.nc - c0 < R) ? dv.nc - c0 : R);
+        float v[16];
+        // ---- two halves of 64 cells: stage, rho*p, the per-cell sums
+        for (int h = 0; h < 2 && ok; ++h) {
+            const int nh = ncell - 64 * h < 64 ? (ncell - 64 * h > 0 ? ncell - 64 * h : 0) : 64;
+            if (tid == 0) {
+                const uint32_t bv = (uint32_t)(nh * P3 * 4);
+                mbar_arrive_expect_tx(&bar_ld, 5 * bv + (first ? (uint32_t)(SensorTcSmem::kW * 4 + SensorTcSmem::kC * 4) : 0u));
+                if (first) {
+                    tma_load_1d(sW, Wtc, (uint32_t)(SensorTcSmem::kW * 4), &bar_ld);
+                    tma_load_1d(sC, Ctc, (uint32_t)(SensorTcSmem::kC * 4), &bar_ld);
+                }
+                if (nh > 0)
+#pragma unroll
+                    for (int vv = 0; vv < 5; ++vv)
+                        tma_load_1d(sS + vv * 64 * P3, dv.Uf + vv * dv.nd + (c0 + 64 * h) * P3, bv, &bar_ld);
+            }
+            first = false;
+            wait(&bar_ld, ph_ld);
+            if (!ok) break;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int rl = 8 * i + (tid >> 6), r = 64 * h + rl;  // local and tile row
+                float val = 0.0f;
+                if (r < ncell) {
+                    float cf[5];
+#pragma unroll
+                    for (int vv = 0; vv < 5; ++vv) cf[vv] = sS[(vv * 64 + rl) * P3 + node];
+                    const int64_t dof = (c0 + r) * P3 + node;
+                    if (!positive_dof_screened(dv, dof, cf)) {
+                        atomicMin(&s->bad_dof, (long long)dof);
+                        s->err = PLENS_GPU_E_POSITIVITY;
+                    }
+                    val = get_p(cf, gm) * cf[0];
+                }
+                v[8 * h + i] = val;
+                float sum = val;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                if (lane == 0) s_half[r][warp & 1] = sum;
+            }
+            __syncthreads();  // this half's staged values read
+        }
+        if (!ok) break;
+        if (tid < R) s_mean[tid] = (s_half[tid][0] + s_half[tid][1]) * (1.0f / 64.0f);
+        __syncthreads();
+        // ---- features into the A operand
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int r = 8 * (i & 7) + (tid >> 6) + 64 * (i >> 3), o = a_off_padded(r, node);
+            const float x = (r < ncell) ? v[i] * (1.0f / s_mean[r]) - 1.0f : 0.0f;
+            const float hi = tc::tf32_hi(x);
+            sOhi[o] = hi;
+            sOlo[o] = x - hi;
+        }
+        tc::fence_smem_async();
+        tc::fence_before();
+        __syncthreads();
+        // ---- layer 1 into columns 0..63, the change of basis into 64..127
+        if (tid == 0) {
+            tc::fence_after();
+            cbm_mma(tmem, sOhi, sOlo, W1hi, W1lo);
+            cbm_mma(tmem + 64, sOhi, sOlo, Chi, Clo);
+            tc::mma_commit(&bar_mma);
+        }
+        mma_out = true;
+        wait(&bar_mma, ph_mma);
+        if (!ok) break;
+        mma_out = false;
+        tc::fence_after();
+        {
+            const int row = 32 * q + lane;
+            const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16);
+            float d[16];
+            tc::tmem_ld16(ta + (uint32_t)(16 * cg), d);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float hv[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) hv[e] = gelu(d[4 * j + e] + b1[16 * cg + 4 * j + e]);
+                const float4 hi = make_float4(tc::tf32_hi(hv[0]), tc::tf32_hi(hv[1]), tc::tf32_hi(hv[2]), tc::tf32_hi(hv[3]));
+                const float4 lo = make_float4(hv[0] - hi.x, hv[1] - hi.y, hv[2] - hi.z, hv[3] - hi.w);
+                const int o = a_off_padded(row, 16 * cg + 4 * j);
+                *reinterpret_cast<float4*>(sOhi + o) = hi;
+                *reinterpret_cast<float4*>(sOlo + o) = lo;
+            }
+            tc::tmem_ld16(ta + (uint32_t)(64 + 16 * cg), d);
+            float e0 = 0, e1 = 0, e2 = 0;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int n = 16 * cg + i, mi = n % P, mj = (n / P) % P, mk = n / (P * P);
+                const float md = d[i] + Crow[n], e = md * md;
+                e0 += e;
+                if (mi < N && mj < N && mk < N) e1 += e;
+                if (mi < N - 1 && mj < N - 1 && mk < N - 1) e2 += e;
+            }
+            s_e[cg][0][row] = e0;
+            s_e[cg][1][row] = e1;
+            s_e[cg][2][row] = e2;
+        }
+        tc::fence_smem_async();
+        tc::fence_before();
+        __syncthreads();
+        // ---- layer 2 into columns 128..191
+        if (tid == 0) {
+            tc::fence_after();
+            cbm_mma(tmem + 128, sOhi, sOlo, W2hi, W2lo);
+            tc::mma_commit(&bar_mma);
+        }
+        mma_out = true;
+        wait(&bar_mma, ph_mma);
+        if (!ok) break;
+        mma_out = false;
+        tc::fence_after();
+        {
+            const int row = 32 * q + lane;
+            float d[16];
+            tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(128 + 16 * cg), d);
+            float z = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) z += w3[16 * cg + i] * gelu(d[i] + b2[16 * cg + i]);
+            s_z[cg][row] = z;
+        }
+        __syncthreads();
+        if (tid < ncell) {
+            const int64_t cell = c0 + tid;
+            const float z = w3[64] + s_z[0][tid] + s_z[1][tid] + s_z[2][tid] + s_z[3][tid];
+            const float at = amax / (1.0f + expf(-z));
+            double a = (at < cut) ? 0.0 : f32_to_f64(at);
+            if (mask && mask[cell]) {
+                // the judge handed the cell back: the plain modal indicator (FP32)
+                const float e0 = s_e[0][0][tid] + s_e[1][0][tid] + s_e[2][0][tid] + s_e[3][0][tid];
+                const float e1 = s_e[0][1][tid] + s_e[1][1][tid] + s_e[2][1][tid] + s_e[3][1][tid];
+                const float e2 = s_e[0][2][tid] + s_e[1][2][tid] + s_e[2][2][tid] + s_e[3][2][tid];
+                float trouble = 1.0f - __fdividef(e1, e0);
+                const float t2 = 1.0f - __fdividef(e2, e1);
+                if (t2 > trouble) trouble = t2;
+                const float thr = f64_to_f32(bp.thr), amin = f64_to_f32(bp.amin);
+                float alpha;
+                if (bp.func == 0) {
+                    const float ah = __fdividef(1.0f, 1.0f + __expf(-f64_to_f32(bp.sharp) * (__fdividef(trouble, thr) - 1.0f)));
+                    alpha = (ah < amin) ? 0.0f : (ah < amax ? ah : amax);
+                } else {
+                    const float ah = __fdividef(trouble, thr);
+                    alpha = (ah > 1.0f) ? 1.0f : ah;
+                }
+                a = f32_to_f64(alpha);
+            }
+            if (dv.cell_wall[cell]) {
+                const double wl = eval_expr(dv, bp.expr_wall, 0, 0, 0, s->time);
+                a = (wl > a) ? wl : a;
+            }
+            out[cell] = a;
+        }
+        tc::fence_before();
+        __syncthreads();  // accumulators read, shared operands free for the next tile
+        tc::fence_after();
+    }
+    if (!ok) {
+        if (tid == 0) s->err = PLENS_GPU_E_TIMEOUT;
+        for (int it = 0; it < (1 << 22) && !mbar_try_wait(&bar_ld, ph_ld); ++it) {
+        }
+        if (mma_out)
+            for (int it = 0; it < (1 << 22) && !mbar_try_wait(&bar_mma, ph_mma); ++it) {
+            }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+}
+
+// the fused tensor-core sensor (degree 3 only; 0 launches otherwise)
+template <int P>
+int launch_sensor_tc(MlpDevice& m, const Dev& dv, const GasP& g, const BlendP& bp, double* out, int gated,
+                     const uint8_t* mask, cudaStream_t st)
+{
+    if constexpr (P == 4) {
+        static int nsm = 0;
+        if (!nsm) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            cudaFuncSetAttribute(k_sensor_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SensorTcSmem::bytes);
+            nsm = std::max(1, nsm);
+        }
+        const int64_t tiles = (dv.nc + tc::kRows - 1) / tc::kRows;
+        k_sensor_tc<P><<<(unsigned)std::min<int64_t>(tiles, nsm), kBtcThreads, SensorTcSmem::bytes, st>>>(
+            dv, m.params_tc, m.cbm, bp, g, out, gated, mask);
+        return 1;
+    } else {
+        return 0;
+    }
+}
+
 template <int P>
 int launch_infer_tc(MlpDevice& m, const Dev& dv, const GasP& g, const BlendP& bp, const Ops& ops, double* out,
                     int gated, const uint8_t* mask, cudaStream_t st)
@@ -719,9 +1002,14 @@ int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, con
     BlendP b0 = bp;
     b0.gate = 0;
     b0.mask = nullptr;
+    // degree 3 with the network on the tensor cores: the fused kernel (its plain indicator for
+    // handed-back cells takes the change of basis of the rho*p features: the default indicator
+    // variable)
+    const bool fused_tc = P == 4 && m.use_tc && m.cbm && bp.var == 0;
     if (m.judge_this_step) {
-        n += m.use_tc ? launch_infer_tc<P>(m, dv, g, bp, ops, m.alpha_plain, 0, nullptr, st)
-                      : launch_infer<P>(dv, m.params_t, g, bp, ops, m.alpha_plain, 0, nullptr, st);
+        n += fused_tc ? launch_sensor_tc<P>(m, dv, g, bp, m.alpha_plain, 0, nullptr, st)
+             : m.use_tc ? launch_infer_tc<P>(m, dv, g, bp, ops, m.alpha_plain, 0, nullptr, st)
+                        : launch_infer<P>(dv, m.params_t, g, bp, ops, m.alpha_plain, 0, nullptr, st);
         n += launch_blender<P>(dv, ops, g, b0, st);
         const unsigned grid = (unsigned)((dv.nc + 127) / 128);
         k_judge_cells<<<grid, 128, 0, st>>>(dv, m.alpha_plain, m.mask, m.tol, m.maxerr, m.nbad);
@@ -731,8 +1019,9 @@ int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, con
     } else {
         // the cells the judge handed back get the plain indicator inside the inference kernel;
         // the plain blender itself runs only in whole-domain fallback
-        n += m.use_tc ? launch_infer_tc<P>(m, dv, g, bp, ops, dv.alpha_raw, 1, m.mask, st)
-                      : launch_infer<P>(dv, m.params_t, g, bp, ops, dv.alpha_raw, 1, m.mask, st);
+        n += fused_tc ? launch_sensor_tc<P>(m, dv, g, bp, dv.alpha_raw, 1, m.mask, st)
+             : m.use_tc ? launch_infer_tc<P>(m, dv, g, bp, ops, dv.alpha_raw, 1, m.mask, st)
+                        : launch_infer<P>(dv, m.params_t, g, bp, ops, dv.alpha_raw, 1, m.mask, st);
         BlendP b1 = bp;
         b1.gate = 1;
         b1.mask = nullptr;

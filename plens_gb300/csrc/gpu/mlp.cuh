@@ -22,6 +22,7 @@ struct MlpDevice {
     float* tiles = nullptr;         // tensor-core form: network inputs, one 64 KB operand image per 128 cells
     float* mod = nullptr;           // tensor-core form: plain-indicator alpha of handed-back cells (-1: none)
     bool use_tc = false;            // the inference kernels with the hidden layers on the tensor cores
+    const float* cbm = nullptr;     // degree 3: C1 (x) C1 (x) C1 as TF32 hi/lo operands, then its row sums
     double* alpha_plain = nullptr;  // [nc] judge: MLP alpha of the judged stage
     unsigned long long* maxerr = nullptr;  // order-preserving max per-cell alpha error
     uint8_t* mask = nullptr;        // [nc] cells handed back to the plain indicator by the judge

@@ -706,7 +706,7 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
     }
     if (c->tab.blender_tc) {
         // the B operand of the tensor-core modal indicator (64 x 64 change of basis, TF32 hi/lo)
-        std::vector<float> op(2 * 64 * 64);
+        std::vector<float> op(2 * 64 * 64 + 64);
         blender_tc_operand(c->ops.C1, op.data());
         if ((r = dalloc(c, &c->cbm_tc, op.size()))) return r;
         CK(cudaMemcpy(c->cbm_tc, op.data(), sizeof(float) * op.size(), cudaMemcpyHostToDevice));
@@ -757,6 +757,10 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
     }
     if (c->learned) {
         if ((r = mlp_create(c->mlp, nc, c->allocs))) return fail(c, PLENS_GPU_E_CUDA, "mlp buffers");
+        // degree 3: the fused tensor-core sensor (its change of basis operand), the default there:
+        // measured faster than the CUDA-core inference kernel
+        c->mlp.cbm = c->cbm_tc;
+        c->mlp.use_tc = c->cbm_tc != nullptr;
         c->mlp.tol = prm->judge_alpha_tol;
     }
     d.sc = c->sc;

@@ -295,11 +295,28 @@ HexMesh read_msh(const std::string& filename)
 
 namespace {
 
+// the side of the nose cylinder's separating plane a cell lies on: the sign of
+// axis . (vertex average - separation point) (manifolds/nose_cylinder.cc:45-77); 0 on the plane
+int nose_side(const HexMesh& m, int64_t c)
+{
+    double ctr[3] = {0, 0, 0};
+    for (int v = 0; v < 8; ++v)
+        for (int d = 0; d < 3; ++d) ctr[d] += 0.125 * m.vertices[m.cells[c][v]][d];
+    double dp = 0;
+    for (int d = 0; d < 3; ++d) dp += m.axis_dir[d] * (ctr[d] - m.axis_point[d]);
+    return (dp > 0) ? 1 : (dp < 0) ? -1 : 0;
+}
+
 // Physical point of reference coordinate xi in cell c through the mesh manifold. Straight cells:
 // trilinear (MappingQGeneric(1)). Cylinder manifold: trilinear in cylindrical coordinates about
 // the axis, which places every point on the cylindrical surfaces the vertices lie on; this stands
 // in for deal.II's CylindricalManifold::get_new_point used when MappingQGeneric(m) places its
-// support points (manifolds/cylinder.cc:15-33, dgsem/plens.cc:746-797).
+// support points (manifolds/cylinder.cc:15-33, dgsem/plens.cc:746-797). Nose cylinder
+// (manifolds/nose_cylinder.cc:15-78): the cylinder rule about the axis through the separation
+// point for cells before the separating plane; beyond it the spherical rule about the nose
+// centre, standing in for SphericalManifold: the radius is the trilinear mean of the vertices'
+// radii and the direction the normalised trilinear mean of their unit directions, which places
+// every point on the spheres the vertices lie on.
 std::array<double, 3> manifold_point(const HexMesh& m, int64_t c, const double xi[3])
 {
     double w[8];
@@ -313,6 +330,19 @@ std::array<double, 3> manifold_point(const HexMesh& m, int64_t c, const double x
     if (m.manifold == 0) {
         for (int v = 0; v < 8; ++v)
             for (int d = 0; d < 3; ++d) out[d] += w[v] * m.vertices[m.cells[c][v]][d];
+        return out;
+    }
+    if (m.manifold == 2 && nose_side(m, c) > 0) {
+        double rr = 0, dir[3] = {0, 0, 0};
+        for (int v = 0; v < 8; ++v) {
+            const auto& p = m.vertices[m.cells[c][v]];
+            const double q[3] = {p[0] - m.nose_center[0], p[1] - m.nose_center[1], p[2] - m.nose_center[2]};
+            const double r = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+            rr += w[v] * r;
+            for (int d = 0; d < 3; ++d) dir[d] += w[v] * q[d] / r;
+        }
+        const double dn = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+        for (int d = 0; d < 3; ++d) out[d] = m.nose_center[d] + rr * dir[d] / dn;
         return out;
     }
     // cylinder: orthonormal frame (e1, e2, axis)
@@ -755,11 +785,29 @@ std::unique_ptr<Case> build_case(const ParameterHandler& prm, int mapping_degree
         mesh.manifold = 0;
         C.mapping_degree = 1;
     } else if (mtype == "curved") {
-        if (prm.get("mesh/curved subtype") != "cylinder")
-            throw std::runtime_error("only the 'cylinder' curved subtype is supported");
-        mesh.manifold = 1;
-        mesh.axis_dir = parse3(prm.get("mesh/cylinder/axis direction"), "axis direction");
-        mesh.axis_point = parse3(prm.get("mesh/cylinder/axis point"), "axis point");
+        const std::string sub = prm.get("mesh/curved subtype");
+        if (sub == "cylinder") {
+            mesh.manifold = 1;
+            mesh.axis_dir = parse3(prm.get("mesh/cylinder/axis direction"), "axis direction");
+            mesh.axis_point = parse3(prm.get("mesh/cylinder/axis point"), "axis point");
+        } else if (sub == "nose cylinder") {
+            // manifolds/nose_cylinder.cc:15-78 and the reading of its parameters (plens.cc:746-797)
+            mesh.manifold = 2;
+            mesh.axis_dir = parse3(prm.get("mesh/nose cylinder/axis direction"), "axis direction");
+            mesh.axis_point = parse3(prm.get("mesh/nose cylinder/separation point"), "separation point");
+            mesh.nose_center = parse3(prm.get("mesh/nose cylinder/nose center"), "nose center");
+            double dp = 0;
+            for (int d = 0; d < 3; ++d) dp += mesh.axis_dir[d] * (mesh.nose_center[d] - mesh.axis_point[d]);
+            if (!(dp < 0))
+                throw std::runtime_error("The nose center lies in spherical region. This will produce a singularity in "
+                                         "spherical manifold.");
+            for (int64_t c = 0; c < (int64_t)mesh.cells.size(); ++c)
+                if (nose_side(mesh, c) == 0)
+                    throw std::runtime_error("One of the cell centers in the triangulation provided lies on the "
+                                             "bifurcation plane (cell " + std::to_string(c) + ").");
+        } else {
+            throw std::runtime_error("curved subtype must be cylinder|nose cylinder");
+        }
         C.mapping_degree = mapping_degree;
     } else {
         throw std::runtime_error("mesh type must be straight|curved");

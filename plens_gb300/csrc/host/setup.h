@@ -34,9 +34,11 @@ struct HexMesh {
     std::vector<std::array<double, 3>> vertices;
     std::vector<std::array<int64_t, 8>> cells;
     std::vector<std::array<int32_t, 6>> face_bid;  // boundary id of boundary faces, -1 otherwise
-    // manifold: 0 = straight (Q1), 1 = cylinder around axis (axis_dir, axis_point)
+    // manifold: 0 = straight (Q1), 1 = cylinder around axis (axis_dir, axis_point), 2 = nose
+    // cylinder: cells whose centre lies beyond the plane through axis_point normal to axis_dir are
+    // spherical about nose_center, the others cylindrical about the axis through axis_point
     int manifold = 0;
-    std::array<double, 3> axis_dir{{0, 0, 1}}, axis_point{{0, 0, 0}};
+    std::array<double, 3> axis_dir{{0, 0, 1}}, axis_point{{0, 0, 0}}, nose_center{{0, 0, 0}};
 };
 
 struct BoxSpec {

@@ -5,9 +5,10 @@ For each sensor the test reports and bounds: the relative L1 distance of rho, mo
 from the FP64 form after the window; the per-cell agreement of the learned form's alpha with the
 modal form's on the same state (mean absolute difference, and the share of cells where one is
 troubled and the other is not); the judge's outcome (judged steps, cells handed back to the
-plain indicator and their rate, the largest alpha error it saw). The learned sensor has to stay
-within the configuration's rho bound (1e-4); the modal form, which evaluates the indicator it
-imitates, is the accuracy reference.
+plain indicator and their rate, the largest alpha error it saw). The workload is the double Mach
+reflection configuration itself (240 x 60 x 1 cells, N = 3) over its first 100 steps; the
+learned sensor has to stay within the configuration's rho bound (1e-4); the modal form, which
+evaluates the indicator it imitates, is the accuracy reference.
 """
 from pathlib import Path
 
@@ -20,14 +21,14 @@ from plens_gb300.api import GpuSolver
 
 pytestmark = pytest.mark.gpu
 
-STEPS = 60
+STEPS = 100
 
 
 def _weights():
     return np.fromfile(Path(__file__).resolve().parent.parent / "plens_gb300" / "sensor_weights.bin", dtype=np.float32)
 
 
-def _run(prec, sensor, nx=120, ny=30):
+def _run(prec, sensor, nx=240, ny=60):
     case = make(configs.dmr(nx=nx, ny=ny, precision=prec, sensor=sensor))
     g = GpuSolver(case)
     if sensor == "learned":
@@ -54,7 +55,7 @@ def test_learned_sensor_against_the_modal_indicator():
     disagree = float(((a_l > 0) != (a_m > 0)).mean())
     st = gl.sensor_stats()
     rate = st["fallbacks"] / max(st["judged"] * case.n_cells, 1)
-    print(f"\nDMR 120x30, {STEPS} steps; rel L1 (rho, momentum, rho E) vs FP64: modal {err_m}, learned {err_l}; "
+    print(f"\nDMR 240x60, {STEPS} steps; rel L1 (rho, momentum, rho E) vs FP64: modal {err_m}, learned {err_l}; "
           f"alpha vs modal: mean |diff| {mad:.2e}, troubled-set disagreement {disagree:.3%}; judge: {st['judged']} "
           f"judged steps, {st['fallbacks']} cells handed back ({rate:.3%}), max alpha error {st['max_alpha_err']:.3f}")
     assert err_m[0] <= 1e-6  # the modal form: FP32 round-off only

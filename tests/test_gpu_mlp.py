@@ -119,3 +119,30 @@ def test_sensor_tensor_cores_match_cuda_cores():
     off = d > 1e-5
     assert off.mean() <= 2e-3, d.max()
     assert np.all(np.minimum(a1[off], a2[off]) < 0.011), (a1[off], a2[off])
+
+
+def test_sensor_tensor_cores_with_handed_back_cells():
+    """The degree-3 tensor-core sensor computes the plain indicator of the cells the judge handed
+    back from the change of basis of its features (the modal coefficients of rho*p are the mean
+    times those plus the row sums of C). A random-initialised network, judged every 5th step,
+    has many cells handed back; the run with the network on the tensor cores follows the
+    CUDA-core run: the same judge counts within a cell or two, the states to 1e-4 relative L1."""
+    from oracle import mlp_oracle
+
+    prm, files, deg = configs.dmr(nx=120, ny=30, precision="mixed", sensor="learned")
+    case = make((prm.replace("set judge every = 25", "set judge every = 5"), files, deg))
+    w = mlp_oracle.init_params(0)
+    runs = []
+    for tc_on in (False, True):
+        g = GpuSolver(case)
+        g.set_sensor_weights(w)
+        g.set_sensor_tensor_cores(tc_on)
+        g.set_state(case.initial_state(), 0.0)
+        g.advance(40)
+        runs.append((g.get_state(), g.sensor_stats()))
+    (U0, s0), (U1, s1) = runs
+    assert s0["judged"] == s1["judged"] >= 8
+    assert s0["fallbacks"] > 100
+    assert abs(s0["fallbacks"] - s1["fallbacks"]) <= 2 + 0.01 * s0["fallbacks"]
+    d = np.abs(U1 - U0).sum(axis=1) / np.abs(U0).sum(axis=1)
+    assert d[[0, 4]].max() <= 1e-4
