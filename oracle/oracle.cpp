@@ -256,6 +256,54 @@ struct NavierStokes {
         for (int i = 0; i < 5; ++i) for (int j = 0; j < 5; ++j) for (int k = 0; k < 5; ++k) A[i][j] += K[i][k] * eig[k] * Ki[k][j];
         for (int i = 0; i < 5; ++i) for (int j = 0; j < 5; ++j) f[i] -= 0.5 * A[i][j] * (r[j] - l[j]);
     }
+    // Modified Steger-Warming (cc:1172-1234; Druguet, Candler & Nompelis 2005): split fluxes
+    // A+ l + A- r, with A+- = K diag(eig+-) K^-1 (the x eigenvector matrices of cc:641-675 and
+    // cc:780-822) at pressure-weighted averages of the two states, the eigenvalues smoothed with
+    // 0.3 a (h:464-476)
+    void msw_side(const State& a, const State& b, double w, bool pos, double A[5][5]) const
+    {
+        const double pa = get_p(a), pb = get_p(b);
+        Vec v;
+        for (int d = 0; d < 3; ++d) v[d] = (1 - w) * a[1 + d] / a[0] + w * b[1 + d] / b[0];
+        const double rho = (1 - w) * a[0] + w * b[0], p = (1 - w) * pa + w * pb;
+        const double c = std::sqrt(gma * p / rho);
+        const double H = gma * p / ((gma - 1) * rho) + 0.5 * dot(v, v);
+        double K[5][5], Ki[5][5];
+        K[0][0] = 1; K[1][0] = v[0] - c; K[2][0] = v[1]; K[3][0] = v[2]; K[4][0] = H - v[0] * c;
+        K[0][1] = 1; K[1][1] = v[0]; K[2][1] = v[1]; K[3][1] = v[2]; K[4][1] = 0.5 * dot(v, v);
+        K[0][2] = 0; K[1][2] = 0; K[2][2] = 1; K[3][2] = 0; K[4][2] = v[1];
+        K[0][3] = 0; K[1][3] = 0; K[2][3] = 0; K[3][3] = 1; K[4][3] = v[2];
+        K[0][4] = 1; K[1][4] = v[0] + c; K[2][4] = v[1]; K[3][4] = v[2]; K[4][4] = H + v[0] * c;
+        const double t = 1 / (gma - 1);
+        Ki[0][0] = H + c * (v[0] - c) * t; Ki[0][1] = -v[0] - c * t; Ki[0][2] = -v[1]; Ki[0][3] = -v[2]; Ki[0][4] = 1;
+        Ki[1][0] = 2 * (2 * c * c * t - H); Ki[1][1] = 2 * v[0]; Ki[1][2] = 2 * v[1]; Ki[1][3] = 2 * v[2]; Ki[1][4] = -2;
+        Ki[2][0] = -2 * v[1] * c * c * t; Ki[2][1] = 0; Ki[2][2] = 2 * c * c * t; Ki[2][3] = 0; Ki[2][4] = 0;
+        Ki[3][0] = -2 * v[2] * c * c * t; Ki[3][1] = 0; Ki[3][2] = 0; Ki[3][3] = 2 * c * c * t; Ki[3][4] = 0;
+        Ki[4][0] = H - c * (v[0] + c) * t; Ki[4][1] = -v[0] + c * t; Ki[4][2] = -v[1]; Ki[4][3] = -v[2]; Ki[4][4] = 1;
+        const double factor = 0.5 * (gma - 1) / (c * c);
+        for (auto& row : Ki) for (double& x : row) x *= factor;
+        const double eps = 0.3 * c;
+        auto sm = [&](double x) { return pos ? 0.5 * (x + std::sqrt(x * x + eps * eps)) : 0.5 * (x - std::sqrt(x * x + eps * eps)); };
+        const double eig[5] = {sm(v[0] - c), sm(v[0]), sm(v[0]), sm(v[0]), sm(v[0] + c)};
+        for (int i = 0; i < 5; ++i)
+            for (int j = 0; j < 5; ++j) {
+                A[i][j] = 0;
+                for (int k = 0; k < 5; ++k) A[i][j] += K[i][k] * eig[k] * Ki[k][j];
+            }
+    }
+    void modified_sw_xflux(const State& l, const State& r, State& f) const
+    {
+        const double pl = get_p(l), pr = get_p(r);
+        const double q = 0.5 * (pr - pl) / std::min(pl, pr);
+        const double w = 0.5 / (1 + q * q);
+        double Ap[5][5], An[5][5];
+        msw_side(l, r, w, true, Ap);
+        msw_side(r, l, w, false, An);
+        for (int i = 0; i < 5; ++i) {
+            f[i] = 0;
+            for (int j = 0; j < 5; ++j) f[i] += Ap[i][j] * l[j] + An[i][j] * r[j];
+        }
+    }
     void inv_surf_xflux(const State& l, const State& r, State& f) const
     {
         switch (isf) {
@@ -277,6 +325,7 @@ struct NavierStokes {
             return;
         }
         case PLENS_ISF_CHANDRASHEKHAR: chandrashekhar_xflux(l, r, f); return;
+        case PLENS_ISF_MODIFIED_SW: modified_sw_xflux(l, r, f); return;
         default: for (int v = 0; v < 5; ++v) f[v] = NAN; return;
         }
     }

@@ -91,9 +91,9 @@ struct Dev {
     // mesh
     const double *detJ, *Ja, *Jinv, *h_min, *center;
     // the FP32 rounding (f64_to_f32) of detJ, Ja and Jinv, made once on the device at context
-    // creation -- the value every FP32 consumer of the FP64 metric terms would compute: all three
-    // in the MIXED_R32 form, Jinv alone (for the FP32 time step) in the MIXED form, none in the
-    // FP64 form; where one is null its FP32 consumers round the FP64 array themselves
+    // creation -- the value every FP32 consumer of the FP64 metric terms would compute -- in both
+    // mixed forms, none in the FP64 form; where one is null its FP32 consumers round the FP64
+    // array themselves
     const float *detJf, *Jaf, *Jinvf;
     // MIXED form: 1/detJ in FP64 (made once at creation), by which the volume kernels scale the
     // FP32 residual sums in FP64 (null otherwise)

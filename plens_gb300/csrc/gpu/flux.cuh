@@ -408,6 +408,79 @@ __device__ __forceinline__ void chandrashekhar_x(const T l[5], const T r[5], T g
     }
 }
 
+// Modified Steger-Warming (navier_stokes.cc:1172-1234; Druguet, Candler & Nompelis 2005): split
+// fluxes A+ l + A- r, with A+- = K diag(eig+-) K^-1 (the x eigenvector matrices of
+// navier_stokes.cc:641-675 and 780-822) at pressure-weighted averages of the two states, the
+// eigenvalues smoothed with 0.3 a (navier_stokes.h:464-476). `pos` selects the A+ side: state a
+// weighted 1 - w, b weighted w.
+template <class T>
+__device__ __forceinline__ void msw_side(const T a[5], const T b[5], T w, bool pos, T gma, T A[5][5])
+{
+    const T pa = get_p(a, gma), pb = get_p(b, gma);
+    T v[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d] = fdiv((T(1) - w) * a[1 + d], a[0]) + fdiv(w * b[1 + d], b[0]);
+    const T rho = (T(1) - w) * a[0] + w * b[0], p = (T(1) - w) * pa + w * pb;
+    const T c = dsqrt(fdiv(gma * p, rho));
+    const T vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    const T H = fdiv(gma * p, (gma - 1) * rho) + T(0.5) * vv;
+    const T K[5][5] = {{1, 1, 0, 0, 1},
+                       {v[0] - c, v[0], 0, 0, v[0] + c},
+                       {v[1], v[1], 1, 0, v[1]},
+                       {v[2], v[2], 0, 1, v[2]},
+                       {H - v[0] * c, T(0.5) * vv, v[1], v[2], H + v[0] * c}};
+    const T t = fdiv(T(1), gma - 1);
+    T Ki[5][5] = {{H + c * (v[0] - c) * t, -v[0] - c * t, -v[1], -v[2], 1},
+                  {2 * (2 * c * c * t - H), 2 * v[0], 2 * v[1], 2 * v[2], -2},
+                  {-2 * v[1] * c * c * t, 0, 2 * c * c * t, 0, 0},
+                  {-2 * v[2] * c * c * t, 0, 0, 2 * c * c * t, 0},
+                  {H - c * (v[0] + c) * t, -v[0] + c * t, -v[1], -v[2], 1}};
+    const T factor = fdiv(T(0.5) * (gma - 1), c * c);
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+#pragma unroll
+        for (int j = 0; j < 5; ++j) Ki[i][j] *= factor;
+    const T eps = T(0.3) * c;
+    T eig[5];
+    const T x[3] = {v[0] - c, v[0], v[0] + c};
+    T sx[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const T s = dsqrt(x[k] * x[k] + eps * eps);
+        sx[k] = pos ? T(0.5) * (x[k] + s) : T(0.5) * (x[k] - s);
+    }
+    eig[0] = sx[0];
+    eig[1] = eig[2] = eig[3] = sx[1];
+    eig[4] = sx[2];
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            T s = 0;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) s += K[i][k] * eig[k] * Ki[k][j];
+            A[i][j] = s;
+        }
+}
+
+template <class T>
+__device__ __forceinline__ void msw_x(const T l[5], const T r[5], T gma, T f[5])
+{
+    const T pl = get_p(l, gma), pr = get_p(r, gma);
+    const T q = fdiv(T(0.5) * (pr - pl), pl < pr ? pl : pr);
+    const T w = fdiv(T(0.5), T(1) + q * q);
+    T Ap[5][5], An[5][5];
+    msw_side(l, r, w, true, gma, Ap);
+    msw_side(r, l, w, false, gma, An);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        T s = 0;
+#pragma unroll
+        for (int j = 0; j < 5; ++j) s += Ap[i][j] * l[j] + An[i][j] * r[j];
+        f[i] = s;
+    }
+}
+
 template <class T>
 __device__ __forceinline__ void surf_xflux(const T l[5], const T r[5], T gma, int isf, T fb, T f[5])
 {
@@ -432,6 +505,7 @@ __device__ __forceinline__ void surf_xflux(const T l[5], const T r[5], T gma, in
         return;
     }
     case PLENS_ISF_CHANDRASHEKHAR: chandrashekhar_x(l, r, gma, fb, f); return;
+    case PLENS_ISF_MODIFIED_SW: msw_x(l, r, gma, f); return;
     default:
 #pragma unroll
         for (int v = 0; v < 5; ++v) f[v] = T(0) / T(0);

@@ -19,6 +19,7 @@ struct StageArgs {
     double c0, c1, c2;
     float fc0, fc1, fc2;  // the same coefficients for the MIXED_R32 form's FP32 register combination
     int reg64;  // mixed forms: 1 (MIXED) FP64 registers, FP64 1/detJ scaling and accumulation; 0 (MIXED_R32) FP32
+    int keep;   // RK4: 1 when a later stage reads this stage's register (every stage but the last)
 };
 
 // ------------------------------------------------------------------------ step bookkeeping
@@ -802,7 +803,7 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 ? 10 : 1)) k_surface(Dev 
 // PLENS::calc_aux_vars + calc_cell_evar_grad (dgsem/plens.cc:2593-2748, 2294-2405): BR1 lifting
 // of the entropy variables, then the stress tensor and heat flux scaled by mu and k.
 template <int P, class T>
-__global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, GasP g)
+__global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 && P == 4) ? 8 : 1) k_aux(Dev dv, Ops ops, GasP g)
 {
     using CB = CellBlock<P>;
     constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1;
@@ -810,31 +811,50 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
     T* sE = reinterpret_cast<T*>(smem_raw);        // [CPB][5][P3]
     T* sJa = sE + CPB * 5 * P3;                     // [CPB][9][P3]
     T* sEf = sJa + CPB * 9 * P3;                    // [CPB][6][5][P2]
+    // D in shared memory: the lanes of a warp read different entries of it, which the constant
+    // cache would serve one address at a time
+    __shared__ T sD[P * P];
     Scalars* s = dv.sc;
     if (!s->active) return;
     const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
     const int64_t cell = (int64_t)blockIdx.x * CPB + cl;
     const bool valid = (cl < CPB) && (cell < dv.nc);
     const T gm = to_real<T>(g.gamma);
+    for (int k = tid; k < P * P; k += blockDim.x) sD[k] = opD<T>(ops, k);
     T cd[5] = {1, 0, 0, 0, 1};  // the node's state in T (FP64 state, or its FP32 image)
+    T ev[5] = {0, 0, 0, 0, 0};   // and its entropy variables
+    T dj = T(1);                  // and det J
     if (valid) {
+        // every load of the thread first (state, metric terms, det J, its face slots), then the
+        // arithmetic: one memory latency per block instead of one per group of loads
+        constexpr int NS = (6 * P2 + P3 - 1) / P3;  // face slots per thread
         const int64_t dof = cell * P3 + node;
-        T c[5], e[5];
-        load_state<T>(dv, dof, c);
+        T ja[9], fc[NS][5];
+        load_state<T>(dv, dof, cd);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) cd[v] = c[v];
-        cons_to_entropy(c, gm, e);
+        for (int m = 0; m < 9; ++m) ja[m] = metric<T>(dv.Ja, dv.Jaf, m * dv.nd + dof);
+        dj = metric<T>(dv.detJ, dv.detJf, dof);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) sE[(cl * 5 + v) * P3 + node] = e[v];
+        for (int k = 0; k < NS; ++k) {
+            const int sl = node + k * P3;
+            if (sl < 6 * P2)
 #pragma unroll
-        for (int m = 0; m < 9; ++m) sJa[(cl * 9 + m) * P3 + node] = metric<T>(dv.Ja, dv.Jaf, m * dv.nd + dof);
-        for (int sl = node; sl < 6 * P2; sl += P3) {
-            T fc[5], fe[5];
+                for (int v = 0; v < 5; ++v) fc[k][v] = as_real<T>(dv.sf)[v * dv.nslot + cell * 6 * P2 + sl];
+        }
+        cons_to_entropy(cd, gm, ev);
 #pragma unroll
-            for (int v = 0; v < 5; ++v) fc[v] = as_real<T>(dv.sf)[v * dv.nslot + cell * 6 * P2 + sl];
-            cons_to_entropy(fc, gm, fe);
+        for (int v = 0; v < 5; ++v) sE[(cl * 5 + v) * P3 + node] = ev[v];
 #pragma unroll
-            for (int v = 0; v < 5; ++v) sEf[((cl * 6 + sl / P2) * 5 + v) * P2 + (sl % P2)] = fe[v];
+        for (int m = 0; m < 9; ++m) sJa[(cl * 9 + m) * P3 + node] = ja[m];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+            const int sl = node + k * P3;
+            if (sl < 6 * P2) {
+                T fe[5];
+                cons_to_entropy(fc[k], gm, fe);
+#pragma unroll
+                for (int v = 0; v < 5; ++v) sEf[((cl * 6 + sl / P2) * 5 + v) * P2 + (sl % P2)] = fe[v];
+            }
         }
     }
     __syncthreads();
@@ -842,20 +862,34 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
     const int ti[3] = {node % P, (node / P) % P, node / P2};
     const T* E = sE + cl * 5 * P3;
     const T* J = sJa + cl * 9 * P3;
+    // volume terms: sum_m sum_md D_(i,m) (E Ja_md,gd)_m, each line node's E and Ja row loaded once
+    // for the three gradient directions; per direction gd the terms add in the order m, md
+    T acc[3][5];
+#pragma unroll
+    for (int gd = 0; gd < 3; ++gd)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) acc[gd][v] = T(0);
+#pragma unroll
+    for (int m = 0; m < P; ++m) {
+#pragma unroll
+        for (int md = 0; md < 3; ++md) {
+            const int lo = (md == 0) ? m + P * ti[1] + P2 * ti[2] : (md == 1) ? ti[0] + P * m + P2 * ti[2] : ti[0] + P * ti[1] + P2 * m;
+            T de[5], jc[3];
+            const T dvl = sD[ti[md] * P + m];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) de[v] = dvl * E[v * P3 + lo];
+#pragma unroll
+            for (int gd = 0; gd < 3; ++gd) jc[gd] = J[(md * 3 + gd) * P3 + lo];
+#pragma unroll
+            for (int gd = 0; gd < 3; ++gd)
+#pragma unroll
+                for (int v = 0; v < 5; ++v) acc[gd][v] += de[v] * jc[gd];
+        }
+    }
+    const T jinv = fdiv(T(1.0), dj);
     T grad[3][5];
 #pragma unroll
     for (int gd = 0; gd < 3; ++gd) {
-        T acc[5] = {0, 0, 0, 0, 0};
-        for (int m = 0; m < P; ++m) {
-#pragma unroll
-            for (int md = 0; md < 3; ++md) {
-                const int lo = (md == 0) ? m + P * ti[1] + P2 * ti[2] : (md == 1) ? ti[0] + P * m + P2 * ti[2] : ti[0] + P * ti[1] + P2 * m;
-                const T jc = J[(md * 3 + gd) * P3 + lo];
-                const T dvl = opD<T>(ops, ti[md] * P + m);
-#pragma unroll
-                for (int v = 0; v < 5; ++v) acc[v] += dvl * E[v * P3 + lo] * jc;
-            }
-        }
 #pragma unroll
         for (int sd = 0; sd < 3; ++sd) {
 #pragma unroll
@@ -868,24 +902,17 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_aux(Dev dv, Ops ops, 
                 const T wend = opW<T>(ops, lr * N);
 #pragma unroll
                 for (int v = 0; v < 5; ++v) {
-                    const T fin = E[v * P3 + node] * jc;
+                    const T fin = ev[v] * jc;
                     const T fsu = sEf[((cl * 6 + f) * 5 + v) * P2 + q] * jc;
-                    acc[v] -= fdiv(sgn * (fsu - fin), wend);
+                    acc[gd][v] -= fdiv(sgn * (fsu - fin), wend);
                 }
             }
         }
-        const T jinv = fdiv(T(1.0), metric<T>(dv.detJ, dv.detJf, cell * P3 + node));
 #pragma unroll
-        for (int v = 0; v < 5; ++v) grad[gd][v] = acc[v] * jinv;
+        for (int v = 0; v < 5; ++v) grad[gd][v] = acc[gd][v] * jinv;
     }
     const int64_t dof = cell * P3 + node;
-    T et[5];
-    {
-        T c[5];
-#pragma unroll
-        for (int v = 0; v < 5; ++v) c[v] = cd[v];
-        cons_to_entropy(c, gm, et);
-    }
+    const T* et = ev;
     T vg[3][3];
 #pragma unroll
     for (int vd = 0; vd < 3; ++vd)
@@ -1381,7 +1408,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                     if (sa.stage >= 3) un = __fma_rn(sa.c0, sa.R0[k], un);
                     if (sa.stage >= 2) un = __fma_rn(sa.c1, sa.R1[k], un);
                     un = __fma_rn(sa.c2, Rs, un);
-                    sa.Rw[k] = Rs;
+                    if (sa.keep) sa.Rw[k] = Rs;
                 } else {
                     if (sa.stage == 1) un = u + Rs;
                     else if (sa.stage == 2) un = 0.75 * dv.U0[k] + 0.25 * u + 0.25 * Rs;
@@ -1419,7 +1446,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
                 if (sa.stage == 1) inc = sa.fc2 * Rs;
                 else if (sa.stage == 2) inc = sa.fc1 * as_real<float>(sa.R1)[k] + sa.fc2 * Rs;
                 else inc = sa.fc0 * as_real<float>(sa.R0)[k] + sa.fc1 * as_real<float>(sa.R1)[k] + sa.fc2 * Rs;
-                as_real<float>(sa.Rw)[k] = Rs;
+                if (sa.keep) as_real<float>(sa.Rw)[k] = Rs;
                 const double un = ud[v] + f32_to_f64(inc);
                 dv.U[k] = un;
                 dv.Uf[k] = f64_to_f32(un);
@@ -1458,7 +1485,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 ? 5 : 1
             if (sa.stage == 1) un = ud[v] + sa.c2 * Rs;
             else if (sa.stage == 2) un = ud[v] + (sa.c1 * sa.R1[k] + sa.c2 * Rs);
             else un = ud[v] + (sa.c0 * sa.R0[k] + sa.c1 * sa.R1[k] + sa.c2 * Rs);
-            sa.Rw[k] = Rs;
+            if (sa.keep) sa.Rw[k] = Rs;
         } else {
             if (sa.stage == 1) un = ud[v] + Rs;
             else if (sa.stage == 2) un = 0.75 * dv.U0[k] + 0.25 * ud[v] + 0.25 * Rs;

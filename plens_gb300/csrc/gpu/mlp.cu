@@ -703,7 +703,8 @@ __global__ void __launch_bounds__(kBtcThreads, 1) k_sensor_tc(Dev dv, const floa
     float* sOlo = sS + BtcSmem::kA;
     Scalars* s = dv.sc;
     if (!s->active) return;
-    if (gated && s->sensor_fallback) return;
+    // whole-domain fallback: every cell takes the plain indicator computed here
+    const bool all_plain = gated && s->sensor_fallback;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t ntiles = (dv.nc + R - 1) / R;
     const float gm = f64_to_f32(g.gamma);
@@ -864,8 +865,9 @@ __global__ void __launch_bounds__(kBtcThreads, 1) k_sensor_tc(Dev dv, const floa
             const float z = w3[64] + s_z[0][tid] + s_z[1][tid] + s_z[2][tid] + s_z[3][tid];
             const float at = amax / (1.0f + expf(-z));
             double a = (at < cut) ? 0.0 : f32_to_f64(at);
-            if (mask && mask[cell]) {
-                // the judge handed the cell back: the plain modal indicator (FP32)
+            if (all_plain || (mask && mask[cell])) {
+                // the judge handed the cell back (or the whole domain is in fallback): the plain
+                // modal indicator (FP32)
                 const float e0 = s_e[0][0][tid] + s_e[1][0][tid] + s_e[2][0][tid] + s_e[3][0][tid];
                 const float e1 = s_e[0][1][tid] + s_e[1][1][tid] + s_e[2][1][tid] + s_e[3][1][tid];
                 const float e2 = s_e[0][2][tid] + s_e[1][2][tid] + s_e[2][2][tid] + s_e[3][2][tid];
@@ -1018,14 +1020,17 @@ int sensor_stage(MlpDevice& m, const Dev& dv, const Ops& ops, const GasP& g, con
         m.judge_this_step = false;  // the remaining stages of this step follow the decision
     } else {
         // the cells the judge handed back get the plain indicator inside the inference kernel;
-        // the plain blender itself runs only in whole-domain fallback
+        // in whole-domain fallback the plain blender runs instead (the fused tensor-core kernel
+        // computes the plain indicator of every cell then itself)
         n += fused_tc ? launch_sensor_tc<P>(m, dv, g, bp, dv.alpha_raw, 1, m.mask, st)
              : m.use_tc ? launch_infer_tc<P>(m, dv, g, bp, ops, dv.alpha_raw, 1, m.mask, st)
                         : launch_infer<P>(dv, m.params_t, g, bp, ops, dv.alpha_raw, 1, m.mask, st);
-        BlendP b1 = bp;
-        b1.gate = 1;
-        b1.mask = nullptr;
-        n += launch_blender<P>(dv, ops, g, b1, st, 152 * 2);
+        if (!fused_tc) {
+            BlendP b1 = bp;
+            b1.gate = 1;
+            b1.mask = nullptr;
+            n += launch_blender<P>(dv, ops, g, b1, st, 152 * 2);
+        }
     }
     k_alpha_smooth<<<(unsigned)((dv.nc + kSmoothThreads - 1) / kSmoothThreads), kSmoothThreads, 0, st>>>(dv, b0);
     return n + 1;

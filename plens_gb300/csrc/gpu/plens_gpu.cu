@@ -417,6 +417,7 @@ int launch_step(plens_ctx* c, double end_time, bool judge = true)
             StageArgs sa{};
             sa.mode = 1;
             sa.stage = s;
+            sa.keep = s < 5 ? 1 : 0;  // the last stage's dt*R is read by no later stage
             sa.Rw = c->R[w];
             sa.R1 = (r1 >= 0) ? c->R[r1] : nullptr;
             sa.R0 = (r0 >= 0) ? c->R[r0] : nullptr;
@@ -510,7 +511,7 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
     if (prm->rk_order != 3 && prm->rk_order != 4) return fail(c, PLENS_GPU_E_INVALID, "RK order must be 3 or 4");
     if (prm->blender_function != 0 && prm->blender_function != 1)
         return fail(c, PLENS_GPU_E_INVALID, "blender function must be Hennemann or linear");
-    if (prm->inv_surf_flux < 0 || prm->inv_surf_flux > PLENS_ISF_CHANDRASHEKHAR || prm->inv_surf_flux == PLENS_ISF_MODIFIED_SW)
+    if (prm->inv_surf_flux < 0 || prm->inv_surf_flux > PLENS_ISF_CHANDRASHEKHAR)
         return fail(c, PLENS_GPU_E_INVALID, "inviscid surface flux scheme not supported on the GPU path");
     if (prm->inv_vol_flux < 0 || prm->inv_vol_flux > PLENS_IVF_ISMAIL_ROE)
         return fail(c, PLENS_GPU_E_INVALID, "bad inviscid volume flux scheme");
@@ -676,16 +677,23 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         if ((r = dalloc(c, &invJ, nd))) return r;
         CK(cudaDeviceSynchronize());  // the uploads above ran on the legacy stream
         k_reciprocal<<<(unsigned)std::min<int64_t>((nd + 255) / 256, 152 * 16), 256, 0, c->stream>>>(d.detJ, invJ, nd);
-        // the time step is an FP32 estimate from the FP32 rounding of J^-1: read from an image
-        // made once (the same values; half the bytes of rounding the FP64 array every step)
-        float* Jinvf = nullptr;
-        if ((r = dalloc(c, &Jinvf, 9 * nd))) return r;
-        k_round_f32<<<(unsigned)std::min<int64_t>((9 * nd + 255) / 256, 152 * 16), 256, 0, c->stream>>>(d.Jinv, Jinvf,
-                                                                                                    9 * nd);
-        c->launches += 2;
-        if ((r = check_launch(c, "1/detJ, J^-1 image"))) return r;
+        // The FP32 consumers of the metric terms (the time step's estimate from J^-1; the
+        // auxiliary-variable and subcell kernels' FP32 arithmetic on Ja and detJ) read the FP32
+        // rounding of the FP64 arrays from images made once: the same values as rounding the FP64
+        // arrays where they are read, half the bytes. The volume kernel reads the FP64 Ja and
+        // rounds it itself; 1/detJ and the register arithmetic stay FP64.
+        float *Jinvf = nullptr, *Jaf = nullptr, *detJf = nullptr;
+        if ((r = dalloc(c, &Jinvf, 9 * nd)) || (r = dalloc(c, &Jaf, 9 * nd)) || (r = dalloc(c, &detJf, nd))) return r;
+        const unsigned grid = (unsigned)std::min<int64_t>((9 * nd + 255) / 256, 152 * 16);
+        k_round_f32<<<grid, 256, 0, c->stream>>>(d.Jinv, Jinvf, 9 * nd);
+        k_round_f32<<<grid, 256, 0, c->stream>>>(d.Ja, Jaf, 9 * nd);
+        k_round_f32<<<grid, 256, 0, c->stream>>>(d.detJ, detJf, nd);
+        c->launches += 4;
+        if ((r = check_launch(c, "1/detJ, metric images"))) return r;
         d.invJ = invJ;
         d.Jinvf = Jinvf;
+        d.Jaf = Jaf;
+        d.detJf = detJf;
     } else if (c->mixed) {
         // MIXED_R32 form: the FP32 rounding of the metric terms, once (every FP32 consumer reads
         // these instead of rounding the FP64 arrays itself: the same values)

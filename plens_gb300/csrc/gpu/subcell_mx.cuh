@@ -66,12 +66,13 @@ static __global__ void __launch_bounds__(kSmoothThreads) k_lo_list(Dev dv)
 // Interior subcell sums of the listed cells, CPB cells per block, one thread per GLL node; line
 // tasks numbered flat over the block's cells (3 P^2 per cell), each running the P - 1 subcell
 // interfaces of one line. The grid is persistent: blocks take groups of CPB listed cells with a
-// stride, up to the count the list kernel wrote. The kernel is latency-bound (a few hundred
-// listed cells, one chain of dependent loads per group): the count and the group's list entries
-// are loaded together (entries past the count are not used), HLLC -- whose subcell flux does not
-// read alpha -- has an instantiation of its own without the alpha load or the scheme switch (a
-// smaller code path to fetch), and the launcher caps the grid at two blocks per SM so that blocks
-// take several groups with their code already fetched.
+// stride, up to the count the list kernel wrote, and the loads are pipelined: while a group's
+// fluxes run, every thread has its node's state image and metric terms of the block's next group
+// in flight in registers, and the threads of the first CPB lanes the list entries of the group
+// after it. A group then waits for no global load; only the block's first group does. HLLC --
+// whose subcell flux does not read alpha -- has an instantiation of its own without the alpha
+// load or the scheme switch. The metric terms are read from the FP32 image both mixed forms
+// keep. The launcher caps the grid at two blocks per SM.
 template <int P, bool HLLC>
 __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Ops ops, GasP g)
 {
@@ -82,35 +83,63 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
     __shared__ float sJ[9][NB];   // FP32 rounding of Ja
     __shared__ float sAcc[CPB][15][P3];
     __shared__ float sAl[CPB];
-    __shared__ int32_t sCell[CPB];
+    __shared__ int32_t sCell[2][CPB];  // cells of this group and of the block's next group
     Scalars* s = dv.sc;
     if (!s->active) return;
     const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
     const float gm = f64_to_f32(g.gamma);
-    for (int grp = blockIdx.x;; grp += gridDim.x) {
-        const int p0 = grp * CPB;
-        if (tid < CPB) {
-            const int n = *dv.lo_count;
-            const int32_t c = (p0 + tid < dv.nc) ? dv.lo_list[p0 + tid] : -1;  // loaded beside the count
-            sCell[tid] = (p0 + tid < n) ? c : -1;
-            if (!HLLC) sAl[tid] = (p0 + tid < n) ? f64_to_f32(dv.alpha[c]) : 0.0f;
+    const int G = gridDim.x;
+    const float* Ja = dv.Jaf;
+    // the list: count and the first two groups' entries (entries past the count are not used)
+    int n = 0;
+    if (tid < CPB) {
+        n = *dv.lo_count;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int p = (blockIdx.x + j * G) * CPB + tid;
+            const int32_t c = (p < dv.nc) ? dv.lo_list[p] : -1;
+            sCell[j][tid] = (p < n) ? c : -1;
         }
-        __syncthreads();
-        if (sCell[0] < 0) break;  // the list ends before this group (the same for the whole block)
-        const int ncb = (CPB == 1 || sCell[CPB - 1] >= 0) ? CPB : [&] {
-            int k = 1;
-            while (k < CPB && sCell[k] >= 0) ++k;
-            return k;
+    }
+    __syncthreads();
+    if (sCell[0][0] < 0) return;  // the list ends before this block's first group
+    // this thread's node of the first group
+    float pc[5] = {0, 0, 0, 0, 0}, pa = 0.0f, pj[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    auto fetch = [&](int32_t c) {
+        if (c < 0) return;
+        const int64_t dof = (int64_t)c * P3 + node;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) pc[v] = dv.Uf[v * dv.nd + dof];
+#pragma unroll
+        for (int m = 0; m < 9; ++m) pj[m] = Ja[m * dv.nd + dof];
+    };
+    if (cl < CPB) fetch(sCell[0][cl]);
+    if (!HLLC && tid < CPB && sCell[0][tid] >= 0) pa = f64_to_f32(dv.alpha[sCell[0][tid]]);
+    for (int k = 0;; ++k) {
+        const int cur = k & 1;
+        const int ncb = (CPB == 1 || sCell[cur][CPB - 1] >= 0) ? CPB : [&] {
+            int q = 1;
+            while (q < CPB && sCell[cur][q] >= 0) ++q;
+            return q;
         }();
+        // this group's node values, fetched during the previous group
         if (cl < ncb) {
-            const int64_t cell = sCell[cl];
-            const int64_t dof = cell * P3 + node;
 #pragma unroll
-            for (int v = 0; v < 5; ++v) sC[v][cl * P3 + node] = dv.Uf[v * dv.nd + dof];
+            for (int v = 0; v < 5; ++v) sC[v][cl * P3 + node] = pc[v];
 #pragma unroll
-            for (int m = 0; m < 9; ++m) sJ[m][cl * P3 + node] = metric<float>(dv.Ja, dv.Jaf, m * dv.nd + dof);
+            for (int m = 0; m < 9; ++m) sJ[m][cl * P3 + node] = pj[m];
         }
+        if (!HLLC && tid < CPB) sAl[tid] = pa;
         __syncthreads();
+        // in flight during the fluxes: the next group's node values, the list entries after it
+        int32_t after = -1;
+        if (cl < CPB) fetch(sCell[cur ^ 1][cl]);
+        if (tid < CPB) {
+            const int p = (blockIdx.x + (k + 2) * G) * CPB + tid;
+            const int32_t c = (p < dv.nc) ? dv.lo_list[p] : -1;
+            after = (p < n) ? c : -1;
+            if (!HLLC && sCell[cur ^ 1][tid] >= 0) pa = f64_to_f32(dv.alpha[sCell[cur ^ 1][tid]]);
+        }
         for (int ft = tid; ft < ncb * TPC; ft += CB::THREADS) {
             const int tc = ft / TPC, task = ft - tc * TPC;
             float fb = 0.0f;
@@ -161,11 +190,14 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
         }
         __syncthreads();
         if (cl < ncb) {
-            const int64_t o = (int64_t)(p0 + cl) * P3 + node;
+            const int64_t o = (int64_t)((blockIdx.x + k * G) * CPB + cl) * P3 + node;
 #pragma unroll
             for (int v = 0; v < 5; ++v) dv.lo_buf[v * dv.nd + o] = sAcc[cl][v][node] + sAcc[cl][5 + v][node] + sAcc[cl][10 + v][node];
         }
-        __syncthreads();  // shared arrays are reused by the next group
+        // the group after next takes this group's slot; the shared arrays are reused
+        if (tid < CPB) sCell[cur][tid] = after;
+        __syncthreads();
+        if (sCell[cur ^ 1][0] < 0) break;  // the block's next group is empty (the same for the whole block)
     }
 }
 

@@ -26,11 +26,36 @@
 
 namespace plens_gpu {
 
+// Node order of the thread-written per-node arrays at P = 4 (node n = x + 4 y + 16 z stored at
+// (x ^ z) + 4 (y ^ x) + 16 z; the identity at other degrees), with the two cells of a block 16
+// banks apart. The flux phase gives each warp one direction, its lanes the 16 lines of both
+// cells: at every position along the lines the 32 lanes then read 32 different banks in all
+// three directions, and 32 consecutive nodes of one cell (the per-node phases) do too. In the
+// plain order the x and y lines put two lanes on each bank.
+template <int P>
+__device__ __forceinline__ int swz(int n)
+{
+    if constexpr (P == 4) {
+        const int x = n & 3, y = (n >> 2) & 3, z = n >> 4;
+        return (x ^ z) | ((y ^ x) << 2) | (z << 4);
+    } else {
+        return n;
+    }
+}
+
 // Shared-memory layout of one block (bytes), all regions 16-byte aligned.
 template <int P, bool VISC, bool R64>
 struct MxSmem {
     static constexpr int P2 = P * P, P3 = P2 * P, CPB = CellBlock<P>::CPB, NB = CPB * P3, NF = CPB * 6 * P2;
     static constexpr int NQ = 10;  // rho, 1/rho, v0, v1, v2, p, beta, ln rho, ln beta, |v|^2
+    // per-cell strides of the node quantities and partial sums (16 banks between the cells at
+    // P = 4) and of the FP32 metric terms; in the MIXED form the threads write the metric terms
+    // (rounded from FP64) in the swizzled order, the MIXED_R32 form stages its FP32 images as
+    // they lie in memory
+    static constexpr int PAD = (P == 4) ? 16 : 0;
+    static constexpr int QCS = NQ * P3 + PAD, ACS = 15 * P3 + PAD;
+    static constexpr bool JSW = R64 && P == 4;
+    static constexpr int JCS = JSW ? P3 + PAD : P3, JMS = CPB * JCS;  // cell and component strides
     // the warps past the line tasks (phase A) and whether the MIXED form gives them the FP64
     // pre-update, which reads the two older registers from global memory (not staged)
     static constexpr int TPC = 3 * P2;
@@ -45,15 +70,15 @@ struct MxSmem {
     static constexpr size_t oU = 0;                                   // double [5][NB]
     static constexpr size_t oUf = oU + up16(8 * 5 * NB);              // float [5][NB]
     static constexpr size_t oDet = oUf + up16(4 * 5 * NB);            // float [NB] (R64: double [NB])
-    static constexpr size_t oJ = oDet + up16((R64 ? 8 : 4) * NB);     // float [9][NB]
-    static constexpr size_t oR0 = oJ + up16(4 * 9 * NB);              // RB [5][NB]
+    static constexpr size_t oJ = oDet + up16((R64 ? 8 : 4) * NB);     // float [9][JMS]
+    static constexpr size_t oR0 = oJ + up16(4 * 9 * JMS);             // RB [5][NB]
     static constexpr size_t oR1 = oR0 + up16(RB * 5 * NB);            // RB [5][NB]
     static constexpr size_t oSf = oR1 + up16(RB * 5 * NB);            // float [5][NF]
     static constexpr size_t oSf3 = oSf + up16(4 * 5 * NF);            // float [5][NF] (viscous)
     static constexpr size_t oAv = oSf3 + (VISC ? up16(4 * 5 * NF) : 0);  // float [9][NB] (viscous)
-    static constexpr size_t oAcc = oAv + (VISC ? up16(4 * 9 * NB) : 0);  // float [CPB][15][P3]
-    static constexpr size_t oQ = oAcc + up16(4 * 15 * NB);            // float [CPB][NQ][P3]
-    static constexpr size_t bytes = oQ + up16(4 * NQ * NB);
+    static constexpr size_t oAcc = oAv + (VISC ? up16(4 * 9 * NB) : 0);  // float [CPB][ACS]: [15][P3]
+    static constexpr size_t oQ = oAcc + up16(4 * CPB * ACS);          // float [CPB][QCS]: [NQ][P3]
+    static constexpr size_t bytes = oQ + up16(4 * CPB * QCS);
 };
 
 // Resident blocks per SM the register allocation is sized for: 128-thread blocks at P = 2, 4 --
@@ -70,6 +95,9 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
     using L = MxSmem<P, VISC, R64>;
     using RT = typename std::conditional<R64, double, float>::type;  // register storage type
     constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, N = P - 1, NQ = L::NQ, NB = L::NB, NF = L::NF;
+    constexpr int QCS = L::QCS, ACS = L::ACS, JCS = L::JCS, JMS = L::JMS;
+    // index of node n in the metric-term array (swizzled where the threads write it)
+    auto jx = [](int n) { return L::JSW ? swz<P>(n) : n; };
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bars[2];
     double* stU = reinterpret_cast<double*>(smem_raw + L::oU);
@@ -143,7 +171,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
 #pragma unroll
         for (int m = 0; m < 9; ++m) ja[m] = dv.Ja[m * dv.nd + dn];
 #pragma unroll
-        for (int m = 0; m < 9; ++m) stJ[m * NB + cl * P3 + node] = f64_to_f32(ja[m]);
+        for (int m = 0; m < 9; ++m) stJ[m * JMS + cl * JCS + jx(node)] = f64_to_f32(ja[m]);
     }
     __syncthreads();  // barrier initialisation visible to every thread
     // the block takes one decision: a wait that ran out anywhere ends the block (error status set,
@@ -156,10 +184,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
     }
 
     const float gm = f64_to_f32(g.gamma);
-    float* Q = sQ + cl * NQ * P3;
+    float* Q = sQ + cl * QCS;  // quantity k at node n of this cell: Q[k * P3 + swz(n)]
     const float* Cc = stUf + cl * P3;  // the FP32 state image: variable v at node n is Cc[v * NB + n]
-    const float* J = stJ + cl * P3;  // component m of Ja at node n of this cell: J[m * NB + n]
-    float* Acc = sAcc + cl * 15 * P3;
+    const float* J = stJ + cl * JCS;  // component m of Ja at node n of this cell: J[m * JMS + jx(n)]
+    float* Acc = sAcc + cl * ACS;  // partial sum k at node n of this cell: Acc[k * P3 + swz(n)]
+    const int sn = swz<P>(node), jn0 = jx(node);
     const int64_t dof = cell * P3 + node;
     const int bn = cl * P3 + node;  // node index within the block's staged chunks
     if (valid) {
@@ -169,16 +198,16 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
         const float p = get_p(c, gm);
         const float ri = 1.0f / c[0];
         const float v0 = c[1] * ri, v1 = c[2] * ri, v2 = c[3] * ri, beta = 0.5f * c[0] / p;
-        Q[0 * P3 + node] = c[0];
-        Q[1 * P3 + node] = ri;
-        Q[2 * P3 + node] = v0;
-        Q[3 * P3 + node] = v1;
-        Q[4 * P3 + node] = v2;
-        Q[5 * P3 + node] = p;
-        Q[6 * P3 + node] = beta;
-        Q[7 * P3 + node] = __logf(c[0]);
-        Q[8 * P3 + node] = __logf(beta);
-        Q[9 * P3 + node] = v0 * v0 + v1 * v1 + v2 * v2;
+        Q[0 * P3 + sn] = c[0];
+        Q[1 * P3 + sn] = ri;
+        Q[2 * P3 + sn] = v0;
+        Q[3 * P3 + sn] = v1;
+        Q[4 * P3 + sn] = v2;
+        Q[5 * P3 + sn] = p;
+        Q[6 * P3 + sn] = beta;
+        Q[7 * P3 + sn] = __logf(c[0]);
+        Q[8 * P3 + sn] = __logf(beta);
+        Q[9 * P3 + sn] = v0 * v0 + v1 * v1 + v2 * v2;
     }
     __syncthreads();
     const double alpha = valid ? dv.alpha[cell] : 0.0;
@@ -214,13 +243,25 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
     }
     {
         const float hg = __fdividef(0.5f, gm - 1.0f), gf = __fdividef(gm, gm - 1.0f);
-        for (int ft = tid; ft < ncb * TPC && tid < TF; ft += TF) {
-            const int tc = ft / TPC, task = ft - tc * TPC;
-            const float* Qa = sQ + tc * NQ * P3;
+        for (int ft = tid; ft < CPB * TPC && tid < TF; ft += TF) {
+            // P = 4: warp dir, lanes (cell, line); otherwise the tasks of a cell in a row
+            int tc, dir, line;
+            if constexpr (P == 4 && CPB == 2 && TF == 96) {
+                dir = ft >> 5;
+                tc = (ft >> 4) & 1;
+                line = ft & 15;
+            } else {
+                tc = ft / TPC;
+                const int task = ft - tc * TPC;
+                dir = task / P2;
+                line = task - dir * P2;
+            }
+            if (tc >= ncb) continue;
+            const float* Qa = sQ + tc * QCS;
             const float* Ca = stUf + tc * P3;
-            const float* Jt = stJ + tc * P3;
-            float* At = sAcc + tc * 15 * P3;
-            const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
+            const float* Jt = stJ + tc * JCS;
+            float* At = sAcc + tc * ACS;
+            const int la = line % P, lb = line / P;
             float acc[P][5];
 #pragma unroll
             for (int i = 0; i < P; ++i)
@@ -231,11 +272,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
             // (D_ii = 0 at interior GLL nodes)
 #pragma unroll
             for (int i = 0; i < P; ++i) {
-                const int ni = line_node<P>(dir, la, lb, i);
+                const int ni = line_node<P>(dir, la, lb, i), qni = swz<P>(ni), jni = jx(ni);
                 float qi[10];
 #pragma unroll
-                for (int k = 0; k < 10; ++k) qi[k] = Qa[k * P3 + ni];
-                const float ji[3] = {Jt[(dir * 3) * NB + ni], Jt[(dir * 3 + 1) * NB + ni], Jt[(dir * 3 + 2) * NB + ni]};
+                for (int k = 0; k < 10; ++k) qi[k] = Qa[k * P3 + qni];
+                const float ji[3] = {Jt[(dir * 3) * JMS + jni], Jt[(dir * 3 + 1) * JMS + jni], Jt[(dir * 3 + 2) * JMS + jni]};
                 if (i == 0 || i == N) {
                     float F[5];
                     chandrashekhar_same_f32(qi, ji, gf, F);
@@ -245,12 +286,12 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
                 }
 #pragma unroll
                 for (int m = i + 1; m < P; ++m) {
-                    const int nm = line_node<P>(dir, la, lb, m);
+                    const int nm = line_node<P>(dir, la, lb, m), qnm = swz<P>(nm), jnm = jx(nm);
                     float qm[10];
 #pragma unroll
-                    for (int k = 0; k < 10; ++k) qm[k] = Qa[k * P3 + nm];
-                    const float nv[3] = {ji[0] + Jt[(dir * 3) * NB + nm], ji[1] + Jt[(dir * 3 + 1) * NB + nm],
-                                         ji[2] + Jt[(dir * 3 + 2) * NB + nm]};
+                    for (int k = 0; k < 10; ++k) qm[k] = Qa[k * P3 + qnm];
+                    const float nv[3] = {ji[0] + Jt[(dir * 3) * JMS + jnm], ji[1] + Jt[(dir * 3 + 1) * JMS + jnm],
+                                         ji[2] + Jt[(dir * 3 + 2) * JMS + jnm]};
                     float F[5];
                     chandrashekhar_pair_f32(qi, qm, nv, hg, F);
                     const float di = opD<float>(ops, i * P + m), dm = opD<float>(ops, m * P + i);
@@ -280,7 +321,8 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
                     const int i = lr ? N : 0;
                     const int ni = line_node<P>(dir, la, lb, i);
                     const int f = 2 * dir + lr;
-                    const float jn[3] = {Jt[(dir * 3) * NB + ni], Jt[(dir * 3 + 1) * NB + ni], Jt[(dir * 3 + 2) * NB + ni]};
+                    const int jni = jx(ni);
+                    const float jn[3] = {Jt[(dir * 3) * JMS + jni], Jt[(dir * 3 + 1) * JMS + jni], Jt[(dir * 3 + 2) * JMS + jni]};
                     const float nn = sqrtf(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
                     const float ci[5] = {Ca[ni], Ca[NB + ni], Ca[2 * NB + ni], Ca[3 * NB + ni], Ca[4 * NB + ni]};
                     float fin[5];
@@ -296,9 +338,9 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
             }
 #pragma unroll
             for (int i = 0; i < P; ++i) {
-                const int ni = line_node<P>(dir, la, lb, i);
+                const int qni = swz<P>(line_node<P>(dir, la, lb, i));
 #pragma unroll
-                for (int v = 0; v < 5; ++v) At[(dir * 5 + v) * P3 + ni] = acc[i][v];
+                for (int v = 0; v < 5; ++v) At[(dir * 5 + v) * P3 + qni] = acc[i][v];
             }
         }
     }
@@ -318,7 +360,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
     if (valid) {
         const float js = R64 ? 1.0f : __fdividef(-1.0f, detJ);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) ho[v] = (Acc[v * P3 + node] + Acc[(5 + v) * P3 + node] + Acc[(10 + v) * P3 + node]) * js;
+        for (int v = 0; v < 5; ++v) ho[v] = (Acc[v * P3 + sn] + Acc[(5 + v) * P3 + sn] + Acc[(10 + v) * P3 + sn]) * js;
     }
 
     // ---- viscous HO residual: nodal viscous fluxes along each contravariant direction
@@ -332,11 +374,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
             const float ci[5] = {Cc[node], Cc[NB + node], Cc[2 * NB + node], Cc[3 * NB + node], Cc[4 * NB + node]};
 #pragma unroll
             for (int md = 0; md < 3; ++md) {
-                const float jn[3] = {J[(md * 3) * NB + node], J[(md * 3 + 1) * NB + node], J[(md * 3 + 2) * NB + node]};
+                const float jn[3] = {J[(md * 3) * JMS + jn0], J[(md * 3 + 1) * JMS + jn0], J[(md * 3 + 2) * JMS + jn0]};
                 float F[5];
                 dif_flux(ci, av, jn, F);  // linear in the direction: F(n/|n|) |n| = F(n)
 #pragma unroll
-                for (int v = 0; v < 5; ++v) Acc[(md * 5 + v) * P3 + node] = F[v];
+                for (int v = 0; v < 5; ++v) Acc[(md * 5 + v) * P3 + sn] = F[v];
             }
         }
         __syncthreads();
@@ -347,7 +389,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
                     const int lo = (md == 0) ? m + P * ti[1] + P2 * ti[2] : (md == 1) ? ti[0] + P * m + P2 * ti[2] : ti[0] + P * ti[1] + P2 * m;
                     const float dvl = opD<float>(ops, ti[md] * P + m);
 #pragma unroll
-                    for (int v = 0; v < 5; ++v) hd[v] += dvl * Acc[(md * 5 + v) * P3 + lo];
+                    for (int v = 0; v < 5; ++v) hd[v] += dvl * Acc[(md * 5 + v) * P3 + swz<P>(lo)];
                 }
             }
             const float ci[5] = {Cc[node], Cc[NB + node], Cc[2 * NB + node], Cc[3 * NB + node], Cc[4 * NB + node]};
@@ -359,7 +401,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
                     if (ti[sd] != (lr ? N : 0)) continue;
                     const int f = 2 * sd + lr;
                     const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
-                    const float jn[3] = {J[(sd * 3) * NB + node], J[(sd * 3 + 1) * NB + node], J[(sd * 3 + 2) * NB + node]};
+                    const float jn[3] = {J[(sd * 3) * JMS + jn0], J[(sd * 3 + 1) * JMS + jn0], J[(sd * 3 + 2) * JMS + jn0]};
                     const float nn = sqrtf(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
                     float fin[5];
                     dif_flux(ci, av, jn, fin);
@@ -399,7 +441,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
                     if (ti[sd] != (lr ? N : 0)) continue;
                     const int f = 2 * sd + lr;
                     const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
-                    const float j0 = J[(sd * 3) * NB + node], j1 = J[(sd * 3 + 1) * NB + node], j2 = J[(sd * 3 + 2) * NB + node];
+                    const float j0 = J[(sd * 3) * JMS + jn0], j1 = J[(sd * 3 + 1) * JMS + jn0], j2 = J[(sd * 3 + 2) * JMS + jn0];
                     const float sw = __fdividef(sqrtf(j0 * j0 + j1 * j1 + j2 * j2), opW<float>(ops, lr * N));
 #pragma unroll
                     for (int v = 0; v < 5; ++v) lo[v] += sfa[v * NF + f * P2 + q] * sw;
@@ -450,7 +492,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
                     if (sa.stage >= 2) un = __fma_rn(sa.c1, stR1[v * NB + bn], un);
                     un = __fma_rn(sa.c2, Rs, un);
                 }
-                sa.Rw[k] = Rs;
+                if (sa.keep) sa.Rw[k] = Rs;
             } else {
                 if (sa.stage == 1) un = u + Rs;
                 else if (sa.stage == 2) un = 0.75 * dv.U0[k] + 0.25 * u + 0.25 * Rs;
@@ -488,7 +530,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
             if (sa.stage == 1) inc = sa.fc2 * Rs;
             else if (sa.stage == 2) inc = sa.fc1 * (float)stR1[v * NB + bn] + sa.fc2 * Rs;
             else inc = sa.fc0 * (float)stR0[v * NB + bn] + sa.fc1 * (float)stR1[v * NB + bn] + sa.fc2 * Rs;
-            as_real<float>(sa.Rw)[k] = Rs;
+            if (sa.keep) as_real<float>(sa.Rw)[k] = Rs;
             const double un = u + f32_to_f64(inc);
             dv.U[k] = un;
             dv.Uf[k] = f64_to_f32(un);

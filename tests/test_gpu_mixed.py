@@ -72,7 +72,7 @@ def test_mixed_sod(prec):
     assert _steps_err(configs.sod(n=40), configs.sod(n=40, precision=prec), 100).max() <= STEPS_TOL
 
 
-@pytest.mark.parametrize("scheme", ["Rusanov", "AUSM+-up", "Rusanov-HLLC", "Chandrashekhar"])
+@pytest.mark.parametrize("scheme", ["Rusanov", "AUSM+-up", "Rusanov-HLLC", "Chandrashekhar", "Modified SW"])
 def test_mixed_surface_schemes(scheme):
     def spec(prec):
         prm, files, deg = configs.dmr(nx=12, ny=4, precision=prec)
@@ -120,6 +120,49 @@ def test_mixed_viscous_shock_vortex(prec):
     print(f"shock-vortex rhs err {e:.3e}")
     assert e <= RHS_TOL
     s = _steps_err(configs.shock_vortex(n=3, modes=2), configs.shock_vortex(n=3, modes=2, precision=prec), 5)
+    assert s.max() <= STEPS_TOL
+
+
+def _all_troubled(spec):
+    """The same workload with the blender's threshold factor at 1e-6 (threshold 2.9e-9 at N = 3):
+    with the DMR's pre-shock density noise at 1e-3 the cells' high-mode energies (~1e-6) clear
+    it by orders of magnitude in both precisions, and 90% of the cells are troubled after two
+    steps. (Noise near the FP32 rounding level would leave the FP32 and FP64 indicators deciding
+    different cells.)"""
+    prm, files, deg = spec
+    key = "    set wall blender limit = 0\n"
+    assert key in prm
+    return prm.replace(key, key + "    set threshold factor = 1e-6\n"), files, deg
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_mixed_long_troubled_list(prec):
+    """A troubled-cell list long enough that every block of the subcell kernel's persistent grid
+    (at most two blocks per SM, two cells per group) takes several groups, so its pipelined loads
+    of the next group and of the list entries after it all run: one RHS against the oracle, the
+    list against the oracle's alpha > 0, and 20 steps."""
+    spec64 = _all_troubled(configs.dmr(nx=120, ny=30, noise=1e-3))
+    specmx = _all_troubled(configs.dmr(nx=120, ny=30, noise=1e-3, precision=prec))
+    c64, cmx = make(spec64), make(specmx)
+    U, t = _state(c64, 2)
+    o = Oracle(c64)
+    o.set_state(U, t)
+    Ro, alpha_o, _ = o.rhs()
+    g = GpuSolver(cmx)
+    g.set_state(U, t)
+    Rg = g.rhs()
+    cells = g.troubled_cells()
+    g.close()
+    ref = np.flatnonzero(alpha_o > 0)
+    print(f"{len(cells)} listed cells, oracle {len(ref)}")
+    assert len(cells) > 4 * 2 * 152 * 2
+    assert np.all(np.diff(cells) > 0)
+    assert len(np.setxor1d(cells, ref)) <= 0.01 * len(ref)
+    e = max_rel_err(Rg, Ro)
+    print(f"rhs err {e:.3e}")
+    assert e <= RHS_TOL
+    s = _steps_err(spec64, specmx)
+    print(f"20-step rel L1 {s}")
     assert s.max() <= STEPS_TOL
 
 

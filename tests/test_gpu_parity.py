@@ -111,7 +111,7 @@ def test_end_time_clip_matches():
     assert rel_l1(g.get_state(), Uo).max() <= STEPS_TOL
 
 
-@pytest.mark.parametrize("scheme", ["Rusanov", "AUSM+-up", "Rusanov-HLLC", "Chandrashekhar"])
+@pytest.mark.parametrize("scheme", ["Rusanov", "AUSM+-up", "Rusanov-HLLC", "Chandrashekhar", "Modified SW"])
 def test_surface_schemes_rhs_parity(scheme):
     prm, files, deg = configs.sod(n=20)
     prm = prm.replace("set inviscid surface flux scheme = HLLC", f"set inviscid surface flux scheme = {scheme}")

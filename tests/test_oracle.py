@@ -178,3 +178,38 @@ def test_positivity_failure_is_reported():
     with pytest.raises(pyoracle.OracleError) as e:
         o.rhs()
     assert e.value.status == 3 and e.value.dof == 7
+
+
+def test_modified_steger_warming_flux(air_params):
+    """The modified Steger-Warming flux (navier_stokes.cc:1172-1234): identical states give the
+    physical flux (the pressure weight is 1/2, A+ + A- = A and A u = F(u)), and the flux is
+    invariant under rotations of the states and the normal (the rotation to the normal frame of
+    navier_stokes.cc:482-569)."""
+    prm = air_params.params
+    old = prm.inv_surf_flux
+    prm.inv_surf_flux = 5  # PLENS_ISF_MODIFIED_SW
+    try:
+        pp = air_params.params_ptr
+        s = [1.3, 0.4, -0.2, 0.1, 3.1]
+        n = np.array([0.3, -0.5, 0.8])
+        n /= np.linalg.norm(n)
+        rho, m, E = s[0], np.array(s[1:4]), s[4]
+        p = 0.4 * (E - 0.5 * m @ m / rho)
+        vn = m @ n / rho
+        phys = np.r_[rho * vn, vn * m + p * n, (E + p) * vn]
+        np.testing.assert_allclose(pyoracle.flux(pp, 0, s, s, n), phys, rtol=1e-12, atol=1e-13)
+        ocs, ncs = [1.5, 3, 1.5, 4.5, 23], [2, 2, 4, 4, 34]
+        fx = pyoracle.flux(pp, 0, ocs, ncs, [1, 0, 0])
+        f = pyoracle.flux(pp, 0, [1.5, -3, -1.5, -4.5, 23], [2, -2, -4, -4, 34], [-1, 0, 0])
+        np.testing.assert_allclose(f, [fx[0], -fx[1], -fx[2], -fx[3], fx[4]], rtol=1e-12, atol=1e-12)
+        th = 0.7
+        R = np.array([[np.cos(th), -np.sin(th), 0], [np.sin(th), np.cos(th), 0], [0, 0, 1]])
+        o2 = np.r_[ocs[0], R @ np.array(ocs[1:4]), ocs[4]]
+        n2 = np.r_[ncs[0], R @ np.array(ncs[1:4]), ncs[4]]
+        f = pyoracle.flux(pp, 0, o2, n2, R @ np.array([1.0, 0, 0]))
+        np.testing.assert_allclose(f, np.r_[fx[0], R @ fx[1:4], fx[4]], rtol=1e-12, atol=1e-12)
+        # the flux differs from HLLC's on a jump (a different scheme is evaluated)
+        prm.inv_surf_flux = 0
+        assert np.abs(pyoracle.flux(pp, 0, ocs, ncs, [1, 0, 0]) - fx).max() > 1e-3
+    finally:
+        prm.inv_surf_flux = old
