@@ -45,6 +45,11 @@ UNIT = "DOF-stage/s"
 # read, 20 written at stages 1-4) and the kernel reads the FP32 images of Ja and detJ (40):
 # 80 + 40 + 16 + 40 = 176.
 BYTES_PER_DOF_STAGE = {"plain": 272, "modal": 272, "learned": 272, "learned_r32": 176}
+# What the MIXED form's volume kernel actually reads and writes per DOF-stage at N = 3, averaged
+# over the five stages (it reads no register where the stage's coefficient is zero, and it moves
+# the FP32 state image and the face values, which the algorithmic count leaves out): 80 (state)
+# + 56 + 32 (registers) + 36 + 8 (Ja image, 1/detJ) + 40 (state image) + 30 (face values).
+MOVED_BYTES_MIXED = 282
 WORKLOAD = "double Mach reflection 240x60x1 cells, N=3, 921600 DoFs, RK4(3)5[3R+]N, HLLC + Chandrashekhar"
 
 
@@ -751,10 +756,17 @@ def main():
             "peak_kind": peak_kind, "kernel": f"k_volume_mx (mixed form, {fast_sensor} sensor)",
             "traffic": _traffic_from_profile("k_volume_mx_dmr.md"),
             "note": "achieved: algorithmic 272 B per DOF-stage (FP64 state r/w 80, two FP64 registers read "
-                    "80, one written 40 at stages 1-4 (none at the last stage, whose dt*R no stage reads), FP64 "
+                    "80, one written 40 at stages 1-4 (none at the last stage, whose dt*R no stage reads), "
                     "Ja and 1/detJ 80) x 921600 DoFs per launch / mean CUDA-event launch time of the "
                     "kernel-timing pass; traffic: ncu DRAM bytes of a stage-1 launch from "
                     "profiles/k_volume_mx_dmr.md",
+            "moved_bytes_per_dof_stage": MOVED_BYTES_MIXED,
+            "achieved_moved": MOVED_BYTES_MIXED * achieved / BYTES_PER_DOF_STAGE["learned"],
+            "moved_note": "what the kernel reads and writes per DOF-stage, averaged over the five stages: FP64 "
+                          "state r/w 80; FP64 registers read 56 (none at stage 1, one at stage 2, two at "
+                          "stages 3-5) and written 32; the FP32 rounding of Ja 36 (an image made once, the "
+                          "values of rounding the FP64 Ja) and FP64 1/detJ 8; the FP32 state image r/w 40; "
+                          "the FP32 face values 30",
         },
         "e2e": {"value": hd["e2e"], "unit": UNIT, "h2d_bytes_per_step": fast["bytes_state"],
                 "d2h_bytes_per_step": fast["bytes_state"],

@@ -70,7 +70,8 @@ __device__ __forceinline__ void cbm_mma(uint32_t d, const float* a_hi, const flo
 constexpr int kBtcThreads = 512;
 
 template <int P>
-__global__ void __launch_bounds__(kBtcThreads, 1) k_blender_tc(Dev dv, const float* __restrict__ Btc, GasP g, BlendP bp, Ops ops)
+__global__ void __launch_bounds__(kBtcThreads, 1) k_blender_tc(Dev dv, const float* __restrict__ Btc, GasP g, BlendP bp, Ops ops,
+                                                               int tr)
 {
     static_assert(P == 4, "the tensor-core change of basis is the 64 x 64 matrix of degree 3");
     constexpr int N = 3, P3 = 64, R = tc::kRows;
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(kBtcThreads, 1) k_blender_tc(Dev dv, const flo
     Scalars* s = dv.sc;
     if (!s->active) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int64_t ntiles = (dv.nc + R - 1) / R;
+    const int64_t ntiles = (dv.nc + tr - 1) / tr;  // tiles of tr <= R cells
     const float gm = f64_to_f32(g.gamma);
     if (warp == 0) tc::tmem_alloc(&tmem_base);
     if (tid == 0) {
@@ -107,8 +108,8 @@ __global__ void __launch_bounds__(kBtcThreads, 1) k_blender_tc(Dev dv, const flo
         if (ok) ph ^= 1;
     };
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t c0 = tile * R;
-        const int ncell = (int)((dv.nc - c0 < R) ? dv.nc - c0 : R);
+        const int64_t c0 = tile * tr;
+        const int ncell = (int)((dv.nc - c0 < tr) ? dv.nc - c0 : tr);
         // ---- staging: one thread issues the copies (and, first, B)
         if (tid == 0) {
             const uint32_t bv = (uint32_t)(ncell * P3 * 4);

@@ -316,6 +316,24 @@ __device__ __forceinline__ int face_node(int f, int q)
     }
 }
 
+// Node order of the thread-written per-node shared arrays of the line-task kernels (the mixed
+// volume and subcell kernels) at P = 4: node n = x + 4 y + 16 z is stored at (x ^ z) +
+// 4 (y ^ x) + 16 z (the identity at other degrees), with the two cells of a block 16 banks apart.
+// Their line phases give each warp one direction, its lanes the 16 lines of both cells: at every
+// position along the lines the 32 lanes then read 32 different banks in all three directions,
+// and 32 consecutive nodes of one cell (the per-node phases) do too. In the plain order the x
+// and y lines put two lanes on each bank.
+template <int P>
+__device__ __forceinline__ int swz(int n)
+{
+    if constexpr (P == 4) {
+        const int x = n & 3, y = (n >> 2) & 3, z = n >> 4;
+        return (x ^ z) | ((y ^ x) << 2) | (z << 4);
+    } else {
+        return n;
+    }
+}
+
 // node index of position i along direction dir on the line (a, b) of the other two directions
 template <int P>
 __device__ __forceinline__ int line_node(int dir, int a, int b, int i)

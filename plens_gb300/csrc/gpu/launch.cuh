@@ -50,8 +50,9 @@ struct Launch {
             cudaFuncSetAttribute(k_blender_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BtcSmem::bytes);
             if (nsm < 1) nsm = 1;
         }
-        const int64_t tiles = (dv.nc + tc::kRows - 1) / tc::kRows;
-        k_blender_tc<P><<<(unsigned)(tiles < nsm ? tiles : nsm), kBtcThreads, BtcSmem::bytes, st>>>(dv, Btc, g, bp, ops);
+        const int tr = tc::tile_rows(dv.nc, nsm);
+        const int64_t tiles = (dv.nc + tr - 1) / tr;
+        k_blender_tc<P><<<(unsigned)(tiles < nsm ? tiles : nsm), kBtcThreads, BtcSmem::bytes, st>>>(dv, Btc, g, bp, ops, tr);
         return 1;
     }
     template <bool HLLC>

@@ -677,7 +677,7 @@ struct SensorTcSmem {
 template <int P>
 __global__ void __launch_bounds__(kBtcThreads, 1) k_sensor_tc(Dev dv, const float* __restrict__ Wtc,
                                                               const float* __restrict__ Ctc, BlendP bp, GasP g,
-                                                              double* out, int gated, const uint8_t* mask)
+                                                              double* out, int gated, const uint8_t* mask, int tr)
 {
     static_assert(P == 4, "the fused tensor-core sensor takes the 4^3 nodes of degree 3 as its inputs");
     constexpr int N = 3, P3 = 64, R = tc::kRows;
@@ -706,7 +706,7 @@ __global__ void __launch_bounds__(kBtcThreads, 1) k_sensor_tc(Dev dv, const floa
     // whole-domain fallback: every cell takes the plain indicator computed here
     const bool all_plain = gated && s->sensor_fallback;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int64_t ntiles = (dv.nc + R - 1) / R;
+    const int64_t ntiles = (dv.nc + tr - 1) / tr;  // tiles of tr <= R cells
     const float gm = f64_to_f32(g.gamma);
     const float cut = fmaxf(f64_to_f32(bp.amin), kLearnedCut), amax = f64_to_f32(bp.amax);
     constexpr uint32_t kCols = 256;  // three 64-column accumulators
@@ -735,8 +735,8 @@ __global__ void __launch_bounds__(kBtcThreads, 1) k_sensor_tc(Dev dv, const floa
     };
     const int node = tid & 63, q = warp & 3, cg = warp >> 2;
     for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int64_t c0 = tile * R;
-        const int ncell = (int)((dv.nc - c0 < R) ? dv.nc - c0 : R);
+        const int64_t c0 = tile * tr;
+        const int ncell = (int)((dv.nc - c0 < tr) ? dv.nc - c0 : tr);
         float v[16];
         // ---- two halves of 64 cells: stage, rho*p, the per-cell sums
         for (int h = 0; h < 2 && ok; ++h) {
@@ -923,9 +923,10 @@ int launch_sensor_tc(MlpDevice& m, const Dev& dv, const GasP& g, const BlendP& b
             cudaFuncSetAttribute(k_sensor_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SensorTcSmem::bytes);
             nsm = std::max(1, nsm);
         }
-        const int64_t tiles = (dv.nc + tc::kRows - 1) / tc::kRows;
+        const int tr = tc::tile_rows(dv.nc, nsm);
+        const int64_t tiles = (dv.nc + tr - 1) / tr;
         k_sensor_tc<P><<<(unsigned)std::min<int64_t>(tiles, nsm), kBtcThreads, SensorTcSmem::bytes, st>>>(
-            dv, m.params_tc, m.cbm, bp, g, out, gated, mask);
+            dv, m.params_tc, m.cbm, bp, g, out, gated, mask, tr);
         return 1;
     } else {
         return 0;

@@ -25,6 +25,19 @@ constexpr int kMatA = kRows * kK * 4;            // bytes of one A operand (hi o
 constexpr int kMatB = kN * kK * 4;               // bytes of one B operand
 constexpr uint32_t kTmemCols = 64;               // FP32 accumulator 128 lanes x 64 columns
 
+// Cells per tile of the one-tile-per-SM kernels (the tensor-core indicators): the fewest tiles
+// that fill the SMs evenly -- ceil(nc / (nsm * waves)) rows with waves = ceil(nc / (nsm * kRows))
+// -- so that a mesh of fewer than nsm x 128 cells spreads over every SM instead of leaving some
+// idle (14,400 cells: 152 tiles of 95 instead of 113 of 128). The rows past a tile's cells are
+// zero operands.
+inline int tile_rows(int64_t nc, int nsm)
+{
+    if (nc < 1 || nsm < 1) return kRows;
+    const int64_t cap = (int64_t)nsm * kRows, waves = (nc + cap - 1) / cap;
+    const int64_t per = (nc + (int64_t)nsm * waves - 1) / ((int64_t)nsm * waves);
+    return (int)(per < 1 ? 1 : (per > kRows ? kRows : per));
+}
+
 // float offset of element (row r, k) in the canonical K-major no-swizzle layout of a 64-wide K
 __host__ __device__ __forceinline__ int core_off(int r, int k)
 {

@@ -678,10 +678,10 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
         CK(cudaDeviceSynchronize());  // the uploads above ran on the legacy stream
         k_reciprocal<<<(unsigned)std::min<int64_t>((nd + 255) / 256, 152 * 16), 256, 0, c->stream>>>(d.detJ, invJ, nd);
         // The FP32 consumers of the metric terms (the time step's estimate from J^-1; the
-        // auxiliary-variable and subcell kernels' FP32 arithmetic on Ja and detJ) read the FP32
-        // rounding of the FP64 arrays from images made once: the same values as rounding the FP64
-        // arrays where they are read, half the bytes. The volume kernel reads the FP64 Ja and
-        // rounds it itself; 1/detJ and the register arithmetic stay FP64.
+        // volume, auxiliary-variable and subcell kernels' FP32 arithmetic on Ja and det J) read
+        // the FP32 rounding of the FP64 arrays from images made once: the same values as
+        // rounding the FP64 arrays where they are read, half the bytes and no conversions.
+        // 1/detJ and the register arithmetic stay FP64.
         float *Jinvf = nullptr, *Jaf = nullptr, *detJf = nullptr;
         if ((r = dalloc(c, &Jinvf, 9 * nd)) || (r = dalloc(c, &Jaf, 9 * nd)) || (r = dalloc(c, &detJf, nd))) return r;
         const unsigned grid = (unsigned)std::min<int64_t>((9 * nd + 255) / 256, 152 * 16);

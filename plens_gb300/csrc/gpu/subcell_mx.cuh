@@ -77,11 +77,13 @@ template <int P, bool HLLC>
 __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Ops ops, GasP g)
 {
     using CB = CellBlock<P>;
-    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB, NB = CPB * P3;
+    constexpr int P2 = CB::P2, P3 = CB::P3, CPB = CB::CPB;
     constexpr int TPC = 3 * P2;
-    __shared__ float sC[5][NB];   // FP32 state image
-    __shared__ float sJ[9][NB];   // FP32 rounding of Ja
-    __shared__ float sAcc[CPB][15][P3];
+    // node arrays in the swizzled order with the cells 16 banks apart at P = 4 (swz, device.cuh)
+    constexpr int PAD = (P == 4) ? 16 : 0, CS = P3 + PAD, NBS = CPB * CS, ACS = 15 * P3 + PAD;
+    __shared__ float sC[5][NBS];  // FP32 state image: variable v of node n of cell c at [v][c CS + swz(n)]
+    __shared__ float sJ[9][NBS];  // FP32 rounding of Ja, the same order
+    __shared__ float sAcc[CPB * ACS];  // partial sum k of node n of cell c at [c ACS + k P3 + swz(n)]
     __shared__ float sAl[CPB];
     __shared__ int32_t sCell[2][CPB];  // cells of this group and of the block's next group
     Scalars* s = dv.sc;
@@ -124,10 +126,11 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
         }();
         // this group's node values, fetched during the previous group
         if (cl < ncb) {
+            const int bn = cl * CS + swz<P>(node);
 #pragma unroll
-            for (int v = 0; v < 5; ++v) sC[v][cl * P3 + node] = pc[v];
+            for (int v = 0; v < 5; ++v) sC[v][bn] = pc[v];
 #pragma unroll
-            for (int m = 0; m < 9; ++m) sJ[m][cl * P3 + node] = pj[m];
+            for (int m = 0; m < 9; ++m) sJ[m][bn] = pj[m];
         }
         if (!HLLC && tid < CPB) sAl[tid] = pa;
         __syncthreads();
@@ -140,33 +143,45 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
             after = (p < n) ? c : -1;
             if (!HLLC && sCell[cur ^ 1][tid] >= 0) pa = f64_to_f32(dv.alpha[sCell[cur ^ 1][tid]]);
         }
-        for (int ft = tid; ft < ncb * TPC; ft += CB::THREADS) {
-            const int tc = ft / TPC, task = ft - tc * TPC;
+        for (int ft = tid; ft < CPB * TPC; ft += CB::THREADS) {
+            // P = 4: warp dir, lanes (cell, line); otherwise the tasks of a cell in a row
+            int tc, dir, line;
+            if constexpr (P == 4 && CPB == 2) {
+                dir = ft >> 5;
+                tc = (ft >> 4) & 1;
+                line = ft & 15;
+            } else {
+                tc = ft / TPC;
+                const int task = ft - tc * TPC;
+                dir = task / P2;
+                line = task - dir * P2;
+            }
+            if (tc >= ncb) continue;
             float fb = 0.0f;
             if (!HLLC) {
                 const float at = sAl[tc];
                 fb = (at <= 0.0f) ? 0.0f : (at <= 1.0f ? at : 1.0f);  // the cell's alpha as flux blender (plens.cc:3492)
             }
-            const int dir = task / P2, line = task - dir * P2, la = line % P, lb = line / P;
-            const int base = tc * P3;
+            const int la = line % P, lb = line / P;
+            const int base = tc * CS;
             float acc[P][5];
 #pragma unroll
             for (int i = 0; i < P; ++i)
 #pragma unroll
                 for (int v = 0; v < 5; ++v) acc[i][v] = 0.0f;
             // running subcell normal n_(i-1,i) = Ja_0 + sum_{l<i} sum_m Q_lm Ja_m (metric_terms.cc:106-141)
-            const int n0 = base + line_node<P>(dir, la, lb, 0);
+            const int n0 = base + swz<P>(line_node<P>(dir, la, lb, 0));
             float sn[3] = {sJ[dir * 3][n0], sJ[dir * 3 + 1][n0], sJ[dir * 3 + 2][n0]};
 #pragma unroll
             for (int id = 1; id < P; ++id) {
 #pragma unroll
                 for (int m = 0; m < P; ++m) {
-                    const int nm = base + line_node<P>(dir, la, lb, m);
+                    const int nm = base + swz<P>(line_node<P>(dir, la, lb, m));
                     const float qlm = opQ<float>(ops, (id - 1) * P + m);
 #pragma unroll
                     for (int d = 0; d < 3; ++d) sn[d] += qlm * sJ[dir * 3 + d][nm];
                 }
-                const int nl = base + line_node<P>(dir, la, lb, id - 1), nr = base + line_node<P>(dir, la, lb, id);
+                const int nl = base + swz<P>(line_node<P>(dir, la, lb, id - 1)), nr = base + swz<P>(line_node<P>(dir, la, lb, id));
                 const float nn = sqrtf(sn[0] * sn[0] + sn[1] * sn[1] + sn[2] * sn[2]);
                 const float dn[3] = {__fdividef(sn[0], nn), __fdividef(sn[1], nn), __fdividef(sn[2], nn)};
                 const float cL[5] = {sC[0][nl], sC[1][nl], sC[2][nl], sC[3][nl], sC[4][nl]};
@@ -183,16 +198,19 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
             }
 #pragma unroll
             for (int i = 0; i < P; ++i) {
-                const int ni = line_node<P>(dir, la, lb, i);
+                const int ni = tc * ACS + swz<P>(line_node<P>(dir, la, lb, i));
 #pragma unroll
-                for (int v = 0; v < 5; ++v) sAcc[tc][dir * 5 + v][ni] = acc[i][v];
+                for (int v = 0; v < 5; ++v) sAcc[ni + (dir * 5 + v) * P3] = acc[i][v];
             }
         }
         __syncthreads();
         if (cl < ncb) {
             const int64_t o = (int64_t)((blockIdx.x + k * G) * CPB + cl) * P3 + node;
 #pragma unroll
-            for (int v = 0; v < 5; ++v) dv.lo_buf[v * dv.nd + o] = sAcc[cl][v][node] + sAcc[cl][5 + v][node] + sAcc[cl][10 + v][node];
+            for (int v = 0; v < 5; ++v) {
+                const int a = cl * ACS + v * P3 + swz<P>(node);
+                dv.lo_buf[v * dv.nd + o] = sAcc[a] + sAcc[a + 5 * P3] + sAcc[a + 10 * P3];
+            }
         }
         // the group after next takes this group's slot; the shared arrays are reused
         if (tid < CPB) sCell[cur][tid] = after;

@@ -12,11 +12,13 @@
 // compacted troubled-cell list beside the face kernels, plus the cell-face terms, which this
 // kernel adds from its staged face values.
 //
-// R64 selects the MIXED form: the metric terms are read in FP64 (each thread rounds its node's
-// nine Ja components for the FP32 fluxes), the residual's FP32 sums are scaled by -dt/detJ in
-// FP64, and the three FP64 RK registers are combined in FP64 (update_rk4, dgsem/plens.cc:
-// 4353-4400). Without R64 (MIXED_R32) the registers hold dt*R in FP32 and the metric terms are
-// read from their FP32 images.
+// R64 selects the MIXED form: the residual's FP32 sums are scaled by -dt/detJ in FP64 (1/detJ
+// made once from the FP64 det J), and the three FP64 RK registers are combined in FP64
+// (update_rk4, dgsem/plens.cc:4353-4400). Its FP32 fluxes take the FP32 rounding of the FP64 Ja,
+// read from the image made once at context creation: the values the threads would round from
+// the FP64 array (f64_to_f32), bit for bit, with half the bytes and none of the nine conversions
+// per node. Without R64 (MIXED_R32) the registers hold dt*R in FP32 and det J is read from its
+// FP32 image as well.
 #pragma once
 
 #include <type_traits>
@@ -26,23 +28,6 @@
 
 namespace plens_gpu {
 
-// Node order of the thread-written per-node arrays at P = 4 (node n = x + 4 y + 16 z stored at
-// (x ^ z) + 4 (y ^ x) + 16 z; the identity at other degrees), with the two cells of a block 16
-// banks apart. The flux phase gives each warp one direction, its lanes the 16 lines of both
-// cells: at every position along the lines the 32 lanes then read 32 different banks in all
-// three directions, and 32 consecutive nodes of one cell (the per-node phases) do too. In the
-// plain order the x and y lines put two lanes on each bank.
-template <int P>
-__device__ __forceinline__ int swz(int n)
-{
-    if constexpr (P == 4) {
-        const int x = n & 3, y = (n >> 2) & 3, z = n >> 4;
-        return (x ^ z) | ((y ^ x) << 2) | (z << 4);
-    } else {
-        return n;
-    }
-}
-
 // Shared-memory layout of one block (bytes), all regions 16-byte aligned.
 template <int P, bool VISC, bool R64>
 struct MxSmem {
@@ -50,8 +35,8 @@ struct MxSmem {
     static constexpr int NQ = 10;  // rho, 1/rho, v0, v1, v2, p, beta, ln rho, ln beta, |v|^2
     // per-cell strides of the node quantities and partial sums (16 banks between the cells at
     // P = 4) and of the FP32 metric terms; in the MIXED form the threads write the metric terms
-    // (rounded from FP64) in the swizzled order, the MIXED_R32 form stages its FP32 images as
-    // they lie in memory
+    // (read from the FP32 image) in the swizzled order, the MIXED_R32 form stages the image as it
+    // lies in memory
     static constexpr int PAD = (P == 4) ? 16 : 0;
     static constexpr int QCS = NQ * P3 + PAD, ACS = 15 * P3 + PAD;
     static constexpr bool JSW = R64 && P == 4;
@@ -164,14 +149,15 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
         }
     }
     if (R64 && valid) {
-        // the FP32 rounding of this node's FP64 metric terms, for the FP32 fluxes (the loads are in
-        // flight while the first copy group lands; the __syncthreads below publishes them)
+        // the FP32 rounding of this node's metric terms, for the FP32 fluxes, from the image, into
+        // the swizzled order (the loads are in flight while the first copy group lands; the
+        // __syncthreads below publishes them)
         const int64_t dn = cell * P3 + node;
-        double ja[9];
+        float ja[9];
 #pragma unroll
-        for (int m = 0; m < 9; ++m) ja[m] = dv.Ja[m * dv.nd + dn];
+        for (int m = 0; m < 9; ++m) ja[m] = dv.Jaf[m * dv.nd + dn];
 #pragma unroll
-        for (int m = 0; m < 9; ++m) stJ[m * JMS + cl * JCS + jx(node)] = f64_to_f32(ja[m]);
+        for (int m = 0; m < 9; ++m) stJ[m * JMS + cl * JCS + jx(node)] = ja[m];
     }
     __syncthreads();  // barrier initialisation visible to every thread
     // the block takes one decision: a wait that ran out anywhere ends the block (error status set,
