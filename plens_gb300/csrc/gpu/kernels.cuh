@@ -888,8 +888,9 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 && P ==
     }
     const T jinv = fdiv(T(1.0), dj);
     T grad[3][5];
-#pragma unroll
-    for (int gd = 0; gd < 3; ++gd) {
+    if constexpr (sizeof(T) == 4) {
+        // FP32 (mixed forms): a face's term for direction gd is -sign Ja_gd (E_face - E) / w, the
+        // difference formed once per face and variable for the three directions
 #pragma unroll
         for (int sd = 0; sd < 3; ++sd) {
 #pragma unroll
@@ -897,27 +898,64 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, (sizeof(T) == 4 && P ==
                 if (ti[sd] != (lr ? N : 0)) continue;
                 const int f = 2 * sd + lr;
                 const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
-                const T jc = J[(sd * 3 + gd) * P3 + node];
-                const T sgn = lr ? T(-1) : T(1);
-                const T wend = opW<T>(ops, lr * N);
+                const T sw = __fdividef(lr ? 1.0f : -1.0f, opW<T>(ops, lr * N));
+                T de[5], js[3];
 #pragma unroll
-                for (int v = 0; v < 5; ++v) {
-                    const T fin = ev[v] * jc;
-                    const T fsu = sEf[((cl * 6 + f) * 5 + v) * P2 + q] * jc;
-                    acc[gd][v] -= fdiv(sgn * (fsu - fin), wend);
-                }
+                for (int v = 0; v < 5; ++v) de[v] = sEf[((cl * 6 + f) * 5 + v) * P2 + q] - ev[v];
+#pragma unroll
+                for (int gd = 0; gd < 3; ++gd) js[gd] = J[(sd * 3 + gd) * P3 + node] * sw;
+#pragma unroll
+                for (int gd = 0; gd < 3; ++gd)
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) acc[gd][v] += js[gd] * de[v];
             }
         }
 #pragma unroll
-        for (int v = 0; v < 5; ++v) grad[gd][v] = acc[gd][v] * jinv;
+        for (int gd = 0; gd < 3; ++gd)
+#pragma unroll
+            for (int v = 0; v < 5; ++v) grad[gd][v] = acc[gd][v] * jinv;
+    } else {
+        // FP64: the reference's order, -sign (F_face Ja - F_in Ja) / w (bit-level parity with the
+        // oracle in the strongly stretched wall cells, where the terms cancel)
+#pragma unroll
+        for (int gd = 0; gd < 3; ++gd) {
+#pragma unroll
+            for (int sd = 0; sd < 3; ++sd) {
+#pragma unroll
+                for (int lr = 0; lr < 2; ++lr) {
+                    if (ti[sd] != (lr ? N : 0)) continue;
+                    const int f = 2 * sd + lr;
+                    const int q = (sd == 0) ? ti[1] + P * ti[2] : (sd == 1) ? ti[0] + P * ti[2] : ti[0] + P * ti[1];
+                    const T jc = J[(sd * 3 + gd) * P3 + node];
+                    const T sgn = lr ? T(-1) : T(1);
+                    const T wend = opW<T>(ops, lr * N);
+#pragma unroll
+                    for (int v = 0; v < 5; ++v) {
+                        const T fin = ev[v] * jc;
+                        const T fsu = sEf[((cl * 6 + f) * 5 + v) * P2 + q] * jc;
+                        acc[gd][v] -= fdiv(sgn * (fsu - fin), wend);
+                    }
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < 5; ++v) grad[gd][v] = acc[gd][v] * jinv;
+        }
     }
     const int64_t dof = cell * P3 + node;
     const T* et = ev;
     T vg[3][3];
+    if constexpr (sizeof(T) == 4) {
+        const T ri = __fdividef(1.0f, et[4]);  // one reciprocal for the eighteen divisions by e4
 #pragma unroll
-    for (int vd = 0; vd < 3; ++vd)
+        for (int vd = 0; vd < 3; ++vd)
 #pragma unroll
-        for (int gd = 0; gd < 3; ++gd) vg[vd][gd] = (et[1 + vd] * grad[gd][4] / et[4] - grad[gd][1 + vd]) / et[4];
+            for (int gd = 0; gd < 3; ++gd) vg[vd][gd] = (et[1 + vd] * grad[gd][4] * ri - grad[gd][1 + vd]) * ri;
+    } else {
+#pragma unroll
+        for (int vd = 0; vd < 3; ++vd)
+#pragma unroll
+            for (int gd = 0; gd < 3; ++gd) vg[vd][gd] = (et[1 + vd] * grad[gd][4] / et[4] - grad[gd][1 + vd]) / et[4];
+    }
     const T tr = vg[0][0] + vg[1][1] + vg[2][2];
     // mu and k (NavierStokes::get_mu / get_k, h:348-360): FP64 from the FP64 state in the plain
     // form, FP32 in the mixed form
