@@ -150,14 +150,16 @@ struct Launch {
     template <bool HLLC>
     static void subcell_launch(const Dev& dv, const Ops& ops, const GasP& g, cudaStream_t st)
     {
-        // persistent grid, at most two blocks per SM: the blocks take the listed cells in groups
+        // persistent grid, at most four blocks per SM: the blocks take the listed cells in groups
+        // (against two per SM: shock-vortex 64^3 18.75 -> 18.49 ms per step, the DMR and the
+        // cylinder unchanged, A/B on the same box)
         static int blocks = 0;
         if (!blocks) {
             int dev = 0, nsm = 0, occ = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_subcell_lo<P, HLLC>, CB::THREADS, 0);
-            blocks = (occ > 2 ? 2 : (occ > 0 ? occ : 1)) * (nsm > 0 ? nsm : 1);
+            blocks = (occ > 4 ? 4 : (occ > 0 ? occ : 1)) * (nsm > 0 ? nsm : 1);
         }
         const int64_t need = (dv.nc + CB::CPB - 1) / CB::CPB;
         k_subcell_lo<P, HLLC><<<(int)(need < blocks ? need : blocks), CB::THREADS, 0, st>>>(dv, ops, g);

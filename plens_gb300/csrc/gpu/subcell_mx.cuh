@@ -72,7 +72,7 @@ static __global__ void __launch_bounds__(kSmoothThreads) k_lo_list(Dev dv)
 // after it. A group then waits for no global load; only the block's first group does. HLLC --
 // whose subcell flux does not read alpha -- has an instantiation of its own without the alpha
 // load or the scheme switch. The metric terms are read from the FP32 image both mixed forms
-// keep. The launcher caps the grid at two blocks per SM.
+// keep. The launcher caps the grid at four blocks per SM.
 template <int P, bool HLLC>
 __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Ops ops, GasP g)
 {

@@ -210,21 +210,47 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
     constexpr int TPC = L::TPC, TF = L::TF;  // line tasks per cell, threads running them
     const bool pre = L::PRE && sa.mode == 1;
     if (pre && tid >= TF) {
-        late_ok = mbar_wait0(&bars[1]);
-        late_waited = true;
-        if (late_ok) {
-            const double* R0g = sa.R0 + cell0 * P3;
-            const double* R1g = sa.R1 + cell0 * P3;
-            for (int i = tid - TF; i < ncb * P3; i += CB::THREADS - TF) {
-                stInv[i] = -stInv[i] * rhs_step(dv, cell0 + i / P3);
+        // two nodes per pass, their register values loaded before the pass waits: the first
+        // pass's loads overlap the wait for the late copy group (U and 1/detJ)
+        const double* R0g = sa.R0 + cell0 * P3;
+        const double* R1g = sa.R1 + cell0 * P3;
+        const bool r0 = sa.stage >= 3, r1 = sa.stage >= 2;
+        constexpr int NW = CB::THREADS - TF;  // threads of the spare warps
+        for (int i = tid - TF; i < ncb * P3; i += 2 * NW) {
+            const int j = i + NW;
+            const bool two = j < ncb * P3;
+            double a0[5], a1[5], b0[5], b1[5];
 #pragma unroll
-                for (int v = 0; v < 5; ++v) {
-                    double w = stU[v * NB + i];
-                    if (sa.stage >= 3) w = __fma_rn(sa.c0, R0g[v * dv.nd + i], w);
-                    if (sa.stage >= 2) w = __fma_rn(sa.c1, R1g[v * dv.nd + i], w);
-                    stU[v * NB + i] = w;
+            for (int v = 0; v < 5; ++v) {
+                a0[v] = r0 ? R0g[v * dv.nd + i] : 0.0;
+                a1[v] = r1 ? R1g[v * dv.nd + i] : 0.0;
+                b0[v] = (r0 && two) ? R0g[v * dv.nd + j] : 0.0;
+                b1[v] = (r1 && two) ? R1g[v * dv.nd + j] : 0.0;
+            }
+            if (!late_waited) {
+                late_ok = mbar_wait0(&bars[1]);
+                late_waited = true;
+            }
+            if (!late_ok) break;
+            stInv[i] = -stInv[i] * rhs_step(dv, cell0 + i / P3);
+            if (two) stInv[j] = -stInv[j] * rhs_step(dv, cell0 + j / P3);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+                double w = stU[v * NB + i];
+                if (r0) w = __fma_rn(sa.c0, a0[v], w);
+                if (r1) w = __fma_rn(sa.c1, a1[v], w);
+                stU[v * NB + i] = w;
+                if (two) {
+                    double x = stU[v * NB + j];
+                    if (r0) x = __fma_rn(sa.c0, b0[v], x);
+                    if (r1) x = __fma_rn(sa.c1, b1[v], x);
+                    stU[v * NB + j] = x;
                 }
             }
+        }
+        if (!late_waited) {
+            late_ok = mbar_wait0(&bars[1]);
+            late_waited = true;
         }
     }
     {
