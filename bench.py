@@ -39,10 +39,10 @@ METRIC = "DOF-stage updates/s: FP32+learned sensor vs FP64 plain, GB300, rho L1 
 UNIT = "DOF-stage/s"
 # Algorithmic bytes of one DOF-stage through the volume kernel, averaged over the five RK4 stages.
 # FP64 and MIXED forms: U read and written 80, two RK registers read 80 (stages 3-5; one at stage
-# 2, none at stage 1: the reference's update touches all three registers at every stage, and the
-# count keeps two reads throughout), one written 40 at stages 1-4 (the last stage's dt*R is read
-# by no later stage and is not written), Ja and detJ (the MIXED form: Ja and 1/detJ) 80:
-# 280 - 40/5 = 272. MIXED_R32 form: the registers hold dt*R in FP32 (2 x 20
+# 2, none at stage 1; the reference's update, which copies its registers down every stage
+# (dgsem/plens.cc:4353-4400), moves more, and the count keeps two reads throughout), one
+# written 40 at stages 1-4 (the last stage's dt*R is read by no later stage and is not written),
+# Ja and detJ (the MIXED form: Ja and 1/detJ) 80: 280 - 40/5 = 272. MIXED_R32 form: the registers hold dt*R in FP32 (2 x 20
 # read, 20 written at stages 1-4) and the kernel reads the FP32 images of Ja and detJ (40):
 # 80 + 40 + 16 + 40 = 176.
 BYTES_PER_DOF_STAGE = {"plain": 272, "modal": 272, "learned": 272, "learned_r32": 176}
