@@ -319,6 +319,13 @@ int plens_gpu_set_sensor_tensor_cores(plens_ctx* ctx, int enable);
  * -- the default, measured faster -- else the separable transform on the CUDA cores.
  * PLENS_GPU_E_INVALID for other contexts. */
 int plens_gpu_set_indicator_tensor_cores(plens_ctx* ctx, int enable);
+/* Compacted troubled-cell list of a mixed-precision context with the Chandrashekhar volume flux:
+ * the subcell kernel finds the cell at each list position itself, from the smoothing kernel's
+ * per-block counts and ballots (enable != 0; the default where the counts fit its shared memory,
+ * up to 1,048,448 cells), or a list kernel writes the list first (enable = 0; the form of larger
+ * meshes). Both give the same list and the same residual, bit for bit. PLENS_GPU_E_INVALID for
+ * other contexts, or enable != 0 on a larger mesh. No reference counterpart. */
+int plens_gpu_set_list_decoding(plens_ctx* ctx, int enable);
 /* Asynchronous snapshot for data output (replaces the host reads of PLENS::write,
  * dgsem/plens.cc:4170-4322): _begin copies U, alpha, alpha_d, the auxiliary variables (viscous)
  * and the clock on the context's stream into a device buffer, then to library-owned pinned host

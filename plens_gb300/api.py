@@ -182,6 +182,7 @@ def gpu_lib() -> C.CDLL:
         L.plens_gpu_snapshot_begin.argtypes = [vp]
         L.plens_gpu_set_sensor_tensor_cores.argtypes = [vp, C.c_int]
         L.plens_gpu_set_indicator_tensor_cores.argtypes = [vp, C.c_int]
+        L.plens_gpu_set_list_decoding.argtypes = [vp, C.c_int]
         L.plens_gpu_snapshot_end.argtypes = [vp, vp, vp, vp, vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(dbl)]
         L.plens_gpu_set_kernel_timing.argtypes = [vp, C.c_int]
         L.plens_gpu_setup_geometry.argtypes = [vp]
@@ -484,6 +485,11 @@ class GpuSolver:
     def set_indicator_tensor_cores(self, enable: bool):
         """Mixed form, degree 3, modal indicator: the change of basis on the tensor cores."""
         self._check(self.L.plens_gpu_set_indicator_tensor_cores(self.h, 1 if enable else 0), "set_indicator_tensor_cores")
+
+    def set_list_decoding(self, enable: bool):
+        """Mixed forms, troubled-cell list: positions decoded in the subcell kernel (the default
+        where it fits) or the list written first by a list kernel."""
+        self._check(self.L.plens_gpu_set_list_decoding(self.h, 1 if enable else 0), "set_list_decoding")
 
     def snapshot_begin(self):
         """Start an asynchronous snapshot (state, alpha, alpha_d, auxiliary variables, clock)."""

@@ -129,12 +129,16 @@ struct Dev {
     double *sf, *sf3;  // surface terms [5][nslot]
     double* avars;     // [9][nd]
     // compacted troubled-cell list of the mixed forms (ordered by cell index): lo_list[pos] =
-    // cell, lo_pos[cell] = pos or -1, *lo_count cells; lo_blk: troubled cells per smoothing block;
-    // lo_buf [5][nd]: the subcell residual sums of the listed cells at position * P^3 + node
+    // cell, *lo_count cells; lo_blk: troubled cells per 128-cell smoothing block, lo_mask: their
+    // warp ballots ([block][4]); lo_decode: 1 when the subcell kernel finds the cell at each list
+    // position from lo_blk and lo_mask itself (and writes lo_list), 0 when k_lo_list builds the
+    // list first (meshes whose block counts do not fit the subcell kernel's shared memory);
+    // lo_buf [5][nd]: the subcell residual sums of each troubled cell at its own dofs
     int32_t* lo_list;
     int32_t* lo_count;
-    int32_t* lo_pos;
     int32_t* lo_blk;
+    uint32_t* lo_mask;
+    int lo_decode;
     float* lo_buf;
     // local time stepping (null unless requested): per-cell stable step, and what multiplies
     // each cell's RHS (loc_time_steps)

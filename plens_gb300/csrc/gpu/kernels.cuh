@@ -518,7 +518,7 @@ __device__ __forceinline__ void smooth_finish(const Dev& dv, const BlendP& bp, S
     dv.alpha_d[c] = (eval_expr(dv, bp.expr_vis, x[0], x[1], x[2], s->time) > 0) ? ((1.0 < a / bp.amax) ? 1.0 : a / bp.amax) : 0.0;
 }
 
-constexpr int kSmoothThreads = 128;  // cells per block of k_alpha_smooth and k_lo_list
+constexpr int kSmoothThreads = 128;  // cells per block of k_alpha_smooth and k_lo_list (four warps)
 
 // neighbour smoothing over interior faces against the pre-smoothing values, optional TV filter
 // and alpha_d (dgsem/plens.cc:2926-2961, blender_calculator.cc:196-259); kSmoothThreads cells per
@@ -540,9 +540,11 @@ static __global__ void __launch_bounds__(kSmoothThreads) k_alpha_smooth(Dev dv, 
             a = (h > a) ? h : a;
         }
         smooth_finish(dv, bp, s, c, a);
-        troubled = a > 0;
+        troubled = stored_gt0<float>(a);  // the volume kernel's test of the stored alpha
     }
     if (dv.lo_blk) {
+        const unsigned m = __ballot_sync(0xffffffffu, troubled);
+        if ((threadIdx.x & 31) == 0) dv.lo_mask[4 * blockIdx.x + (threadIdx.x >> 5)] = m;
         const int n = __syncthreads_count(troubled ? 1 : 0);
         if (threadIdx.x == 0) dv.lo_blk[blockIdx.x] = n;
     }

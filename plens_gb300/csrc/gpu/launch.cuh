@@ -162,7 +162,14 @@ struct Launch {
             blocks = (occ > 4 ? 4 : (occ > 0 ? occ : 1)) * (nsm > 0 ? nsm : 1);
         }
         const int64_t need = (dv.nc + CB::CPB - 1) / CB::CPB;
-        k_subcell_lo<P, HLLC><<<(int)(need < blocks ? need : blocks), CB::THREADS, 0, st>>>(dv, ops, g);
+        // decoding: the prefix sums of the smoothing blocks' counts in dynamic shared memory
+        const int bytes = dv.lo_decode ? (int)(4 * ((dv.nc + kSmoothThreads - 1) / kSmoothThreads + 1)) : 0;
+        static int attr = 0;
+        if (bytes > attr) {
+            cudaFuncSetAttribute(k_subcell_lo<P, HLLC>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            attr = bytes;
+        }
+        k_subcell_lo<P, HLLC><<<(int)(need < blocks ? need : blocks), CB::THREADS, bytes, st>>>(dv, ops, g);
     }
     static int subcell(const Dev& dv, const Ops& ops, const GasP& g, cudaStream_t st)
     {

@@ -310,7 +310,7 @@ int launch_rhs(plens_ctx* c, const StageArgs& sa)
         k_alpha_smooth<<<(unsigned)((c->nc + kSmoothThreads - 1) / kSmoothThreads), kSmoothThreads, 0, c->side>>>(c->dv, c->bp);
         ++c->launches;
     }
-    if (c->dv.lo_blk) {  // the compacted troubled-cell list from the smoothing's block counts
+    if (c->dv.lo_blk && !c->dv.lo_decode) {  // the list, where the subcell kernel does not decode it
         k_lo_list<<<(unsigned)((c->nc + kSmoothThreads - 1) / kSmoothThreads), kSmoothThreads, 0, c->side>>>(c->dv);
         ++c->launches;
     }
@@ -757,11 +757,15 @@ int plens_gpu_create(const plens_mesh_desc* mesh, const plens_params* prm, plens
     if (c->mixed && c->tab.uses_lo_list(c->gas)) {
         // the compacted troubled-cell list and the subcell sums of the listed cells
         const int64_t nblk = (nc + kSmoothThreads - 1) / kSmoothThreads;
-        if ((r = dalloc(c, &d.lo_list, nc)) || (r = dalloc(c, &d.lo_count, 1)) || (r = dalloc(c, &d.lo_pos, nc)) ||
-            (r = dalloc(c, &d.lo_blk, nblk)) || (r = dalloc(c, &d.lo_buf, 5 * nd)))
+        if ((r = dalloc(c, &d.lo_list, nc)) || (r = dalloc(c, &d.lo_count, 1)) || (r = dalloc(c, &d.lo_blk, nblk)) ||
+            (r = dalloc(c, &d.lo_mask, 4 * nblk)) || (r = dalloc(c, &d.lo_buf, 5 * nd)))
             return r;
         CK(cudaMemset(d.lo_count, 0, sizeof(int32_t)));
-        CK(cudaMemset(d.lo_pos, 0xff, sizeof(int32_t) * nc));
+        CK(cudaMemset(d.lo_list, 0, sizeof(int32_t) * nc));
+        // the subcell kernel finds each list position's cell itself while the smoothing blocks'
+        // prefix sums fit 32 KB of its shared memory (up to 1,048,448 cells); larger meshes take
+        // k_lo_list first
+        d.lo_decode = (nblk + 1 <= kLoDecodeMaxBlocks) ? 1 : 0;
     }
     if (c->learned) {
         if ((r = mlp_create(c->mlp, nc, c->allocs))) return fail(c, PLENS_GPU_E_CUDA, "mlp buffers");
@@ -1247,7 +1251,7 @@ int plens_gpu_get_cell_scalars(plens_ctx* c, double* alpha, double* alpha_d, dou
 int plens_gpu_troubled_cells(plens_ctx* c, int32_t* cells, int64_t* count)
 {
     if (!c || !count) return PLENS_GPU_E_INVALID;
-    if (!c->dv.lo_pos) return fail(c, PLENS_GPU_E_INVALID, "this context has no compacted troubled-cell list");
+    if (!c->dv.lo_list) return fail(c, PLENS_GPU_E_INVALID, "this context has no compacted troubled-cell list");
     CK(cudaStreamSynchronize(c->stream));
     int32_t n = 0;
     CK(cudaMemcpy(&n, c->dv.lo_count, sizeof(n), cudaMemcpyDeviceToHost));
@@ -1355,6 +1359,22 @@ int plens_gpu_set_indicator_tensor_cores(plens_ctx* c, int enable)
     if (int r = sync_and_check(c)) return r;
     c->indicator_tc = enable != 0;
     for (auto& gx : c->step_graph)  // the step's launch sequence changed
+        if (gx) {
+            cudaGraphExecDestroy(gx);
+            gx = nullptr;
+        }
+    return 0;
+}
+
+int plens_gpu_set_list_decoding(plens_ctx* c, int enable)
+{
+    if (!c) return PLENS_GPU_E_INVALID;
+    if (!c->dv.lo_blk) return fail(c, PLENS_GPU_E_INVALID, "this context has no compacted troubled-cell list");
+    if (enable && (c->nc + kSmoothThreads - 1) / kSmoothThreads + 1 > kLoDecodeMaxBlocks)
+        return fail(c, PLENS_GPU_E_INVALID, "the mesh's block counts do not fit the subcell kernel's shared memory");
+    if (int r = sync_and_check(c)) return r;
+    c->dv.lo_decode = enable ? 1 : 0;
+    for (auto& gx : c->step_graph)  // the step's launch sequence and kernel arguments changed
         if (gx) {
             cudaGraphExecDestroy(gx);
             gx = nullptr;

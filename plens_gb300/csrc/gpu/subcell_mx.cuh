@@ -2,24 +2,29 @@
 // list: calc_cell_lo_inv_residual (dgsem/plens.cc:3469-3583) for the cells with alpha > 0 only,
 // in a kernel of its own on the indicator stream, beside the face kernels.
 //
-// The list is ordered by cell index and built without atomics: the smoothing kernel counts each
-// block's troubled cells (k_alpha_smooth, 128 cells per block), k_lo_list gives every block its
-// offset (the sum of the counts of the blocks before it) and every troubled cell its rank within
-// the block (warp ballots), so the list and each cell's position lo_pos are the same on every run.
-// k_subcell_lo then runs the subcell interfaces inside each listed cell (the line tasks' P - 1
-// interior fluxes) and writes the cell's unscaled sums of the three directions to
-// lo_buf[var][position * P^3 + node]. It needs the state, the metric terms and alpha only; the
-// cell-face terms of the first-order residual (the inviscid face flux x |Ja| / w at the nodes on
-// the cell's faces, plens.cc:3544-3575) need this stage's face fluxes and are added by the volume
-// kernel, which has them staged.
+// The list is ordered by cell index and built without atomics, the same on every run. The
+// smoothing kernel (k_alpha_smooth, 128 cells per block) writes each block's troubled-cell count
+// and its four warp ballots. k_subcell_lo then finds the cell at each list position itself: every
+// block takes the prefix sums of the counts into shared memory, and a position maps to its
+// smoothing block by a binary search there and to its cell by the rank among the block's ballot
+// bits. (Meshes whose counts do not fit there take k_lo_list first, which writes the list from
+// the same counts and ballots.) It runs the subcell interfaces inside each listed cell (the line
+// tasks' P - 1 interior fluxes) and writes the cell's unscaled sums of the three directions to
+// lo_buf[var][cell dofs]. It needs the state, the metric terms and alpha only; the cell-face terms
+// of the first-order residual (the inviscid face flux x |Ja| / w at the nodes on the cell's faces,
+// plens.cc:3544-3575) need this stage's face fluxes and are added by the volume kernel, which has
+// them staged.
 #pragma once
 
 #include "kernels.cuh"
 
 namespace plens_gpu {
 
-// positions of the troubled cells: lo_list[pos] = cell, lo_pos[cell] = pos (-1 if alpha = 0),
-// *lo_count = number of troubled cells
+// the most smoothing-block prefix sums (ints, 32 KB) the subcell kernel takes into shared memory
+constexpr int kLoDecodeMaxBlocks = 8192;
+
+// The troubled cells in cell order, lo_list[pos] = cell, and *lo_count, from the smoothing
+// kernel's block counts and ballots (meshes whose counts do not fit k_subcell_lo's shared memory)
 static __global__ void __launch_bounds__(kSmoothThreads) k_lo_list(Dev dv)
 {
     Scalars* s = dv.sc;
@@ -42,25 +47,40 @@ static __global__ void __launch_bounds__(kSmoothThreads) k_lo_list(Dev dv)
     }
     __syncthreads();
     const int64_t c = (int64_t)b * kSmoothThreads + tid;
-    // the smoothing kernel's predicate on the stored value (alpha > 0)
-    const bool flag = c < dv.nc && dv.alpha[c] > 0;
-    const unsigned m = __ballot_sync(0xffffffffu, flag);
-    const int rank = __popc(m & ((1u << lane) - 1u));
-    __syncthreads();  // s_part is reused for the warp counts
-    if (lane == 0) s_part[warp] = __popc(m);
-    __syncthreads();
+    const unsigned m = dv.lo_mask[4 * b + warp];
+    const bool flag = (m >> lane) & 1u;
     int wofs = 0;
-    for (int w = 0; w < warp; ++w) wofs += s_part[w];
-    const int pos = s_off + wofs + rank;
-    if (c < dv.nc) {
-        dv.lo_pos[c] = flag ? pos : -1;
-        if (flag) dv.lo_list[pos] = (int32_t)c;
+    for (int w = 0; w < warp; ++w) wofs += __popc(dv.lo_mask[4 * b + w]);
+    const int pos = s_off + wofs + __popc(m & ((1u << lane) - 1u));
+    if (flag && c < dv.nc) dv.lo_list[pos] = (int32_t)c;
+    if (b == (int)gridDim.x - 1 && tid == 0) *dv.lo_count = s_off + dv.lo_blk[b];
+}
+
+// list position p -> cell, from the exclusive prefix sums pre[0..nblk] of the smoothing blocks'
+// troubled-cell counts (pre[nblk] = the list's length) and their ballots: the block is the last
+// one whose prefix does not exceed p, the cell the (p - prefix)-th set bit of its ballots
+__device__ __forceinline__ int32_t lo_decode(int p, const int* pre, int nblk, const uint32_t* mask)
+{
+    int lo = 0, hi = nblk;  // pre[lo] <= p < pre[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (pre[mid] <= p) lo = mid;
+        else hi = mid;
     }
-    if (b == (int)gridDim.x - 1 && tid == 0) {
-        int t = s_off;
-        for (int w = 0; w < kSmoothThreads / 32; ++w) t += s_part[w];
-        *dv.lo_count = t;
+    int r = p - pre[lo];
+    const uint4 m4 = reinterpret_cast<const uint4*>(mask)[lo];
+    const unsigned w[4] = {m4.x, m4.y, m4.z, m4.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int cnt = __popc(w[k]);
+        if (r < cnt) {
+            unsigned x = w[k];
+            for (int i = 0; i < r; ++i) x &= x - 1u;  // clear the r lowest set bits
+            return (int32_t)(lo * kSmoothThreads + 32 * k + (__ffs(x) - 1));
+        }
+        r -= cnt;
     }
+    return -1;
 }
 
 // Interior subcell sums of the listed cells, CPB cells per block, one thread per GLL node; line
@@ -86,22 +106,66 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
     __shared__ float sAcc[CPB * ACS];  // partial sum k of node n of cell c at [c ACS + k P3 + swz(n)]
     __shared__ float sAl[CPB];
     __shared__ int32_t sCell[2][CPB];  // cells of this group and of the block's next group
+    __shared__ int sW[CB::THREADS / 32];
+    extern __shared__ int sPre[];  // decoding: [nblk + 1] prefix sums of the block counts
     Scalars* s = dv.sc;
     if (!s->active) return;
-    const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3;
+    const int tid = threadIdx.x, cl = tid / P3, node = tid - cl * P3, lane = tid & 31, warp = tid >> 5;
     const float gm = f64_to_f32(g.gamma);
     const int G = gridDim.x;
     const float* Ja = dv.Jaf;
-    // the list: count and the first two groups' entries (entries past the count are not used)
-    int n = 0;
-    if (tid < CPB) {
-        n = *dv.lo_count;
+    const bool decode = dv.lo_decode != 0;
+    const int nblk = (int)((dv.nc + kSmoothThreads - 1) / kSmoothThreads);
+    int n = 0;  // the list's length
+    if (decode) {
+        // the exclusive prefix sums of the smoothing blocks' counts: each thread scans a chunk,
+        // the chunk sums are scanned across the block, the chunks are rewritten with offsets
+        for (int i = tid; i < nblk; i += CB::THREADS) sPre[i] = dv.lo_blk[i];
+        __syncthreads();
+        const int chunk = (nblk + CB::THREADS - 1) / CB::THREADS;
+        const int b0 = tid * chunk, b1 = (b0 + chunk < nblk) ? b0 + chunk : nblk;
+        int sum = 0;
+        for (int i = b0; i < b1; ++i) sum += sPre[i];
+        int x = sum;
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const int p = (blockIdx.x + j * G) * CPB + tid;
-            const int32_t c = (p < dv.nc) ? dv.lo_list[p] : -1;
-            sCell[j][tid] = (p < n) ? c : -1;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
+        if (lane == 31) sW[warp] = x;
+        __syncthreads();
+        int run = x - sum, total = 0;
+        for (int w = 0; w < CB::THREADS / 32; ++w) {
+            if (w < warp) run += sW[w];
+            total += sW[w];
+        }
+        for (int i = b0; i < b1; ++i) {
+            const int v = sPre[i];
+            sPre[i] = run;
+            run += v;
+        }
+        if (tid == 0) sPre[nblk] = total;
+        __syncthreads();
+        n = total;
+        if (blockIdx.x == 0 && tid == 0) *dv.lo_count = n;
+    } else if (tid < CPB) {
+        n = *dv.lo_count;
+    }
+    // the cell at list position p (-1 past the end); decoding also writes the list entry
+    auto entry = [&](int p) -> int32_t {
+        if (decode) {
+            if (p >= n) return -1;
+            const int32_t c = lo_decode(p, sPre, nblk, dv.lo_mask);
+            dv.lo_list[p] = c;
+            return c;
+        }
+        const int32_t c = (p < dv.nc) ? dv.lo_list[p] : -1;
+        return (p < n) ? c : -1;
+    };
+    // the first two groups' cells
+    if (tid < CPB) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) sCell[j][tid] = entry((blockIdx.x + j * G) * CPB + tid);
     }
     __syncthreads();
     if (sCell[0][0] < 0) return;  // the list ends before this block's first group
@@ -124,6 +188,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
             while (q < CPB && sCell[cur][q] >= 0) ++q;
             return q;
         }();
+        const int32_t mycell = (cl < ncb) ? sCell[cur][cl] : -1;  // this thread's cell of the group
         // this group's node values, fetched during the previous group
         if (cl < ncb) {
             const int bn = cl * CS + swz<P>(node);
@@ -138,9 +203,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
         int32_t after = -1;
         if (cl < CPB) fetch(sCell[cur ^ 1][cl]);
         if (tid < CPB) {
-            const int p = (blockIdx.x + (k + 2) * G) * CPB + tid;
-            const int32_t c = (p < dv.nc) ? dv.lo_list[p] : -1;
-            after = (p < n) ? c : -1;
+            after = entry((blockIdx.x + (k + 2) * G) * CPB + tid);
             if (!HLLC && sCell[cur ^ 1][tid] >= 0) pa = f64_to_f32(dv.alpha[sCell[cur ^ 1][tid]]);
         }
         for (int ft = tid; ft < CPB * TPC; ft += CB::THREADS) {
@@ -205,7 +268,7 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS) k_subcell_lo(Dev dv, Op
         }
         __syncthreads();
         if (cl < ncb) {
-            const int64_t o = (int64_t)((blockIdx.x + k * G) * CPB + cl) * P3 + node;
+            const int64_t o = (int64_t)mycell * P3 + node;  // the cell's own dofs
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
                 const int a = cl * ACS + v * P3 + swz<P>(node);

@@ -435,16 +435,15 @@ __global__ void __launch_bounds__(CellBlock<P>::THREADS, vol_mx_min_blocks<P, R6
     }
 
     // ---- phase C: first-order subcell residual, only where alpha > 0: the interior sums
-    // k_subcell_lo wrote for this cell's place in the compacted troubled-cell list, plus the
-    // cell-face terms at the nodes on the cell's faces: this stage's face flux x |Ja| / w
-    // (contribution sign x flux sign = +1, calc_cell_lo_inv_residual, dgsem/plens.cc:3544-3575)
+    // k_subcell_lo wrote at this cell's dofs (it takes every cell of the list, the cells whose
+    // stored alpha passes this same test), plus the cell-face terms at the nodes on the cell's
+    // faces: this stage's face flux x |Ja| / w (contribution sign x flux sign = +1,
+    // calc_cell_lo_inv_residual, dgsem/plens.cc:3544-3575)
     float lo[5] = {0, 0, 0, 0, 0};
     if (valid && stored_gt0<float>(alpha)) {
-        const int32_t pos = dv.lo_pos[cell];
-        if (pos >= 0) {
-            const int64_t o = (int64_t)pos * P3 + node;
+        {
 #pragma unroll
-            for (int v = 0; v < 5; ++v) lo[v] = dv.lo_buf[v * dv.nd + o];
+            for (int v = 0; v < 5; ++v) lo[v] = dv.lo_buf[v * dv.nd + dof];
             const float* sfa = stSf + cl * 6 * P2;
 #pragma unroll
             for (int sd = 0; sd < 3; ++sd) {

@@ -62,3 +62,44 @@ def test_fp64_context_has_no_list():
     g.rhs()
     with pytest.raises(PlensError):
         g.troubled_cells()
+
+
+def _long_list(spec):
+    """The DMR with the blender threshold factor at 1e-6 and pre-shock noise at 1e-3: about 90%
+    of the cells troubled, so every block of the subcell kernel's grid takes several groups."""
+    prm, files, deg = spec
+    key = "    set wall blender limit = 0\n"
+    assert key in prm
+    return prm.replace(key, key + "    set threshold factor = 1e-6\n"), files, deg
+
+
+@pytest.mark.parametrize("prec,sensor,long", [("mixed", "modal", False), ("mixed", "modal", True),
+                                              ("mixed", "learned", True), ("mixed_r32", "modal", True)])
+def test_list_decoding_and_list_kernel_agree(prec, sensor, long):
+    """The two forms of the list: the subcell kernel decoding each position's cell from the
+    smoothing kernel's block counts and ballots (the default), and the list kernel writing the
+    list first (the form of meshes above 1,048,448 cells). The same list and the same RHS, bit
+    for bit, and the same state after five steps."""
+    spec = configs.dmr(nx=120, ny=30, noise=1e-3, precision=prec, sensor=sensor)
+    case = make(_long_list(spec) if long else spec)
+    out = []
+    for decode in (True, False):
+        g = GpuSolver(case)
+        if sensor == "learned":
+            g.set_sensor_weights(_weights())
+        g.set_list_decoding(decode)
+        g.set_state(case.initial_state(), case.start_time)
+        g.advance(2)
+        R = g.rhs()
+        lst = g.troubled_cells()
+        g.advance(5)
+        out.append((R, lst, g.get_state()))
+        g.close()
+    (Ra, la, Ua), (Rb, lb, Ub) = out
+    print(f"{len(la)} listed cells")
+    assert len(la) > 0
+    if long:
+        assert len(la) > 2 * 4 * 152 * 2
+    assert np.array_equal(la, lb)
+    assert np.array_equal(Ra, Rb)
+    assert np.array_equal(Ua, Ub)
